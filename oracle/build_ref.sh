@@ -1,0 +1,30 @@
+#!/bin/bash
+# Builds the reference's own CPU path (its OpenMP branch, no -DGPU) straight from
+# the reference sources, plus oracle/ref_harness.cu, into oracle/_ref/libg3lref.so.
+#
+# The sources are compiled where they lie (G3L_REF_SRC, default
+# /root/reference/src); nothing is copied.  -ffp-contract=off keeps the host
+# arithmetic free of fused multiply-adds on every platform, so the build and the
+# oracle restatement evaluate the same IEEE operations.
+set -euo pipefail
+REF=${G3L_REF_SRC:-/root/reference/src}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+if [ ! -f "$REF/NNMap_Model.cu" ]; then
+    echo "reference sources not found at $REF" >&2
+    exit 2
+fi
+mkdir -p "$OUT/obj"
+CXXF="-std=c++17 -O2 -fopenmp -fPIC -ffp-contract=off -I$REF"
+NVF="-std=c++17 -O3 -rdc=true -Xcompiler -fopenmp,-fPIC,-ffp-contract=off -I$REF"
+pids=()
+for f in hcubature Cosmology Params; do
+    g++ $CXXF -c "$REF/$f.cpp" -o "$OUT/obj/$f.o" & pids+=($!)
+done
+for f in HOD generalFunctions NNMap_Model NMapMap_Model; do
+    nvcc $NVF -c "$REF/$f.cu" -o "$OUT/obj/$f.o" 2> "$OUT/obj/$f.log" & pids+=($!)
+done
+nvcc $NVF -c "$HERE/ref_harness.cu" -o "$OUT/obj/ref_harness.o" & pids+=($!)
+for p in "${pids[@]}"; do wait "$p"; done
+nvcc -shared -rdc=true -Xcompiler -fopenmp "$OUT"/obj/*.o -o "$OUT/libg3lref.so"
+echo "built $OUT/libg3lref.so"

@@ -1,0 +1,136 @@
+"""Generate the golden vectors in tests/golden/ from the reference's own CPU build.
+
+Run from the repository root where the reference sources exist:
+    python tests/golden/make_golden.py
+It builds oracle/_ref/libg3lref.so (oracle/build_ref.sh) from the reference's
+unmodified sources, drives NNMap_Model / NMapMap_Model / hcubature_v in memory
+through oracle/ref_harness.cu, and writes tests/golden/ref_n64.npz.  The tables
+the vectors were computed on are stored in the same file, so the fixture does
+not depend on the table generator being bit-identical across platforms.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from g3lhalo_gb300 import workloads as W  # noqa: E402
+from g3lhalo_gb300.tables import make_tables  # noqa: E402
+import pyoracle as P  # noqa: E402
+
+OUT = os.path.join(ROOT, "tests", "golden", "ref_n64.npz")
+
+# analytic integrands for the engine-only vectors (Genz test families)
+def genz_gauss(x):
+    a = np.array([3.0, 2.0, 5.0, 1.5, 4.0, 2.5, 3.5])[: x.shape[1]]
+    u = np.array([0.3, 0.6, 0.45, 0.7, 0.2, 0.55, 0.4])[: x.shape[1]]
+    return np.exp(-np.sum(a * a * (x - u) ** 2, axis=1))
+
+
+def genz_osc(x):
+    a = np.array([2.0, 1.0, 3.0, 1.5, 2.5, 0.5, 1.2])[: x.shape[1]]
+    return np.cos(2 * np.pi * 0.3 + x @ a)
+
+
+def genz_corner(x):
+    a = np.array([1.0, 2.0, 0.5, 1.5, 1.0, 0.7, 1.1])[: x.shape[1]]
+    return (1.0 + x @ a) ** (-(x.shape[1] + 1))
+
+
+ENGINE_CASES = [  # (name, dim, maxEval, rtol)
+    ("gauss", 1, 0, 1e-10), ("gauss", 2, 20000, 1e-8), ("gauss", 5, 40000, 1e-6),
+    ("osc", 3, 30000, 1e-9), ("osc", 7, 60000, 1e-6), ("corner", 4, 40000, 1e-7),
+    ("corner", 6, 50000, 1e-7), ("osc", 1, 0, 1e-12),
+]
+FUNCS = {"gauss": genz_gauss, "osc": genz_osc, "corner": genz_corner}
+
+
+def main():
+    P.build_ref()
+    T = make_tables(Nz=64, Nm=64, Nk=64, kmax_h=1e7 / 0.7)
+    h1, h2 = W.hod_default(), W.hod_second()
+    out = {f"tab_{k}": v for k, v in T.arrays().items()}
+    out["tab_meta"] = np.array([T.Nz, T.Nm, T.Nk, T.zmin, T.zmax, T.mmin, T.mmax, T.kmin, T.kmax])
+    out["cosmo"] = T.cosmo.as_array()
+    out["hod1"], out["hod2"] = h1, h2
+
+    rng = np.random.default_rng(20261203)
+    trip = W.triplets_all()
+    thetas = np.array([trip[0], trip[57], trip[219], W.triplets_equal((1.0,))[0]])
+    out["thetas"] = thetas
+
+    # --- NNMap model, two populations ---
+    R = P.RefBuild(T, h1, h2, kind=0)
+    O = P.Oracle(T, h1, h2, clamp_k=False)
+    rho, n1, n2 = R.densities()
+    out["nn_rho_bar"], out["nn_nbar1"], out["nn_nbar2"] = rho, n1, n2
+    for term in (1, 2, 3):
+        lo, hi = O.bounds(term)
+        x = rng.uniform(lo, hi, size=(48, len(lo)))
+        pts = x.copy()
+        pts[:, :2] = 10 ** pts[:, :2]
+        pts[:, 3:-1] = 10 ** pts[:, 3:-1]
+        vals = np.array([[R.kernel(term, thetas[1], p, t1, t2) for (t1, t2) in
+                          ((1, 2), (1, 1), (2, 2))] for p in pts])
+        out[f"nn_pts_t{term}"] = pts
+        out[f"nn_kernel_t{term}"] = vals
+    rows = []
+    for it, th in enumerate(thetas):
+        for term in (1, 2, 3):
+            for (t1, t2) in ((1, 2), (1, 1)):
+                v, e, n = R.term(term, th, t1, t2, maxEval=60000, rtol=1e-4)
+                rows.append([it, term, t1, t2, 60000, v, e, n])
+    out["nn_terms"] = np.array(rows, dtype=np.float64)
+    stock = [[term, R.method(term, thetas[1], 1, 2)] for term in (1, 2, 3)]
+    out["nn_stock"] = np.array(stock)
+    R.close()
+
+    # --- NNMap model with one HOD object in both slots ---
+    R = P.RefBuild(T, h1, None, kind=0)
+    rows = []
+    for term in (1, 2, 3):
+        v, e, n = R.term(term, thetas[2], 1, 2, maxEval=40000, rtol=1e-4)
+        rows.append([2, term, 1, 2, 40000, v, e, n])
+    out["nn_same_terms"] = np.array(rows, dtype=np.float64)
+    R.close()
+
+    # --- NMapMap model ---
+    R = P.RefBuild(T, h2, None, kind=1)
+    rho, nb, _ = R.densities()
+    out["nm_rho_bar"], out["nm_nbar"] = rho, nb
+    for term in (1, 2, 3):
+        lo, hi = O.bounds(term)
+        x = rng.uniform(lo, hi, size=(48, len(lo)))
+        pts = x.copy()
+        pts[:, :2] = 10 ** pts[:, :2]
+        pts[:, 3:-1] = 10 ** pts[:, 3:-1]
+        out[f"nm_pts_t{term}"] = pts
+        out[f"nm_kernel_t{term}"] = np.array([R.kernel(term, thetas[0], p) for p in pts])
+    rows = []
+    for it, th in enumerate(thetas[:3]):
+        for term in (1, 2, 3):
+            v, e, n = R.term(term, th, maxEval=60000, rtol=1e-4)
+            rows.append([it, term, 0, 0, 60000, v, e, n])
+    out["nm_terms"] = np.array(rows, dtype=np.float64)
+    out["nm_stock"] = np.array([[1, R.method(1, thetas[0])]])
+    R.close()
+
+    # --- engine-only vectors on analytic integrands ---
+    rows = []
+    for ci, (name, dim, me, rtol) in enumerate(ENGINE_CASES):
+        v, e, n = P.oracle_hcubature(FUNCS[name], dim, np.zeros(dim), np.ones(dim), me, rtol,
+                                     use_ref=True)
+        rows.append([ci, dim, me, rtol, v, e, n])
+    out["engine"] = np.array(rows)
+
+    np.savez_compressed(OUT, **out)
+    print("wrote", OUT, os.path.getsize(OUT), "bytes")
+
+
+if __name__ == "__main__":
+    main()
