@@ -1,0 +1,352 @@
+"""Python front-end of libg3lgpu.so (ctypes over the C ABI in include/g3l_gpu.h).
+
+This module mirrors the reference's model interface for the hot path:
+
+* ``NNMapModel``   ~ g3lhalo::NNMap_Model   (src/NNMap_Model.h:124-241)
+* ``NMapMapModel`` ~ g3lhalo::NMapMap_Model (src/NMapMap_Model.h:115-168)
+
+with the per-term methods ``NNMap_1h/2h/3h``, ``NNMap`` and ``calculateAll``,
+plus batched forms that integrate many (triplet, term) pairs in one launch.
+Every computation runs in the CUDA library; there is no CPU fallback: if the
+library cannot be loaded or no GPU is present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+FP64 = 0
+MIXED = 1
+NNMAP = 0
+NMAPMAP = 1
+
+STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "POOL", 5: "NONFINITE",
+          6: "CANCELLED", 7: "ROUNDS", 8: "NO_DEVICE", 9: "BUSY"}
+
+_dp = C.POINTER(C.c_double)
+
+
+class Tables(C.Structure):
+    _fields_ = [("Nz", C.c_int), ("Nm", C.c_int), ("Nk", C.c_int),
+                ("zmin", C.c_double), ("zmax", C.c_double), ("mmin", C.c_double),
+                ("mmax", C.c_double), ("kmin", C.c_double), ("kmax", C.c_double),
+                ("g", _dp), ("p_lens1", _dp), ("p_lens2", _dp), ("w", _dp), ("dwdz", _dp),
+                ("hmf", _dp), ("b_h", _dp), ("conc", _dp), ("P_lin", _dp),
+                ("Om", C.c_double), ("OL", C.c_double), ("Ob", C.c_double),
+                ("sigma8", C.c_double), ("H0", C.c_double), ("ns", C.c_double),
+                ("clamp_k", C.c_int)]
+
+
+class Integral(C.Structure):
+    _fields_ = [("kind", C.c_int), ("term", C.c_int), ("hod1", C.c_int), ("hod2", C.c_int),
+                ("theta", C.c_double * 3), ("rtol", C.c_double), ("max_eval", C.c_uint64)]
+
+
+class Result(C.Structure):
+    _fields_ = [("val", C.c_double), ("err", C.c_double), ("result", C.c_double),
+                ("neval", C.c_uint64), ("status", C.c_int32), ("rounds", C.c_int32)]
+
+
+class Options(C.Structure):
+    _fields_ = [("eval_blocks_per_sm", C.c_int), ("eval_warps_per_block", C.c_int),
+                ("use_graph", C.c_int), ("max_rounds", C.c_int), ("unlimited_pool", C.c_uint64)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("kernel_launches", C.c_uint64), ("rounds", C.c_uint64),
+                ("regions_evaluated", C.c_uint64), ("points_evaluated", C.c_uint64),
+                ("tie_fallbacks", C.c_uint64), ("small_arg_fp64", C.c_uint64),
+                ("device_ms", C.c_double), ("eval_ms", C.c_double)]
+
+
+INTEGRAND_V = C.CFUNCTYPE(C.c_int, C.c_uint, C.c_size_t, _dp, C.c_void_p, C.c_uint, _dp)
+
+_lib = None
+_lock = threading.Lock()
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Load libg3lgpu.so, building it first if it is missing or stale."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            L = C.CDLL(path)
+            L.g3l_ctx_create.argtypes = [C.POINTER(Tables), C.c_int, C.POINTER(C.c_void_p)]
+            L.g3l_ctx_destroy.argtypes = [C.c_void_p]
+            L.g3l_set_hod.argtypes = [C.c_void_p, C.c_int, _dp]
+            L.g3l_set_correlation.argtypes = [C.c_void_p, C.c_double, C.c_double]
+            L.g3l_get_densities.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
+            L.g3l_eval.argtypes = [C.c_void_p, C.POINTER(Integral), C.c_int, C.c_int,
+                                   C.POINTER(Result)]
+            L.g3l_submit.argtypes = [C.c_void_p, C.POINTER(Integral), C.c_int, C.c_int,
+                                     C.POINTER(C.c_int64)]
+            L.g3l_poll.argtypes = [C.c_void_p, C.c_int64, C.POINTER(Result), C.c_int]
+            L.g3l_cancel.argtypes = [C.c_void_p, C.c_int64]
+            L.g3l_get_options.argtypes = [C.c_void_p, C.POINTER(Options)]
+            L.g3l_set_options.argtypes = [C.c_void_p, C.POINTER(Options)]
+            L.g3l_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
+            L.g3l_last_error.restype = C.c_char_p
+            L.g3l_host_densities.argtypes = [C.POINTER(Tables), _dp, _dp, _dp]
+            L.g3l_hcubature_v.argtypes = [C.c_uint, C.c_void_p, C.c_void_p, C.c_uint, _dp, _dp,
+                                          C.c_size_t, C.c_double, C.c_double, C.c_int, _dp, _dp]
+            _lib = L
+    return _lib
+
+
+class G3LError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (%s): %s" % (STATUS.get(status, status), status, msg))
+        self.status = status
+
+
+def _check(st):
+    if st != 0:
+        raise G3LError(st, lib().g3l_last_error().decode(errors="replace"))
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def make_ctables(t, clamp_k=True):
+    """C table struct from a tables.Tables; returns (struct, keep-alive arrays)."""
+    keep = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in t.arrays().items()}
+    c = t.cosmo
+    ct = Tables(Nz=t.Nz, Nm=t.Nm, Nk=t.Nk, zmin=t.zmin, zmax=t.zmax, mmin=t.mmin, mmax=t.mmax,
+                kmin=t.kmin, kmax=t.kmax, g=_ptr(keep["g"]), p_lens1=_ptr(keep["p_lens1"]),
+                p_lens2=_ptr(keep["p_lens2"]), w=_ptr(keep["w"]), dwdz=_ptr(keep["dwdz"]),
+                hmf=_ptr(keep["hmf"]), b_h=_ptr(keep["b_h"]), conc=_ptr(keep["conc"]),
+                P_lin=_ptr(keep["P_lin"]), Om=c.Om, OL=c.OL, Ob=c.Ob, sigma8=c.s8, H0=c.H0,
+                ns=c.ns, clamp_k=1 if clamp_k else 0)
+    return ct, keep
+
+
+def host_densities(tables, hod):
+    """rho_bar(z), n_bar(z) of one HOD with the library's host integrator (no GPU needed)."""
+    ct, keep = make_ctables(tables)
+    rho = np.zeros(tables.Nz)
+    nb = np.zeros(tables.Nz)
+    h = np.ascontiguousarray(hod, dtype=np.float64)
+    _check(lib().g3l_host_densities(C.byref(ct), _ptr(h), _ptr(rho), _ptr(nb)))
+    return rho, nb
+
+
+def hcubature_v(f, dim, xmin, xmax, max_eval=0, rtol=1e-4, reqabs=0.0):
+    """The library's host hcubature_v with a Python vectorised integrand f(x[n, dim])."""
+    def cb(ndim, npt, x, fdata, fdim, fval):
+        xs = np.ctypeslib.as_array(x, shape=(npt * ndim,)).reshape(npt, ndim)
+        np.ctypeslib.as_array(fval, shape=(npt,))[:] = f(xs)
+        return 0
+    cf = INTEGRAND_V(cb)
+    lo = np.ascontiguousarray(xmin, dtype=np.float64)
+    hi = np.ascontiguousarray(xmax, dtype=np.float64)
+    val, err = C.c_double(), C.c_double()
+    st = lib().g3l_hcubature_v(1, C.cast(cf, C.c_void_p), None, dim, _ptr(lo), _ptr(hi),
+                               max_eval, reqabs, rtol, 0, C.byref(val), C.byref(err))
+    _check(st)
+    return val.value, err.value
+
+
+class Context:
+    """Device-resident tables plus HOD slots; one CUDA stream."""
+
+    def __init__(self, tables, device=0, clamp_k=True):
+        L = lib()
+        self._ct, self._keep = make_ctables(tables, clamp_k)
+        h = C.c_void_p()
+        _check(L.g3l_ctx_create(C.byref(self._ct), device, C.byref(h)))
+        self.h = h
+        self.tables = tables
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().g3l_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_hod(self, slot, params):
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        _check(lib().g3l_set_hod(self.h, slot, _ptr(p)))
+
+    def set_correlation(self, A, eps):
+        _check(lib().g3l_set_correlation(self.h, A, eps))
+
+    def densities(self, slot):
+        rho = np.zeros(self.tables.Nz)
+        nb = np.zeros(self.tables.Nz)
+        _check(lib().g3l_get_densities(self.h, slot, _ptr(rho), _ptr(nb)))
+        return rho, nb
+
+    def options(self):
+        o = Options()
+        _check(lib().g3l_get_options(self.h, C.byref(o)))
+        return o
+
+    def set_options(self, **kw):
+        o = self.options()
+        for k, v in kw.items():
+            setattr(o, k, v)
+        _check(lib().g3l_set_options(self.h, C.byref(o)))
+
+    def stats(self):
+        s = Stats()
+        _check(lib().g3l_get_stats(self.h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in Stats._fields_}
+
+    @staticmethod
+    def make_items(specs):
+        """specs: iterable of (kind, term, hod1, hod2, (th1, th2, th3), rtol, max_eval)."""
+        specs = list(specs)
+        arr = (Integral * max(1, len(specs)))()
+        for i, (kind, term, h1, h2, th, rtol, me) in enumerate(specs):
+            arr[i].kind, arr[i].term, arr[i].hod1, arr[i].hod2 = kind, term, h1, h2
+            arr[i].theta[0], arr[i].theta[1], arr[i].theta[2] = th
+            arr[i].rtol = rtol
+            arr[i].max_eval = int(me)
+        return arr, len(specs)
+
+    def eval(self, specs, precision=FP64, check=True):
+        """Integrate every spec in one launch; returns a structured numpy array."""
+        items, n = self.make_items(specs)
+        out = (Result * max(1, n))()
+        st = lib().g3l_eval(self.h, items, n, precision, out)
+        if check and st != 0 and st not in (4, 5, 7):
+            _check(st)
+        return results_to_numpy(out, n)
+
+
+def results_to_numpy(out, n):
+    dt = np.dtype([("val", "f8"), ("err", "f8"), ("result", "f8"), ("neval", "u8"),
+                   ("status", "i4"), ("rounds", "i4")])
+    r = np.zeros(n, dtype=dt)
+    for i in range(n):
+        o = out[i]
+        r[i] = (o.val, o.err, o.result, o.neval, o.status, o.rounds)
+    return r
+
+
+class NNMapModel:
+    """The reference's NNMap_Model interface on the GPU engine.
+
+    hod1 / hod2 are parameter vectors {f, alpha, Mth, sigma, M', beta}; passing
+    the same object (or hod2=None) reproduces the reference's single-population
+    case where both type slots point to one HOD (src/HOD.cu:82).
+    The per-term methods use the reference's hard-coded budgets (maxEval 5e6,
+    rtol 1e-3, 1e-3, 1e-4; src/NNMap_Model.cu:318,343,368) unless overridden.
+    """
+
+    RTOL = {1: 1e-3, 2: 1e-3, 3: 1e-4}
+    MAX_EVAL = 5_000_000
+
+    def __init__(self, tables, hod1, hod2=None, A=0.0, epsilon=0.0, precision=FP64, device=0,
+                 clamp_k=True, ctx=None):
+        self.ctx = ctx or Context(tables, device, clamp_k)
+        self.precision = precision
+        self.updateHODs(hod1, hod2)
+        self.ctx.set_correlation(A, epsilon)
+
+    def updateHODs(self, hod1, hod2=None):
+        same = hod2 is None or hod2 is hod1
+        self.ctx.set_hod(0, hod1)
+        if not same:
+            self.ctx.set_hod(1, hod2)
+        self._slot = {1: 0, 2: 0 if same else 1}
+
+    def _spec(self, term, th, type1, type2, rtol=None, max_eval=None):
+        return (NNMAP, term, self._slot[type1], self._slot[type2], tuple(th),
+                self.RTOL[term] if rtol is None else rtol,
+                self.MAX_EVAL if max_eval is None else max_eval)
+
+    def term(self, term, theta1, theta2, theta3, type1=1, type2=2, rtol=None, max_eval=None):
+        r = self.ctx.eval([self._spec(term, (theta1, theta2, theta3), type1, type2, rtol,
+                                      max_eval)], self.precision)
+        return float(r["result"][0])
+
+    def NNMap_1h(self, t1, t2, t3, type1=1, type2=2):
+        return self.term(1, t1, t2, t3, type1, type2)
+
+    def NNMap_2h(self, t1, t2, t3, type1=1, type2=2):
+        return self.term(2, t1, t2, t3, type1, type2)
+
+    def NNMap_3h(self, t1, t2, t3, type1=1, type2=2):
+        return self.term(3, t1, t2, t3, type1, type2)
+
+    def NNMap(self, t1, t2, t3, type1=1, type2=2):
+        r = self.batch([(t1, t2, t3)], (1, 2, 3), type1, type2)
+        return float(r["result"].sum())
+
+    def batch(self, thetas, terms=(1, 2, 3), type1=1, type2=2, rtol=None, max_eval=None):
+        specs = [self._spec(t, th, type1, type2, rtol, max_eval) for th in thetas for t in terms]
+        return self.ctx.eval(specs, self.precision)
+
+    def calculateAll(self, thetas1, thetas2, thetas3, hod1, hod2, A=0.0, epsilon=0.0,
+                     rtol=None, max_eval=None):
+        """N1N2, N1N1, N2N2 blocks of NNMap for every triplet (src/NNMap_Model.cu:382-415)."""
+        self.updateHODs(hod1, hod2)
+        self.ctx.set_correlation(A, epsilon)
+        th = list(zip(thetas1, thetas2, thetas3))
+        specs = []
+        for (a, b) in ((1, 2), (1, 1), (2, 2)):
+            specs += [self._spec(t, x, a, b, rtol, max_eval) for x in th for t in (1, 2, 3)]
+        r = self.ctx.eval(specs, self.precision)
+        return r["result"].reshape(3 * len(th), 3).sum(axis=1)
+
+
+class NMapMapModel:
+    """The reference's NMapMap_Model interface (one HOD, lens p(z) = p_lens1)."""
+
+    RTOL = {1: 1e-3, 2: 1e-3, 3: 1e-3}
+    MAX_EVAL = 5_000_000
+
+    def __init__(self, tables, hod, precision=FP64, device=0, clamp_k=True, ctx=None):
+        self.ctx = ctx or Context(tables, device, clamp_k)
+        self.precision = precision
+        self.updateHOD(hod)
+
+    def updateHOD(self, hod):
+        self.ctx.set_hod(0, hod)
+
+    def _spec(self, term, th, rtol=None, max_eval=None):
+        return (NMAPMAP, term, 0, 0, tuple(th), self.RTOL[term] if rtol is None else rtol,
+                self.MAX_EVAL if max_eval is None else max_eval)
+
+    def term(self, term, t1, t2, t3, rtol=None, max_eval=None):
+        r = self.ctx.eval([self._spec(term, (t1, t2, t3), rtol, max_eval)], self.precision)
+        return float(r["result"][0])
+
+    def NMapMap_1h(self, t1, t2, t3):
+        return self.term(1, t1, t2, t3)
+
+    def NMapMap_2h(self, t1, t2, t3):
+        return self.term(2, t1, t2, t3)
+
+    def NMapMap_3h(self, t1, t2, t3):
+        return self.term(3, t1, t2, t3)
+
+    def NMapMap(self, t1, t2, t3):
+        return float(self.batch([(t1, t2, t3)])["result"].sum())
+
+    def batch(self, thetas, terms=(1, 2, 3), rtol=None, max_eval=None):
+        return self.ctx.eval([self._spec(t, th, rtol, max_eval) for th in thetas for t in terms],
+                             self.precision)
+
+    def calculateAll(self, thetas1, thetas2, thetas3, hod, rtol=None, max_eval=None):
+        self.updateHOD(hod)
+        th = list(zip(thetas1, thetas2, thetas3))
+        r = self.batch(th, (1, 2, 3), rtol, max_eval)
+        return r["result"].reshape(len(th), 3).sum(axis=1)

@@ -1,0 +1,422 @@
+// engine.cu -- device-resident refinement loop of the adaptive cubature.
+//
+// The reference's loop (rulecubature with parallel=1, src/hcubature.cpp:938-989)
+// pops regions from a max-heap keyed on the error until the error left in the
+// heap is within tolerance or the evaluation budget is spent, bisects them,
+// evaluates the children and pushes them back.  Here each round is
+//   k_select : one CTA per integral.  Sums the live regions' values and errors,
+//              applies the reference's stopping tests (numEval >= maxEval,
+//              converged(): err <= |val| rtol, src/converged.h:10-14) and picks
+//              the regions the heap would pop: the largest errors, in order,
+//              until the remaining error is <= rtol |val| (Gladwell), capped by
+//              the evaluation budget.  Both cut-offs are found with an MSD radix
+//              select on the IEEE bit pattern of the errors; the running error
+//              sums use 64-bit fixed point, so the choice is deterministic and
+//              independent of thread scheduling.
+//   k_scan   : prefix sum of the per-integral pop counts -> flat work list; sets
+//              the graph's WHILE condition (no host round trip).
+//   k_eval*  : cut + rule evaluation (eval_fp64.cu / eval_mixed.cu).
+// Compiled with -fmad=false.
+#include <cuda_runtime.h>
+
+#include "g3l_device.cuh"
+
+namespace g3l {
+
+constexpr int SEL_BS = 256;
+constexpr int SEL_WARPS = SEL_BS / 32;
+
+__device__ __forceinline__ unsigned long long ekey(const double *err, long long s)
+{
+    return (unsigned long long)__double_as_longlong(err[s]);
+}
+
+// deterministic block reduction (fixed pairing)
+template <typename T>
+__device__ T block_sum(T v, T *sh)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    T r = 0;
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < SEL_WARPS; ++w) r += sh[w];
+        sh[0] = r;
+    }
+    __syncthreads();
+    r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// exclusive block scan of 0/1 flags; returns prefix, writes the total
+__device__ int block_flag_scan(int flag, int *sh, int &total)
+{
+    unsigned b = __ballot_sync(0xffffffffu, flag);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int pre = __popc(b & ((1u << lane) - 1u));
+    if (lane == 0) sh[w] = __popc(b);
+    __syncthreads();
+    int off = 0, tot = 0;
+    for (int k = 0; k < SEL_WARPS; ++k) {
+        if (k < w) off += sh[k];
+        tot += sh[k];
+    }
+    __syncthreads();
+    total = tot;
+    return off + pre;
+}
+
+struct SelShared {
+    unsigned int cnt[256];
+    unsigned long long sum[256];
+    unsigned long long prefix, mask;
+    unsigned long long sum_above;
+    unsigned int cnt_above;
+    int chosen, unique;
+    double dred[SEL_WARPS];
+    unsigned long long ured[SEL_WARPS];
+    int ired[SEL_WARPS];
+};
+
+// MSD radix select over the live errors of one integral, descending.  by_sum:
+// find the bucket where the cumulative fixed-point error first reaches `need`;
+// otherwise where the cumulative count reaches `need`.  Returns the boundary key
+// and the count/sum of strictly larger keys.
+__device__ void radix_select(const double *err, const unsigned long long *q, long long base, int R,
+                             bool by_sum, unsigned long long need, SelShared &sh,
+                             unsigned long long &bkey, unsigned int &cnt_above,
+                             unsigned long long &sum_above)
+{
+    if (threadIdx.x == 0) {
+        sh.prefix = 0;
+        sh.mask = 0;
+        sh.sum_above = 0;
+        sh.cnt_above = 0;
+        sh.unique = 0;
+    }
+    __syncthreads();
+    for (int pass = 0; pass < 8; ++pass) {
+        const int shift = 56 - 8 * pass;
+        sh.cnt[threadIdx.x] = 0;
+        sh.sum[threadIdx.x] = 0;
+        __syncthreads();
+        const unsigned long long prefix = sh.prefix, mask = sh.mask;
+        for (int j = threadIdx.x; j < R; j += SEL_BS) {
+            unsigned long long k = ekey(err, base + j);
+            if ((k & mask) == prefix) {
+                int dg = (int)((k >> shift) & 255ull);
+                atomicAdd(&sh.cnt[dg], 1u);
+                if (by_sum) atomicAdd(&sh.sum[dg], q[base + j]);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            // lane l owns buckets 255-8l .. 248-8l (descending)
+            const int lane = threadIdx.x;
+            unsigned long long s = 0, c = 0;
+            for (int b = 0; b < 8; ++b) {
+                int dg = 255 - 8 * lane - b;
+                s += sh.sum[dg];
+                c += sh.cnt[dg];
+            }
+            unsigned long long v = by_sum ? s : c;
+            unsigned long long inc = v;  // inclusive scan in descending bucket order
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned long long t = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += t;
+            }
+            const unsigned long long base_v = by_sum ? sh.sum_above : sh.cnt_above;
+            unsigned hit = __ballot_sync(0xffffffffu, base_v + inc >= need);
+            int first = hit ? __ffs(hit) - 1 : 31;
+            unsigned long long exs = 0, exc_c = 0;
+            // exclusive sums of both quantities at the owning lane
+            unsigned long long sc = s, cc = c;
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned long long t1 = __shfl_up_sync(0xffffffffu, sc, o);
+                unsigned long long t2 = __shfl_up_sync(0xffffffffu, cc, o);
+                if (lane >= o) {
+                    sc += t1;
+                    cc += t2;
+                }
+            }
+            exs = sc - s;
+            exc_c = cc - c;
+            if (lane == first) {
+                unsigned long long sa = sh.sum_above + exs, ca = sh.cnt_above + exc_c;
+                int chosen = 255 - 8 * lane - 7;
+                for (int b = 0; b < 8; ++b) {
+                    int dg = 255 - 8 * lane - b;
+                    unsigned long long nv = by_sum ? sa + sh.sum[dg] : ca + sh.cnt[dg];
+                    if (nv >= need) {
+                        chosen = dg;
+                        break;
+                    }
+                    sa += sh.sum[dg];
+                    ca += sh.cnt[dg];
+                }
+                sh.sum_above = sa;
+                sh.cnt_above = (unsigned int)ca;
+                sh.chosen = chosen;
+                sh.prefix = prefix | ((unsigned long long)chosen << shift);
+                sh.mask = mask | (0xFFull << shift);
+                sh.unique = (sh.cnt[chosen] == 1u);
+            }
+        }
+        __syncthreads();
+        if (sh.unique) {
+            // a single element carries the boundary: find its full key
+            const unsigned long long p2 = sh.prefix, m2 = sh.mask;
+            for (int j = threadIdx.x; j < R; j += SEL_BS) {
+                unsigned long long k = ekey(err, base + j);
+                if ((k & m2) == p2) sh.prefix = k;  // exactly one writer
+            }
+            __syncthreads();
+            break;
+        }
+    }
+    bkey = sh.prefix;
+    cnt_above = sh.cnt_above;
+    sum_above = sh.sum_above;
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D,
+                                                   IntState *__restrict__ S, Pool P, BatchHdr *H)
+{
+    __shared__ SelShared sh;
+    __shared__ int s_flag[4];
+    __shared__ double s_tot[2];
+    const int n = H->n;
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        if (S[i].done) {
+            if (threadIdx.x == 0) S[i].K = 0;
+            continue;
+        }
+        const IntDesc &d = D[i];
+        const long long base = d.base;
+        const int R = S[i].nR;
+        if (R == 0) {
+            // fresh integral: its root region is this round's single work item
+            if (threadIdx.x == 0) {
+                P.cand[base] = -1;
+                S[i].K = 1;
+                S[i].nR = 1;
+                S[i].neval = (unsigned long long)d.npts;
+            }
+            __syncthreads();
+            continue;
+        }
+        // totals over live regions
+        double sv = 0, se = 0;
+        for (int j = threadIdx.x; j < R; j += SEL_BS) {
+            sv += P.val[base + j];
+            se += P.err[base + j];
+        }
+        double V = block_sum(sv, sh.dred);
+        double E = block_sum(se, sh.dred);
+        if (threadIdx.x == 0) {
+            IntState st = S[i];
+            int fin = 0, status = ST_OK;
+            if (H->cancel) {
+                fin = 1;
+                status = ST_CANCELLED;
+            } else if (!isfinite(V) || !isfinite(E)) {
+                fin = 1;
+                status = ST_NONFINITE;
+            } else if (d.max_eval && st.neval >= d.max_eval) {
+                fin = 1;
+            } else if (!(E > 0 && E > fabs(V) * d.rtol)) {
+                fin = 1;  // converged (src/converged.h:10-14 with reqAbsError = 0)
+            } else if (st.rounds >= H->max_rounds) {
+                fin = 1;
+                status = ST_ROUNDS;
+            }
+            st.val = V;
+            st.err = E;
+            if (fin) {
+                st.done = 1;
+                st.status = status;
+                st.K = 0;
+                S[i] = st;
+            } else {
+                S[i].val = V;
+                S[i].err = E;
+            }
+            s_flag[0] = fin;
+            s_tot[0] = V;
+            s_tot[1] = E;
+        }
+        __syncthreads();
+        if (s_flag[0]) {
+            __syncthreads();
+            continue;
+        }
+        V = s_tot[0];
+        E = s_tot[1];
+        const unsigned long long neval = S[i].neval;
+        const unsigned long long twoNp = 2ull * (unsigned long long)d.npts;
+        unsigned long long Kcap = (unsigned long long)R;
+        if (d.max_eval) {
+            unsigned long long left = d.max_eval - neval;  // > 0 here
+            unsigned long long kc = (left + twoNp - 1) / twoNp;
+            if (kc < Kcap) Kcap = kc;
+        }
+        // fixed-point errors: q = floor(err * 2^60 / E)
+        const double scale = 1152921504606846976.0 / E;  // 2^60 / E
+        unsigned long long qs = 0;
+        for (int j = threadIdx.x; j < R; j += SEL_BS) {
+            double t = P.err[base + j] * scale;
+            unsigned long long qq = t >= 1.8e19 ? 0xFFFFFFFFFFFFFFFFull : (unsigned long long)t;
+            P.q[base + j] = qq;
+            qs += qq;
+        }
+        const unsigned long long Q = block_sum(qs, sh.ured);
+        const double thr = fabs(V) * d.rtol * scale;
+        const unsigned long long qthr = thr >= 1.8e19 ? 0xFFFFFFFFFFFFFFFFull : (unsigned long long)thr;
+        const unsigned long long need = Q > qthr ? Q - qthr : 0;
+        // K_conv: smallest k >= 1 whose popped error sum reaches `need`
+        unsigned long long Kconv;
+        unsigned long long bkey = 0, tneed = 0;
+        unsigned int cnt_above = 0;
+        unsigned long long sum_above = 0;
+        if (need == 0) {
+            Kconv = 1;
+        } else {
+            radix_select(P.err, P.q, base, R, true, need, sh, bkey, cnt_above, sum_above);
+            // all keys equal to bkey carry the same q (any writer stores the same value)
+            if (threadIdx.x == 0) sh.ured[0] = 0;
+            __syncthreads();
+            for (int j = threadIdx.x; j < R; j += SEL_BS)
+                if (ekey(P.err, base + j) == bkey) sh.ured[0] = P.q[base + j];
+            __syncthreads();
+            unsigned long long qb = sh.ured[0];
+            __syncthreads();
+            unsigned long long rest = need - sum_above;
+            tneed = qb ? (rest + qb - 1) / qb : 1;
+            Kconv = (unsigned long long)cnt_above + tneed;
+        }
+        unsigned long long K = Kconv < Kcap ? Kconv : Kcap;
+        if (K < 1) K = 1;
+        if (K > (unsigned long long)R) K = R;
+        if (K != Kconv || need == 0) {
+            if (K == (unsigned long long)R) {
+                bkey = 0;
+                cnt_above = 0;
+                tneed = R;  // every key >= 0: take all
+            } else {
+                radix_select(P.err, P.q, base, R, false, K, sh, bkey, cnt_above, sum_above);
+                tneed = K - cnt_above;
+            }
+        }
+        // pool capacity
+        if ((long long)R + (long long)K > (long long)d.cap) {
+            if (threadIdx.x == 0) {
+                S[i].done = 1;
+                S[i].status = ST_POOL;
+                S[i].K = 0;
+            }
+            __syncthreads();
+            continue;
+        }
+        // compact the selection in slot order
+        int run_sel = 0, run_tie = 0;
+        for (int c0 = 0; c0 < R; c0 += SEL_BS) {
+            int j = c0 + threadIdx.x;
+            unsigned long long k = j < R ? ekey(P.err, base + j) : 0;
+            int is_eq = (j < R && k == bkey && !(K == (unsigned long long)R)) ? 1 : 0;
+            int is_gt = (j < R && (K == (unsigned long long)R || k > bkey)) ? 1 : 0;
+            int ntie;
+            int tr = run_tie + block_flag_scan(is_eq, sh.ired, ntie);
+            int sel = is_gt || (is_eq && (unsigned long long)tr < tneed);
+            int nsel;
+            int pos = run_sel + block_flag_scan(sel, sh.ired, nsel);
+            if (sel) P.cand[base + pos] = j;
+            run_tie += ntie;
+            run_sel += nsel;
+        }
+        if (threadIdx.x == 0) {
+            S[i].K = (int)K;
+            S[i].neval = neval + twoNp * K;
+            S[i].nR = R + (int)K;
+            S[i].rounds += 1;
+        }
+        __syncthreads();
+    }
+}
+
+// prefix sum of K over integrals; work list offsets; loop condition
+__global__ void __launch_bounds__(1024) k_scan(IntState *__restrict__ S, long long *woff,
+                                               BatchHdr *H, cudaGraphConditionalHandle handle,
+                                               int use_cond)
+{
+    __shared__ long long part[1024];
+    const int n = H->n;
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(n, b + per);
+    long long loc = 0;
+    for (int i = b; i < e; ++i) loc += S[i].K;
+    part[threadIdx.x] = loc;
+    __syncthreads();
+    for (int o = 1; o < (int)blockDim.x; o <<= 1) {
+        long long t = threadIdx.x >= (unsigned)o ? part[threadIdx.x - o] : 0;
+        __syncthreads();
+        part[threadIdx.x] += t;
+        __syncthreads();
+    }
+    long long run = part[threadIdx.x] - loc;
+    for (int i = b; i < e; ++i) {
+        woff[i] = run;
+        run += S[i].K;
+    }
+    if (threadIdx.x == blockDim.x - 1) {
+        long long tot = part[blockDim.x - 1];
+        woff[n] = tot;
+        H->total_work = tot;
+        H->any_active = tot > 0;
+        H->regions += 2ull * (unsigned long long)tot;
+        if (tot > 0) H->rounds_done += 1;
+        if (use_cond) cudaGraphSetConditional(handle, tot > 0 ? 1u : 0u);
+    }
+}
+
+// root regions and fresh state
+__global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, Pool P,
+                       BatchHdr *H)
+{
+    const int n = H->n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const IntDesc &d = D[i];
+        for (int k = 0; k < MAX_DIM; ++k) {
+            if (k < d.dim) {
+                P.center[k * P.stride + d.base] = d.c0[k];
+                P.level[k * P.stride + d.base] = 0;
+            }
+        }
+        IntState st;
+        st.val = 0;
+        st.err = 0;
+        st.neval = 0;
+        st.nR = 0;
+        st.K = 0;
+        st.done = 0;
+        st.status = ST_OK;
+        st.rounds = 0;
+        st.pad = 0;
+        S[i] = st;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        H->any_active = 1;
+        H->total_work = 0;
+        H->regions = (unsigned long long)n;
+        H->rounds_done = 0;
+        H->ties = 0;
+        H->small_arg = 0;
+    }
+}
+
+void *select_kernel() { return (void *)k_select; }
+void *scan_kernel() { return (void *)k_scan; }
+void *init_kernel() { return (void *)k_init; }
+
+}  // namespace g3l

@@ -1,0 +1,381 @@
+// eval_fp64.cu -- all-FP64 rule evaluation: the plain FP64 form of the engine.
+//
+// One warp evaluates one work item: it cuts a selected parent region along its
+// split dimension (cut_region, src/hcubature.cpp:206-218) and applies the
+// Genz-Malik 7/5 rule to both children (rule75genzmalik_evalError,
+// src/hcubature.cpp:456-577), or evaluates a root region.  The per-dimension
+// coordinate variants (c, c-+lambda*h) are computed once per child together
+// with everything that depends on one coordinate only (10^x, aperture filter,
+// HOD occupations, bin indices); each lane then evaluates whole points.  The
+// rule sums are formed by one lane per child in the reference's summation
+// order.  Compiled with -fmad=false so every product and sum rounds as in the
+// reference's CPU build.
+#include "phys64.cuh"
+
+namespace g3l {
+
+struct Slot64 {
+    double a[6];
+    int i0, i1;
+};
+
+template <int KIND, int TERM>
+struct Model64 {
+    static constexpr int DIM = TERM + 4;
+
+    // Fill one coordinate-variant slot (everything that depends on one coordinate).
+    __device__ static void fill(const DevTables &T, const IntDesc &d, int dimidx, double x,
+                                Slot64 &S, unsigned long long *ties)
+    {
+        if (dimidx < 2) {  // l1, l2 (log10 l)
+            double l = pow(10, x);
+            S.a[0] = l;
+            S.a[1] = aperture64(d.theta[dimidx] * l);
+        } else if (dimidx == 2) {  // phi
+            S.a[0] = cos(x);
+        } else if (dimidx < 3 + TERM) {  // halo masses (log10 m)
+            double m = pow(10, x);
+            S.a[0] = m;
+            m_index(T, x, m, S.i0, S.i1, ties);
+            const double *h1 = T.hod + 6 * d.hod1;
+            const double *h2 = T.hod + 6 * d.hod2;
+            S.a[1] = ncen64(h1, m);
+            S.a[2] = nsat64(h1, m);
+            if (KIND == 0) {
+                S.a[3] = ncen64(h2, m);
+                S.a[4] = nsat64(h2, m);
+                S.a[5] = nsatnsat64(h1, h2, d.same, T.A, T.eps, m);
+            }
+        } else {  // z
+            S.a[0] = x;
+            double zr = (x - T.zmin) * T.Nz / (T.zmax - T.zmin);
+            S.i0 = min(max((int)round(zr), 0), T.Nz - 1);
+            S.i1 = min(max((int)zr, 0), T.Nz - 1);
+        }
+    }
+
+    // Integrand at one point from its variant slots (kernel_function_* of the reference).
+    __device__ static double point(const DevTables &T, const IntDesc &d, const Slot64 *const *s)
+    {
+        const Slot64 &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
+        const double l1 = L1.a[0], l2 = L2.a[0], cphi = PH.a[0], z = Z.a[0];
+        const int z_ix = Z.i0, z_it = Z.i1, Nm = T.Nm;
+        const double w_ = __ldg(T.w + z_ix);
+        const double l3 = sqrt(l1 * l1 + l2 * l2 + 2 * l1 * l2 * cphi);
+        const double k1 = l1 / w_;
+        const double k2 = l2 / w_;
+        const double k3 = l3 / w_;
+        const double rho = __ldg(T.rho_bar + z_ix);
+        const double rhot = __ldg(T.rho_bar + z_it);
+        const double f1 = T.hod[6 * d.hod1];
+        const double U3 = aperture64(d.theta[2] * l3);
+        if (KIND == 0) {
+            const double nbar1 = __ldg(T.nbar + d.hod1 * T.Nz + z_ix);
+            const double nbar2 = __ldg(T.nbar + d.hod2 * T.Nz + z_ix);
+            const double f2 = T.hod[6 * d.hod2];
+            if (TERM == 1) {
+                // src/NNMap_Model.cu:544-593
+                const Slot64 &M = *s[3];
+                const double m = M.a[0];
+                const double r2 = r200_64(m, rhot);
+                const double cc = __ldg(T.conc + z_it * Nm + M.i1);
+                const double u3 = u_nfw64(k3, r2, cc, 1);
+                const double u2 = u_nfw64(k2, r2, cc, f2);
+                const double u1 = u_nfw64(k1, r2, cc, f1);
+                double Bggd = 1. / nbar1 / nbar2 / rho * __ldg(T.hmf + z_ix * Nm + M.i0) * m * u3;
+                Bggd *= M.a[1] * M.a[4] * u2 + M.a[3] * M.a[2] * u1 + M.a[5] * u1 * u2;
+                double bggk = Bggd / __ldg(T.dwdz + z_ix) * __ldg(T.g + z_ix) *
+                              __ldg(T.p1 + z_ix) * __ldg(T.p2 + z_ix) / w_ / w_ / w_ * (1. + z);
+                return l1 * l2 * m * l1 * l2 * L1.a[1] * L2.a[1] * U3 * bggk;
+            } else if (TERM == 2) {
+                // src/NNMap_Model.cu:787-856
+                const Slot64 &M1 = *s[3], &M2 = *s[4];
+                const double m1 = M1.a[0], m2 = M2.a[0];
+                const double Pk1 = plin64(T, z_ix, k1);
+                const double Pk2 = plin64(T, z_ix, k2);
+                const double Pk3 = plin64(T, z_ix, k3);
+                const double ra = r200_64(m1, rhot), rb = r200_64(m2, rhot);
+                const double ca = __ldg(T.conc + z_it * Nm + M1.i1);
+                const double cb = __ldg(T.conc + z_it * Nm + M2.i1);
+                const double u3_1 = u_nfw64(k3, ra, ca, 1);
+                const double u3_2 = u_nfw64(k3, rb, cb, 1);
+                const double u1_1 = u_nfw64(k1, ra, ca, f1);
+                const double u2_1 = u_nfw64(k2, ra, ca, f2);
+                const double u1_2 = u_nfw64(k1, rb, cb, f1);
+                const double u2_2 = u_nfw64(k2, rb, cb, f2);
+                // G_gg(k1, k2, m2)
+                const double Ggg = M2.a[1] * M2.a[4] * u2_2 + M2.a[3] * M2.a[2] * u1_2 +
+                                   M2.a[5] * u1_2 * u2_2;
+                const double Gg_k1m1 = M1.a[1] + M1.a[2] * u1_1;  // hod1 at m1
+                const double Gg_k2m2 = M2.a[3] + M2.a[4] * u2_2;  // hod2 at m2
+                const double Gg_k2m1 = M1.a[3] + M1.a[4] * u2_1;  // hod2 at m1
+                const double Gg_k1m2 = M2.a[1] + M2.a[2] * u1_2;  // hod1 at m2
+                double Bggd = 1. / nbar1 / nbar2 / rho * __ldg(T.hmf + z_ix * Nm + M1.i0) *
+                              __ldg(T.hmf + z_ix * Nm + M2.i0) * __ldg(T.b_h + z_ix * Nm + M1.i0) *
+                              __ldg(T.b_h + z_ix * Nm + M2.i0) *
+                              (m1 * u3_1 * Ggg * Pk3 + m2 * u3_2 * Gg_k1m1 * Gg_k2m2 * Pk1 +
+                               m2 * u3_2 * Gg_k2m1 * Gg_k1m2 * Pk2);
+                double bggk = 1. / __ldg(T.dwdz + z_ix) * __ldg(T.g + z_ix) * __ldg(T.p1 + z_ix) *
+                              __ldg(T.p2 + z_ix) / w_ / w_ / w_ * (1. + z) * Bggd;
+                return l1 * l2 * m1 * m2 * l1 * l2 * L1.a[1] * L2.a[1] * U3 * bggk;
+            } else {
+                // src/NNMap_Model.cu:1003-1037
+                const Slot64 &M1 = *s[3], &M2 = *s[4], &M3 = *s[5];
+                const double m1 = M1.a[0], m2 = M2.a[0], m3 = M3.a[0];
+                const double u3 = u_nfw64(k3, r200_64(m3, rhot), __ldg(T.conc + z_it * Nm + M3.i1), 1);
+                const double u1 = u_nfw64(k1, r200_64(m1, rhot), __ldg(T.conc + z_it * Nm + M1.i1), f1);
+                const double u2 = u_nfw64(k2, r200_64(m2, rhot), __ldg(T.conc + z_it * Nm + M2.i1), f2);
+                const double Gg1 = M1.a[1] + M1.a[2] * u1;  // hod1 at m1
+                const double Gg2 = M2.a[3] + M2.a[4] * u2;  // hod2 at m2
+                double Bggd = 1. / nbar1 / nbar2 / rho * __ldg(T.hmf + z_ix * Nm + M1.i0) *
+                              __ldg(T.hmf + z_ix * Nm + M2.i0) * __ldg(T.hmf + z_ix * Nm + M3.i0) *
+                              m3 * u3 * Gg1 * Gg2 * bi_lin64(T, k1, k2, cphi, z_ix) *
+                              __ldg(T.b_h + z_ix * Nm + M1.i0) * __ldg(T.b_h + z_ix * Nm + M2.i0) *
+                              __ldg(T.b_h + z_ix * Nm + M3.i0);
+                double bggk = Bggd / __ldg(T.dwdz + z_ix) * __ldg(T.g + z_ix) * __ldg(T.p1 + z_ix) *
+                              __ldg(T.p2 + z_ix) / w_ / w_ / w_ * (1. + z);
+                return l1 * l2 * m1 * m2 * m3 * l1 * l2 * L1.a[1] * L2.a[1] * U3 * bggk;
+            }
+        } else {
+            const double nbar = __ldg(T.nbar + d.hod1 * T.Nz + z_ix);
+            const double f = f1;
+            const double gz = __ldg(T.g + z_ix);
+            if (TERM == 1) {
+                // src/NMapMap_Model.cu:263-301
+                const Slot64 &M = *s[3];
+                const double m = M.a[0];
+                const double r2 = r200_64(m, rhot);
+                const double cc = __ldg(T.conc + z_it * Nm + M.i1);
+                double Bgdd = 1. / nbar / rho / rho * __ldg(T.hmf + z_ix * Nm + M.i0) * m * m *
+                              (M.a[1] + M.a[2] * u_nfw64(k1, r2, cc, f)) * u_nfw64(k2, r2, cc, 1) *
+                              u_nfw64(k3, r2, cc, 1);
+                double bgkk = Bgdd / __ldg(T.dwdz + z_ix) * gz * gz * __ldg(T.p1 + z_ix) / w_ / w_ *
+                              (1. + z) * (1. + z);
+                return l1 * l2 * m * l1 * l2 * L1.a[1] * L2.a[1] * U3 * bgkk / nbar;
+            } else if (TERM == 2) {
+                // src/NMapMap_Model.cu:402-468
+                const Slot64 &M1 = *s[3], &M2 = *s[4];
+                const double m1 = M1.a[0], m2 = M2.a[0];
+                const double Pk1 = plin64(T, z_ix, k1);
+                const double Pk2 = plin64(T, z_ix, k2);
+                const double Pk3 = plin64(T, z_ix, k3);
+                const double ra = r200_64(m1, rhot), rb = r200_64(m2, rhot);
+                const double ca = __ldg(T.conc + z_it * Nm + M1.i1);
+                const double cb = __ldg(T.conc + z_it * Nm + M2.i1);
+                const double u2_1 = u_nfw64(k2, ra, ca, 1);
+                const double u3_2 = u_nfw64(k3, rb, cb, 1);
+                const double u1_2f = u_nfw64(k1, rb, cb, f);
+                const double u3_1 = u_nfw64(k3, ra, ca, 1);
+                const double u2_2 = u_nfw64(k2, rb, cb, 1);
+                const double u1_1f = u_nfw64(k1, ra, ca, f);
+                double Bgdd = 1. / nbar / rho / rho * __ldg(T.hmf + z_ix * Nm + M1.i0) *
+                              __ldg(T.hmf + z_ix * Nm + M2.i0) * __ldg(T.b_h + z_ix * Nm + M1.i0) *
+                              __ldg(T.b_h + z_ix * Nm + M2.i0) *
+                              (m1 * m2 * u2_1 * u3_2 * (M2.a[1] + M2.a[2] * u1_2f) * Pk2 +
+                               m1 * m2 * u3_1 * u2_2 * (M2.a[1] + M2.a[2] * u1_2f) * Pk3 +
+                               m2 * m2 * u2_1 * u3_2 * (M1.a[1] + M1.a[2] * u1_1f) * Pk1);
+                double bgkk = Bgdd / __ldg(T.dwdz + z_ix) * gz * gz * __ldg(T.p1 + z_ix) / w_ / w_ *
+                              (1. + z) * (1. + z);
+                return l1 * l2 * m1 * m2 * l1 * l2 * L1.a[1] * L2.a[1] * U3 * bgkk / nbar;
+            } else {
+                // src/NMapMap_Model.cu:592-632 (Nc, Ns at m3; u_NFW(k1, m2, f))
+                const Slot64 &M1 = *s[3], &M2 = *s[4], &M3 = *s[5];
+                const double m1 = M1.a[0], m2 = M2.a[0], m3 = M3.a[0];
+                const double ra = r200_64(m1, rhot), rb = r200_64(m2, rhot);
+                const double ca = __ldg(T.conc + z_it * Nm + M1.i1);
+                const double cb = __ldg(T.conc + z_it * Nm + M2.i1);
+                double Bgdd = 1. / nbar / rho / rho * __ldg(T.hmf + z_ix * Nm + M1.i0) *
+                              __ldg(T.hmf + z_ix * Nm + M2.i0) * __ldg(T.hmf + z_ix * Nm + M3.i0) *
+                              __ldg(T.b_h + z_ix * Nm + M1.i0) * __ldg(T.b_h + z_ix * Nm + M2.i0) *
+                              __ldg(T.b_h + z_ix * Nm + M3.i0) * m1 * m2 * u_nfw64(k2, ra, ca, 1) *
+                              u_nfw64(k3, rb, cb, 1) * (M3.a[1] + M3.a[2] * u_nfw64(k1, rb, cb, f)) *
+                              bi_lin64(T, k1, k2, cphi, z_ix);
+                double bgkk = Bgdd / __ldg(T.dwdz + z_ix) * gz * gz * __ldg(T.p1 + z_ix) / w_ / w_ *
+                              (1. + z) * (1. + z);
+                return l1 * l2 * m1 * m2 * m3 * l1 * l2 * L1.a[1] * L2.a[1] * U3 * bgkk / nbar;
+            }
+        }
+    }
+};
+
+// Rule sums of one region in the reference's order (src/hcubature.cpp:512-576).
+template <int DIM>
+__device__ void combine64(const double *v, double vol, double &val, double &err, int &split)
+{
+    const double ratio = (G3L_LAMBDA2 * G3L_LAMBDA2) / (G3L_LAMBDA4 * G3L_LAMBDA4);
+    const double weight1 = (double)(12824 - 9120 * DIM + 400 * DIM * DIM) / (double)19683;
+    const double weight3 = (double)(1820 - 400 * DIM) / (double)19683;
+    const double weight5 = (double)6859 / (double)19683 / (double)(1u << DIM);
+    const double weightE1 = (double)(729 - 950 * DIM + 50 * DIM * DIM) / (double)729;
+    const double weightE3 = (double)(265 - 100 * DIM) / (double)1458;
+    const double weight2 = 980. / 6561., weight4 = 200. / 19683.;
+    const double weightE2 = 245. / 486., weightE4 = 25. / 729.;
+    double val0 = v[0], sum2 = 0, sum3 = 0, sum4 = 0, sum5 = 0;
+    double maxdiff = 0;
+    int dimDiffMax = 0;
+    int k0 = 1;
+    for (int k = 0; k < DIM; ++k) {
+        double v0 = v[k0 + 4 * k], v1 = v[k0 + 4 * k + 1];
+        double v2 = v[k0 + 4 * k + 2], v3 = v[k0 + 4 * k + 3];
+        sum2 += v0 + v1;
+        sum3 += v2 + v3;
+        double diff = 0;
+        diff += fabs(v0 + v1 - 2 * val0 - ratio * (v2 + v3 - 2 * val0));
+        if (diff > maxdiff) {
+            maxdiff = diff;
+            dimDiffMax = k;
+        }
+    }
+    k0 += 4 * DIM;
+    for (int k = 0; k < 2 * DIM * (DIM - 1); ++k) sum4 += v[k0 + k];
+    k0 += 2 * DIM * (DIM - 1);
+    for (int k = 0; k < (1 << DIM); ++k) sum5 += v[k0 + k];
+    double result = vol * (weight1 * val0 + weight2 * sum2 + weight3 * sum3 + weight4 * sum4 +
+                           weight5 * sum5);
+    double res5th = vol * (weightE1 * val0 + weightE2 * sum2 + weightE3 * sum3 + weightE4 * sum4);
+    val = result;
+    err = fabs(res5th - result);
+    split = dimDiffMax;
+}
+
+template <int KIND, int TERM>
+__global__ void __launch_bounds__(128) k_eval64(DevTables T, const IntDesc *__restrict__ D,
+                                                IntState *__restrict__ S, Pool P, BatchHdr *H,
+                                                const long long *__restrict__ woff)
+{
+    constexpr int DIM = TERM + 4;
+    constexpr int NP = rule_points(DIM);
+    constexpr int NSLOT = (DIM + 1) * NVAR;
+    constexpr int WPB = 4;
+    __shared__ uint32_t sdesc[NP];
+    __shared__ Slot64 sslot[WPB][NSLOT];
+    __shared__ double svals[WPB][2 * NP];
+    const int g = KIND * 3 + TERM - 1;
+    for (int p = threadIdx.x; p < NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gb = H->gbeg[g], ge = H->gbeg[g + 1];
+    if (gb >= ge) return;
+    const long long wbeg = woff[gb], wend = woff[ge];
+    unsigned long long *ties = &H->ties;
+    Slot64 *slots = sslot[wib];
+    double *vals = svals[wib];
+    const long long nwarps = (long long)gridDim.x * WPB;
+    for (long long w = wbeg + (long long)blockIdx.x * WPB + wib; w < wend; w += nwarps) {
+        int lo = gb, hi = ge - 1;  // last integral i with woff[i] <= w
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (woff[mid] <= w) lo = mid;
+            else hi = mid - 1;
+        }
+        const int i = lo;
+        const long long j = w - woff[i];
+        const IntDesc &d = D[i];
+        const long long stride = P.stride;
+        const int cj = P.cand[d.base + j];
+        const bool root = cj < 0;  // a fresh integral's root region
+        long long pslot = d.base + (root ? 0 : cj), qslot = -1;
+        int sdim = 0;
+        if (!root) {
+            qslot = d.base + (S[i].nR - S[i].K) + j;
+            sdim = P.split[pslot];
+        }
+        const int nchild = root ? 1 : 2;
+        // parent geometry
+        double c_l = 0;
+        int lev = 0;
+        if (lane < DIM) {
+            c_l = P.center[lane * stride + pslot];
+            lev = P.level[lane * stride + pslot];
+        }
+        double cL = 0, cR = 0;
+        int levs = __shfl_sync(0xffffffffu, lev, sdim) + (root ? 0 : 1);
+        double cs = __shfl_sync(0xffffffffu, c_l, sdim);
+        double hws = ldexp(d.hw0[sdim], -levs);
+        if (!root) {
+            cL = cs - hws;
+            cR = cs + hws;
+        }
+        int levsum = __reduce_add_sync(0xffffffffu, lane < DIM ? lev : 0) + (root ? 0 : 1);
+        // coordinate variant slots: dims 0..DIM-1 of child 0, then dim sdim of child 1
+        const int nslot = (DIM + nchild - 1) * NVAR;
+        for (int t = lane; t < nslot; t += 32) {
+            int dd = t / NVAR, v = t - dd * NVAR;
+            int dim = dd < DIM ? dd : sdim;
+            double c = P.center[dim * stride + pslot];
+            int L = P.level[dim * stride + pslot];
+            if (!root && dim == sdim) {
+                L += 1;
+                c = (dd < DIM) ? cL : cR;
+            }
+            double hw = ldexp(d.hw0[dim], -L);
+            double x = c;
+            if (v > 0) {
+                double lam = (v <= 2) ? G3L_LAMBDA2 : (v <= 4 ? G3L_LAMBDA4 : G3L_LAMBDA5);
+                double r = hw * lam;
+                x = (v & 1) ? c - r : c + r;
+            }
+            Model64<KIND, TERM>::fill(T, d, dim, x, slots[t], ties);
+        }
+        __syncwarp();
+        // points
+        for (int p = lane; p < nchild * NP; p += 32) {
+            int ch = p >= NP ? 1 : 0;
+            int pp = p - ch * NP;
+            uint32_t vv = sdesc[pp];
+            const Slot64 *sp[DIM];
+#pragma unroll
+            for (int dd = 0; dd < DIM; ++dd) {
+                int v = (vv >> (3 * dd)) & 7;
+                sp[dd] = (ch && dd == sdim) ? &slots[DIM * NVAR + v] : &slots[dd * NVAR + v];
+            }
+            vals[p] = Model64<KIND, TERM>::point(T, d, sp);
+        }
+        __syncwarp();
+        // rule sums: lane 0 -> child 0, lane 1 -> child 1
+        if (lane < nchild) {
+            double vol = ldexp(d.rootvol, -levsum);
+            double val, err;
+            int split;
+            combine64<DIM>(vals + lane * NP, vol, val, err, split);
+            long long slot = lane == 0 ? pslot : qslot;
+            P.val[slot] = val;
+            P.err[slot] = err;
+            P.split[slot] = (unsigned char)split;
+        }
+        // child geometry
+        if (!root && lane < DIM) {
+            double cnew = c_l;
+            int lnew = lev;
+            if (lane == sdim) {
+                lnew = levs;
+                cnew = cL;
+            }
+            P.center[lane * stride + pslot] = cnew;
+            P.level[lane * stride + pslot] = (unsigned char)lnew;
+            P.center[lane * stride + qslot] = lane == sdim ? cR : c_l;
+            P.level[lane * stride + qslot] = (unsigned char)lnew;
+        }
+        __syncwarp();
+    }
+}
+
+#define G3L_INST64(K, Tm)                                                                        \
+    template __global__ void k_eval64<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,      \
+                                             BatchHdr *, const long long *);
+G3L_INST64(0, 1)
+G3L_INST64(0, 2)
+G3L_INST64(0, 3)
+G3L_INST64(1, 1)
+G3L_INST64(1, 2)
+G3L_INST64(1, 3)
+
+void *eval64_kernel(int kind, int term)
+{
+    static void *tab[2][3] = {
+        {(void *)k_eval64<0, 1>, (void *)k_eval64<0, 2>, (void *)k_eval64<0, 3>},
+        {(void *)k_eval64<1, 1>, (void *)k_eval64<1, 2>, (void *)k_eval64<1, 3>}};
+    return tab[kind][term - 1];
+}
+
+}  // namespace g3l

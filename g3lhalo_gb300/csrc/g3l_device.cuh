@@ -1,0 +1,147 @@
+// g3l_device.cuh -- data layout shared by the engine kernels.
+//
+// Region pool (per call, in HBM, structure of arrays):
+//   center[d * stride + slot]  FP64 region centre per dimension
+//   level [d * stride + slot]  bisection depth per dimension; the half-width is
+//                              hw0[d] * 2^-level exactly, and the reference's cached
+//                              volume is rootvol * 2^-(sum of levels) exactly
+//                              (compute_vol / cut_region, src/hcubature.cpp:134-141,
+//                              206-218: halving and products scale exactly by 2)
+//   val, err                   FP64 rule value and error of the region
+//   split                      dimension to bisect next (src/hcubature.cpp:565-575)
+// Integral i owns slots [base_i, base_i + cap_i); its live regions are the first nR_i.
+#pragma once
+#include <cstdint>
+
+namespace g3l {
+
+constexpr int MAX_DIM = 7;
+constexpr int NVAR = 7;  // coordinate variants per dimension: c, c-+r2, c-+r4, c-+r5
+constexpr int MAX_HOD_SLOTS = 1024;
+constexpr int NGROUPS = 6;  // kind * 3 + (term - 1)
+
+// status codes (mirror g3l_status)
+enum : int {
+    ST_OK = 0, ST_INVALID = 1, ST_CUDA = 2, ST_NOMEM = 3, ST_POOL = 4, ST_NONFINITE = 5,
+    ST_CANCELLED = 6, ST_ROUNDS = 7
+};
+
+// Genz-Malik degree 7/5 rule (Genz & Malik 1983; src/hcubature.cpp:458-466).
+// lambda2 = sqrt(9/70), lambda4 = sqrt(9/10), lambda5 = sqrt(9/19).
+#define G3L_LAMBDA2 0.3585685828003180919906451539079374954541
+#define G3L_LAMBDA4 0.9486832980505137995996680633298155601160
+#define G3L_LAMBDA5 0.6882472016116852977216287342936235251269
+
+__host__ __device__ constexpr int rule_points(int dim)
+{
+    return 1 + 4 * dim + 2 * dim * (dim - 1) + (1 << dim);
+}
+
+// Tables and model scalars, passed by value to every kernel.
+struct DevTables {
+    int Nz, Nm, Nk, clamp_k;
+    double zmin, zmax, mmin, mmax, kmin, kmax;
+    double ln_mratio, ln_kratio;  // log(mmax/mmin), log(kmax/kmin)
+    double m_x0, m_scale;         // m index ~ (log10 m - m_x0) * m_scale
+    double A, eps;                // satellite-pair correlation
+    const double *g, *p1, *p2, *w, *dwdz, *rho_bar;  // [Nz]
+    const double *hmf, *b_h, *conc;                  // [Nz*Nm]
+    const double *P_lin;                             // [Nz*Nk]
+    const double *nbar;                              // [slot][Nz]
+    const double *hod;                               // [slot][6] f, alpha, Mth, sigma, M', beta
+    // exact nearest-bin indices of the tie-prone m-centre values, resolved on the
+    // host with the reference's own expression (sorted by bit pattern)
+    const unsigned long long *tie_m_bits;
+    const int *tie_m_round, *tie_m_trunc;
+    int n_tie_m;
+    // FP32 tables of the mixed-precision path (scaled; see eval_mixed.cu)
+    const float *f_hmf, *f_bh, *f_conc, *f_plin, *f_lnplin;
+    const float *f_zA, *f_zB;       // per-z factors of NNMap / NMapMap
+    const float *f_w, *f_invw, *f_rho, *f_rhot, *f_nbar; // [Nz] / [slot][Nz]
+    const float2 *f_kb;             // per-z double-float (ln(w kmin)) * Nk / ln(kmax/kmin)
+    float2 k_a;                     // double-float ln(10) * Nk / ln(kmax/kmin)
+    float2 m_s2, m_x02;             // double-float m_scale, m_x0
+    float2 z_s2, z_02;              // double-float Nz/(zmax-zmin), zmin
+};
+
+struct IntDesc {
+    double theta[3];
+    double c0[MAX_DIM];   // root centre
+    double hw0[MAX_DIM];  // root half-widths
+    double rootvol;
+    double rtol;
+    double scale;         // mixed path: true value = scaled value * scale
+    unsigned long long max_eval;
+    long long base;       // first pool slot
+    int cap;              // pool capacity in regions
+    int hod1, hod2, same; // HOD slots; same = same-population branch
+    int kind, term, dim, npts;
+    int pad;
+};
+
+struct IntState {
+    double val, err;
+    unsigned long long neval;
+    int nR, K, done, status, rounds, pad;
+};
+
+struct Pool {
+    double *center;
+    unsigned char *level;
+    double *val, *err;
+    unsigned char *split;
+    unsigned long long *q;  // fixed-point errors (selection scratch)
+    int *cand;              // selected parents, per-integral segment at base
+    long long stride;
+};
+
+// Per-call header kept in device memory so one instantiated graph serves any batch.
+struct BatchHdr {
+    int n;                       // integrals (sorted by group)
+    int gbeg[NGROUPS + 1];       // group g = integrals [gbeg[g], gbeg[g+1])
+    int max_rounds;
+    int cancel;                  // set by the host to stop the loop
+    int any_active;              // written by the scan kernel
+    long long total_work;
+    unsigned long long points;   // statistics
+    unsigned long long ties;
+    unsigned long long small_arg;
+    unsigned long long regions;
+    int rounds_done;
+};
+
+// Point p of a dim-dimensional Genz-Malik rule -> coordinate variant of dim d,
+// in the reference's generation order (src/hcubature.cpp:343-414, 476-503):
+//   p = 0                   centre
+//   p = 1 + 4k + s          axis k: s = 0..3 -> c-r2, c+r2, c-r4, c+r4
+//   then the 2 dim (dim-1)  (+-r4, +-r4) pairs (i<j), order (-,-) (+,-) (+,+) (-,+)
+//   then 2^dim corners      +-r5 in reflected Gray-code order, first all '+'
+// variant codes: 0 c, 1 c-r2, 2 c+r2, 3 c-r4, 4 c+r4, 5 c-r5, 6 c+r5.
+// Packed 3 bits per dimension.
+__host__ __device__ inline uint32_t point_variants(int dim, int p)
+{
+    if (p == 0) return 0u;
+    int q = p - 1;
+    if (q < 4 * dim) {
+        int k = q >> 2, s = q & 3;
+        return (uint32_t)(s + 1) << (3 * k);
+    }
+    q -= 4 * dim;
+    int nrr = 2 * dim * (dim - 1);
+    if (q < nrr) {
+        int pair = q >> 2, t = q & 3;
+        int i = 0, rem = pair;
+        while (rem >= dim - 1 - i) { rem -= dim - 1 - i; ++i; }
+        int j = i + 1 + rem;
+        uint32_t vi = (t == 1 || t == 2) ? 4u : 3u;
+        uint32_t vj = (t >= 2) ? 4u : 3u;
+        return (vi << (3 * i)) | (vj << (3 * j));
+    }
+    q -= nrr;
+    uint32_t gray = (uint32_t)q ^ ((uint32_t)q >> 1);
+    uint32_t out = 0;
+    for (int d = 0; d < dim; ++d) out |= (((gray >> d) & 1u) ? 5u : 6u) << (3 * d);
+    return out;
+}
+
+}  // namespace g3l

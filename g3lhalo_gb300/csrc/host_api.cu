@@ -1,0 +1,694 @@
+// host_api.cu -- the C ABI: context, tables, HOD slots, batched evaluation.
+//
+// A call to g3l_eval turns its integrals into per-integral descriptors (sorted
+// by kind and term so each rule-evaluation kernel sees one integrand), sizes
+// the region pools from the evaluation caps, and runs one CUDA graph:
+//   k_init -> WHILE(any work) { k_select -> k_scan -> k_eval per group }
+// The loop condition is set on the device by k_scan, so the host waits once,
+// at the end of the call.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "g3l_device.cuh"
+#include "g3l_gpu.h"
+#include "host_internal.h"
+
+namespace g3l {
+void *eval64_kernel(int kind, int term);
+void *evalmx_kernel(int kind, int term);
+void *select_kernel();
+void *scan_kernel();
+void *init_kernel();
+namespace host {
+const char *last_error_cstr();
+}
+}  // namespace g3l
+
+using namespace g3l;
+
+namespace {
+
+#define G3L_CK(call)                                                                          \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) {                                                              \
+            host::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));              \
+            return G3L_ERR_CUDA;                                                              \
+        }                                                                                     \
+    } while (0)
+
+template <typename T>
+int dalloc(T **p, size_t n)
+{
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        host::set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        *p = nullptr;
+        return G3L_ERR_NOMEM;
+    }
+    return G3L_OK;
+}
+
+struct Workspace {
+    size_t pool_cap = 0;
+    int n_cap = 0;
+    Pool P{};
+    IntDesc *D = nullptr;
+    IntState *S = nullptr;
+    long long *woff = nullptr;
+    BatchHdr *H = nullptr;
+    int gen = 0;
+};
+
+struct GraphEntry {
+    int gen, precision, gmask;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+};
+
+}  // namespace
+
+struct g3l_ctx {
+    int device = 0, nsm = 0;
+    cudaStream_t stream = nullptr;
+    host::Binning B{};
+    double Om = 0, OL = 0, Ob = 0, s8 = 0, H0 = 0, ns = 0;
+    std::vector<double> hmf_h, rho_h;
+    std::vector<double> hod_h, nbar_h;
+    std::vector<char> hod_set;
+    double A = 0, eps = 0;
+    DevTables T{};
+    std::vector<void *> allocs;
+    double *d_hod = nullptr, *d_nbar = nullptr;
+    Workspace W;
+    std::vector<GraphEntry> graphs;
+    g3l_options opt{};
+    g3l_stats stats{};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    long long *h_pinned = nullptr;
+    int64_t next_ticket = 1;
+    std::map<int64_t, std::pair<int, std::vector<g3l_result>>> tickets;
+};
+
+namespace {
+
+int upload(g3l_ctx *c, const double *src, size_t n, const double **dst)
+{
+    double *p;
+    int st = dalloc(&p, n);
+    if (st) return st;
+    c->allocs.push_back(p);
+    G3L_CK(cudaMemcpy(p, src, n * sizeof(double), cudaMemcpyHostToDevice));
+    *dst = p;
+    return G3L_OK;
+}
+
+bool finite_all(const double *a, size_t n)
+{
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(a[i])) return false;
+    return true;
+}
+
+int ensure_workspace(g3l_ctx *c, int n, size_t pool)
+{
+    Workspace &W = c->W;
+    if (n <= W.n_cap && pool <= W.pool_cap) return G3L_OK;
+    cudaStreamSynchronize(c->stream);
+    int ncap = std::max(n, W.n_cap);
+    size_t pcap = std::max(pool, W.pool_cap);
+    if (n > W.n_cap) ncap = std::max(ncap, (int)(n * 1.25) + 16);
+    if (pool > W.pool_cap) pcap = std::max(pcap, (size_t)(pool * 1.25) + 1024);
+    void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.q, W.P.cand,
+                    W.D,        W.S,       W.woff,  W.H};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    W = Workspace{W.pool_cap, W.n_cap, Pool{}, nullptr, nullptr, nullptr, nullptr, W.gen};
+    W.pool_cap = 0;
+    W.n_cap = 0;
+    int st = 0;
+    st |= dalloc(&W.P.center, pcap * MAX_DIM);
+    st |= dalloc(&W.P.level, pcap * MAX_DIM);
+    st |= dalloc(&W.P.val, pcap);
+    st |= dalloc(&W.P.err, pcap);
+    st |= dalloc(&W.P.split, pcap);
+    st |= dalloc(&W.P.q, pcap);
+    st |= dalloc(&W.P.cand, pcap);
+    st |= dalloc(&W.D, (size_t)ncap);
+    st |= dalloc(&W.S, (size_t)ncap);
+    st |= dalloc(&W.woff, (size_t)ncap + 1);
+    st |= dalloc(&W.H, 1);
+    if (st) return G3L_ERR_NOMEM;
+    W.P.stride = (long long)pcap;
+    W.pool_cap = pcap;
+    W.n_cap = ncap;
+    W.gen += 1;
+    for (auto &g : c->graphs) {
+        cudaGraphExecDestroy(g.exec);
+        cudaGraphDestroy(g.graph);
+    }
+    c->graphs.clear();
+    return G3L_OK;
+}
+
+void *eval_fn(int precision, int group)
+{
+    int kind = group / 3, term = group % 3 + 1;
+    return precision == G3L_FP64 ? eval64_kernel(kind, term) : evalmx_kernel(kind, term);
+}
+
+int eval_grid(g3l_ctx *c, void *fn)
+{
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, 0) != cudaSuccess || nb < 1) nb = 1;
+    if (c->opt.eval_blocks_per_sm > 0) nb = std::min(nb, c->opt.eval_blocks_per_sm);
+    return nb * c->nsm;
+}
+
+struct KernelArgs {
+    DevTables T;
+    IntDesc *D;
+    IntState *S;
+    Pool P;
+    BatchHdr *H;
+    long long *woff;
+    cudaGraphConditionalHandle handle;
+    int use_cond;
+};
+
+int add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *deps, size_t ndeps,
+               void *fn, int grid, int block, void **args)
+{
+    cudaKernelNodeParams kp{};
+    kp.func = fn;
+    kp.gridDim = dim3(grid);
+    kp.blockDim = dim3(block);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+    G3L_CK(cudaGraphAddKernelNode(node, g, deps, ndeps, &kp));
+    return G3L_OK;
+}
+
+int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
+{
+    Workspace &W = c->W;
+    KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 1};
+    cudaGraph_t g;
+    G3L_CK(cudaGraphCreate(&g, 0));
+    cudaGraphNode_t n_init;
+    {
+        void *args[] = {&a.D, &a.S, &a.P, &a.H};
+        int st = add_kernel(g, &n_init, nullptr, 0, init_kernel(), c->nsm * 4, 256, args);
+        if (st) return st;
+    }
+    G3L_CK(cudaGraphConditionalHandleCreate(&a.handle, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = a.handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t n_while;
+    G3L_CK(cudaGraphAddNode(&n_while, g, &n_init, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    cudaGraphNode_t n_sel, n_scan, prev;
+    {
+        void *args[] = {&a.D, &a.S, &a.P, &a.H};
+        int st = add_kernel(body, &n_sel, nullptr, 0, select_kernel(), c->nsm * 8, 256, args);
+        if (st) return st;
+    }
+    {
+        void *args[] = {&a.S, &a.woff, &a.H, &a.handle, &a.use_cond};
+        int st = add_kernel(body, &n_scan, &n_sel, 1, scan_kernel(), 1, 1024, args);
+        if (st) return st;
+    }
+    prev = n_scan;
+    for (int grp = 0; grp < NGROUPS; ++grp) {
+        if (!(gmask & (1 << grp))) continue;
+        void *fn = eval_fn(precision, grp);
+        void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
+        cudaGraphNode_t n_ev;
+        int st = add_kernel(body, &n_ev, &prev, 1, fn, eval_grid(c, fn), 128, args);
+        if (st) return st;
+        prev = n_ev;
+    }
+    cudaGraphExec_t ex;
+    G3L_CK(cudaGraphInstantiate(&ex, g, 0));
+    out = GraphEntry{W.gen, precision, gmask, g, ex};
+    return G3L_OK;
+}
+
+int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
+{
+    Workspace &W = c->W;
+    KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 0};
+    cudaStream_t s = c->stream;
+    {
+        void *args[] = {&a.D, &a.S, &a.P, &a.H};
+        G3L_CK(cudaLaunchKernel(init_kernel(), dim3(c->nsm * 4), dim3(256), args, 0, s));
+        ++*launches;
+    }
+    for (int r = 0; r < c->opt.max_rounds + 4; ++r) {
+        void *sargs[] = {&a.D, &a.S, &a.P, &a.H};
+        G3L_CK(cudaLaunchKernel(select_kernel(), dim3(c->nsm * 8), dim3(256), sargs, 0, s));
+        void *cargs[] = {&a.S, &a.woff, &a.H, &a.handle, &a.use_cond};
+        G3L_CK(cudaLaunchKernel(scan_kernel(), dim3(1), dim3(1024), cargs, 0, s));
+        *launches += 2;
+        for (int grp = 0; grp < NGROUPS; ++grp) {
+            if (!(gmask & (1 << grp))) continue;
+            void *fn = eval_fn(precision, grp);
+            void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
+            G3L_CK(cudaLaunchKernel(fn, dim3(eval_grid(c, fn)), dim3(128), args, 0, s));
+            ++*launches;
+        }
+        G3L_CK(cudaMemcpyAsync(c->h_pinned, &W.H->total_work, sizeof(long long),
+                               cudaMemcpyDeviceToHost, s));
+        G3L_CK(cudaStreamSynchronize(s));
+        if (*c->h_pinned == 0) break;
+    }
+    return G3L_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *g3l_last_error(void) { return host::last_error_cstr(); }
+int g3l_abi_version(void) { return G3L_ABI_VERSION; }
+int g3l_max_hod_slots(void) { return MAX_HOD_SLOTS; }
+
+int g3l_host_densities(const g3l_tables *t, const double hod[6], double *rho_bar, double *n_bar)
+{
+    if (!t || !hod || !rho_bar || !n_bar || t->Nz < 2 || t->Nm < 2) {
+        host::set_error("g3l_host_densities: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    host::Binning B{t->Nz, t->Nm, t->Nk, t->zmin, t->zmax, t->mmin, t->mmax, t->kmin, t->kmax};
+    host::rho_bar(B, t->Om, t->OL, t->H0, rho_bar);
+    if (host::n_bar(B, t->hmf, hod, n_bar)) return G3L_ERR_INVALID;
+    return G3L_OK;
+}
+
+int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
+{
+    if (!out) return G3L_ERR_INVALID;
+    *out = nullptr;
+    if (!t || t->Nz < 2 || t->Nm < 2 || t->Nk < 2 || !t->g || !t->p_lens1 || !t->p_lens2 || !t->w ||
+        !t->dwdz || !t->hmf || !t->b_h || !t->conc || !t->P_lin) {
+        host::set_error("g3l_ctx_create: missing tables or bins < 2");
+        return G3L_ERR_INVALID;
+    }
+    if (!(t->zmax > t->zmin) || !(t->mmax > t->mmin) || !(t->mmin > 0) || !(t->kmax > t->kmin) ||
+        !(t->kmin > 0) || !(t->H0 > 0)) {
+        host::set_error("g3l_ctx_create: invalid binning or cosmology");
+        return G3L_ERR_INVALID;
+    }
+    const size_t Nz = t->Nz, Nm = t->Nm, Nk = t->Nk;
+    const double *z1[] = {t->g, t->p_lens1, t->p_lens2, t->w, t->dwdz};
+    for (const double *a : z1)
+        if (!finite_all(a, Nz)) {
+            host::set_error("g3l_ctx_create: non-finite value in a redshift table");
+            return G3L_ERR_INVALID;
+        }
+    if (!finite_all(t->hmf, Nz * Nm) || !finite_all(t->b_h, Nz * Nm) || !finite_all(t->conc, Nz * Nm) ||
+        !finite_all(t->P_lin, Nz * Nk)) {
+        host::set_error("g3l_ctx_create: non-finite value in a 2-D table");
+        return G3L_ERR_INVALID;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || device < 0 || device >= ndev) {
+        host::set_error("g3l_ctx_create: no CUDA device");
+        return G3L_ERR_NO_DEVICE;
+    }
+    std::unique_ptr<g3l_ctx> c(new g3l_ctx);
+    c->device = device;
+    G3L_CK(cudaSetDevice(device));
+    G3L_CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
+    G3L_CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    G3L_CK(cudaEventCreate(&c->ev0));
+    G3L_CK(cudaEventCreate(&c->ev1));
+    G3L_CK(cudaMallocHost(&c->h_pinned, 64));
+    c->B = host::Binning{t->Nz, t->Nm, t->Nk, t->zmin, t->zmax, t->mmin, t->mmax, t->kmin, t->kmax};
+    c->Om = t->Om;
+    c->OL = t->OL;
+    c->Ob = t->Ob;
+    c->s8 = t->sigma8;
+    c->H0 = t->H0;
+    c->ns = t->ns;
+    c->hmf_h.assign(t->hmf, t->hmf + Nz * Nm);
+    c->rho_h.resize(Nz);
+    host::rho_bar(c->B, t->Om, t->OL, t->H0, c->rho_h.data());
+    c->hod_h.assign((size_t)MAX_HOD_SLOTS * 6, 0.0);
+    c->nbar_h.assign((size_t)MAX_HOD_SLOTS * Nz, 0.0);
+    c->hod_set.assign(MAX_HOD_SLOTS, 0);
+    c->opt.eval_blocks_per_sm = 0;
+    c->opt.eval_warps_per_block = 0;
+    c->opt.use_graph = 1;
+    c->opt.max_rounds = 4096;
+    c->opt.unlimited_pool = 1 << 20;
+
+    DevTables &T = c->T;
+    T.Nz = t->Nz;
+    T.Nm = t->Nm;
+    T.Nk = t->Nk;
+    T.clamp_k = t->clamp_k ? 1 : 0;
+    T.zmin = t->zmin;
+    T.zmax = t->zmax;
+    T.mmin = t->mmin;
+    T.mmax = t->mmax;
+    T.kmin = t->kmin;
+    T.kmax = t->kmax;
+    T.ln_mratio = std::log(t->mmax / t->mmin);
+    T.ln_kratio = std::log(t->kmax / t->kmin);
+    T.m_x0 = std::log10(t->mmin);
+    T.m_scale = t->Nm / std::log10(t->mmax / t->mmin);
+    int st = 0;
+    st |= upload(c.get(), t->g, Nz, &T.g);
+    st |= upload(c.get(), t->p_lens1, Nz, &T.p1);
+    st |= upload(c.get(), t->p_lens2, Nz, &T.p2);
+    st |= upload(c.get(), t->w, Nz, &T.w);
+    st |= upload(c.get(), t->dwdz, Nz, &T.dwdz);
+    st |= upload(c.get(), c->rho_h.data(), Nz, &T.rho_bar);
+    st |= upload(c.get(), t->hmf, Nz * Nm, &T.hmf);
+    st |= upload(c.get(), t->b_h, Nz * Nm, &T.b_h);
+    st |= upload(c.get(), t->conc, Nz * Nm, &T.conc);
+    st |= upload(c.get(), t->P_lin, Nz * Nk, &T.P_lin);
+    if (st) return st;
+    st |= dalloc(&c->d_hod, (size_t)MAX_HOD_SLOTS * 6);
+    st |= dalloc(&c->d_nbar, (size_t)MAX_HOD_SLOTS * Nz);
+    if (st) return st;
+    c->allocs.push_back(c->d_hod);
+    c->allocs.push_back(c->d_nbar);
+    G3L_CK(cudaMemset(c->d_hod, 0, sizeof(double) * MAX_HOD_SLOTS * 6));
+    G3L_CK(cudaMemset(c->d_nbar, 0, sizeof(double) * MAX_HOD_SLOTS * Nz));
+    T.hod = c->d_hod;
+    T.nbar = c->d_nbar;
+    // tie-prone mass-centre indices
+    host::TieTable tt = host::build_m_ties(c->B);
+    unsigned long long *tb;
+    int *tr, *tq;
+    st |= dalloc(&tb, tt.bits.size());
+    st |= dalloc(&tr, tt.bits.size());
+    st |= dalloc(&tq, tt.bits.size());
+    if (st) return st;
+    c->allocs.push_back(tb);
+    c->allocs.push_back(tr);
+    c->allocs.push_back(tq);
+    G3L_CK(cudaMemcpy(tb, tt.bits.data(), tt.bits.size() * 8, cudaMemcpyHostToDevice));
+    G3L_CK(cudaMemcpy(tr, tt.round_ix.data(), tt.bits.size() * 4, cudaMemcpyHostToDevice));
+    G3L_CK(cudaMemcpy(tq, tt.trunc_ix.data(), tt.bits.size() * 4, cudaMemcpyHostToDevice));
+    T.tie_m_bits = tb;
+    T.tie_m_round = tr;
+    T.tie_m_trunc = tq;
+    T.n_tie_m = (int)tt.bits.size();
+    *out = c.release();
+    return G3L_OK;
+}
+
+void g3l_ctx_destroy(g3l_ctx *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto &g : c->graphs) {
+        cudaGraphExecDestroy(g.exec);
+        cudaGraphDestroy(g.graph);
+    }
+    Workspace &W = c->W;
+    void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.q, W.P.cand,
+                    W.D,        W.S,       W.woff,  W.H};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (void *p : c->allocs) cudaFree(p);
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int g3l_set_hod(g3l_ctx *c, int slot, const double params[6])
+{
+    if (!c || !params || slot < 0 || slot >= MAX_HOD_SLOTS) {
+        host::set_error("g3l_set_hod: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    for (int k = 0; k < 6; ++k)
+        if (!std::isfinite(params[k])) {
+            host::set_error("g3l_set_hod: non-finite HOD parameter");
+            return G3L_ERR_INVALID;
+        }
+    if (!(params[2] > 0) || !(params[3] != 0) || !(params[4] > 0)) {
+        host::set_error("g3l_set_hod: Mth, M' must be > 0 and sigma != 0");
+        return G3L_ERR_INVALID;
+    }
+    const int Nz = c->B.Nz;
+    std::vector<double> nb(Nz);
+    if (host::n_bar(c->B, c->hmf_h.data(), params, nb.data())) {
+        host::set_error("g3l_set_hod: n_bar integration failed");
+        return G3L_ERR_INVALID;
+    }
+    std::copy(params, params + 6, c->hod_h.begin() + 6 * slot);
+    std::copy(nb.begin(), nb.end(), c->nbar_h.begin() + (size_t)Nz * slot);
+    c->hod_set[slot] = 1;
+    G3L_CK(cudaSetDevice(c->device));
+    G3L_CK(cudaMemcpyAsync(c->d_hod + 6 * slot, params, 6 * sizeof(double), cudaMemcpyHostToDevice,
+                           c->stream));
+    G3L_CK(cudaMemcpyAsync(c->d_nbar + (size_t)Nz * slot, c->nbar_h.data() + (size_t)Nz * slot,
+                           Nz * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    G3L_CK(cudaStreamSynchronize(c->stream));
+    return G3L_OK;
+}
+
+int g3l_set_correlation(g3l_ctx *c, double A, double eps)
+{
+    if (!c || !std::isfinite(A) || !std::isfinite(eps)) return G3L_ERR_INVALID;
+    c->A = A;
+    c->eps = eps;
+    c->T.A = A;
+    c->T.eps = eps;
+    for (auto &g : c->graphs) {  // the tables struct is baked into the graph's kernel args
+        cudaGraphExecDestroy(g.exec);
+        cudaGraphDestroy(g.graph);
+    }
+    c->graphs.clear();
+    return G3L_OK;
+}
+
+int g3l_get_densities(g3l_ctx *c, int slot, double *rho, double *nbar)
+{
+    if (!c || slot < 0 || slot >= MAX_HOD_SLOTS || !c->hod_set[slot]) return G3L_ERR_INVALID;
+    const int Nz = c->B.Nz;
+    if (rho) std::copy(c->rho_h.begin(), c->rho_h.end(), rho);
+    if (nbar) std::copy(c->nbar_h.begin() + (size_t)Nz * slot, c->nbar_h.begin() + (size_t)Nz * (slot + 1), nbar);
+    return G3L_OK;
+}
+
+int g3l_get_options(g3l_ctx *c, g3l_options *o)
+{
+    if (!c || !o) return G3L_ERR_INVALID;
+    *o = c->opt;
+    return G3L_OK;
+}
+
+int g3l_set_options(g3l_ctx *c, const g3l_options *o)
+{
+    if (!c || !o || o->max_rounds < 1 || o->unlimited_pool < 16) return G3L_ERR_INVALID;
+    c->opt = *o;
+    for (auto &g : c->graphs) {
+        cudaGraphExecDestroy(g.exec);
+        cudaGraphDestroy(g.graph);
+    }
+    c->graphs.clear();
+    return G3L_OK;
+}
+
+int g3l_get_stats(g3l_ctx *c, g3l_stats *s)
+{
+    if (!c || !s) return G3L_ERR_INVALID;
+    *s = c->stats;
+    return G3L_OK;
+}
+
+int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_result *out)
+{
+    if (!c || n < 0 || (n > 0 && (!items || !out)) ||
+        (precision != G3L_FP64 && precision != G3L_MIXED)) {
+        host::set_error("g3l_eval: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    if (n == 0) return G3L_OK;
+    if (precision == G3L_MIXED && !evalmx_kernel(0, 1)) {
+        host::set_error("g3l_eval: mixed-precision kernels not built");
+        return G3L_ERR_INVALID;
+    }
+    for (int i = 0; i < n; ++i) {
+        const g3l_integral &it = items[i];
+        bool ok = (it.kind == G3L_NNMAP || it.kind == G3L_NMAPMAP) && it.term >= 1 && it.term <= 3 &&
+                  it.hod1 >= 0 && it.hod1 < MAX_HOD_SLOTS && c->hod_set[it.hod1] &&
+                  std::isfinite(it.rtol) && it.rtol >= 0;
+        if (ok && it.kind == G3L_NNMAP)
+            ok = it.hod2 >= 0 && it.hod2 < MAX_HOD_SLOTS && c->hod_set[it.hod2];
+        for (int k = 0; k < 3 && ok; ++k) ok = std::isfinite(it.theta[k]) && it.theta[k] > 0;
+        if (!ok) {
+            host::set_error("g3l_eval: invalid integral " + std::to_string(i) +
+                            " (kind, term, unset HOD slot, theta or rtol)");
+            return G3L_ERR_INVALID;
+        }
+    }
+    G3L_CK(cudaSetDevice(c->device));
+    // order by group
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    auto grp = [&](int i) { return items[i].kind * 3 + items[i].term - 1; };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return grp(a) < grp(b); });
+    std::vector<IntDesc> D(n);
+    BatchHdr H{};
+    H.n = n;
+    int gmask = 0;
+    long long base = 0;
+    for (int r = 0; r < n; ++r) {
+        const g3l_integral &it = items[order[r]];
+        IntDesc &d = D[r];
+        std::memset(&d, 0, sizeof d);
+        for (int k = 0; k < 3; ++k) d.theta[k] = it.theta[k];
+        double lo[MAX_DIM], hi[MAX_DIM];
+        d.dim = c->B.bounds(it.term, lo, hi);
+        for (int k = 0; k < d.dim; ++k) {
+            d.c0[k] = 0.5 * (lo[k] + hi[k]);
+            d.hw0[k] = 0.5 * (hi[k] - lo[k]);
+        }
+        double vol = 1;
+        for (int k = 0; k < d.dim; ++k) vol *= 2 * d.hw0[k];
+        d.rootvol = vol;
+        d.rtol = it.rtol;
+        d.scale = 1.0;
+        d.max_eval = it.max_eval;
+        d.kind = it.kind;
+        d.term = it.term;
+        d.npts = rule_points(d.dim);
+        d.hod1 = it.hod1;
+        d.hod2 = it.kind == G3L_NNMAP ? it.hod2 : it.hod1;
+        d.same = d.hod1 == d.hod2;
+        unsigned long long cap;
+        if (it.max_eval) {
+            unsigned long long np = d.npts;
+            cap = 3 + (it.max_eval + np) / (2 * np);
+        } else {
+            cap = c->opt.unlimited_pool;
+        }
+        if (cap > (1ull << 30)) {
+            host::set_error("g3l_eval: max_eval too large for one region pool");
+            return G3L_ERR_INVALID;
+        }
+        d.cap = (int)cap;
+        d.base = base;
+        base += (long long)cap;
+        gmask |= 1 << grp(order[r]);
+    }
+    for (int g = 0, r = 0; g <= NGROUPS; ++g) {
+        while (r < n && grp(order[r]) < g) ++r;
+        H.gbeg[g] = r;
+    }
+    H.gbeg[NGROUPS] = n;
+    H.max_rounds = c->opt.max_rounds;
+    int st = ensure_workspace(c, n, (size_t)base);
+    if (st) return st;
+    Workspace &W = c->W;
+    G3L_CK(cudaMemcpyAsync(W.D, D.data(), sizeof(IntDesc) * n, cudaMemcpyHostToDevice, c->stream));
+    G3L_CK(cudaMemcpyAsync(W.H, &H, sizeof(BatchHdr), cudaMemcpyHostToDevice, c->stream));
+    int launches = 0;
+    G3L_CK(cudaEventRecord(c->ev0, c->stream));
+    if (c->opt.use_graph) {
+        GraphEntry *ge = nullptr;
+        for (auto &g : c->graphs)
+            if (g.gen == W.gen && g.precision == precision && g.gmask == gmask) ge = &g;
+        if (!ge) {
+            GraphEntry e;
+            st = build_graph(c, precision, gmask, e);
+            if (st) return st;
+            c->graphs.push_back(e);
+            ge = &c->graphs.back();
+        }
+        G3L_CK(cudaGraphLaunch(ge->exec, c->stream));
+        launches = -1;  // filled from the round count below
+    } else {
+        st = run_host_loop(c, precision, gmask, &launches);
+        if (st) return st;
+    }
+    G3L_CK(cudaEventRecord(c->ev1, c->stream));
+    std::vector<IntState> S(n);
+    G3L_CK(cudaMemcpyAsync(S.data(), W.S, sizeof(IntState) * n, cudaMemcpyDeviceToHost, c->stream));
+    BatchHdr Hout;
+    G3L_CK(cudaMemcpyAsync(&Hout, W.H, sizeof(BatchHdr), cudaMemcpyDeviceToHost, c->stream));
+    G3L_CK(cudaStreamSynchronize(c->stream));
+    G3L_CK(cudaGetLastError());
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    int ngroups = __builtin_popcount((unsigned)gmask);
+    g3l_stats &sx = c->stats;
+    sx = g3l_stats{};
+    sx.rounds = (uint64_t)Hout.rounds_done;
+    sx.kernel_launches = launches >= 0 ? (uint64_t)launches
+                                       : (uint64_t)(1 + (Hout.rounds_done + 1) * (2 + ngroups));
+    sx.regions_evaluated = Hout.regions;
+    sx.tie_fallbacks = Hout.ties;
+    sx.small_arg_fp64 = Hout.small_arg;
+    sx.device_ms = ms;
+    int first_bad = G3L_OK;
+    uint64_t pts = 0;
+    for (int r = 0; r < n; ++r) {
+        const IntDesc &d = D[r];
+        const IntState &s = S[r];
+        g3l_result &o = out[order[r]];
+        o.val = s.val * d.scale;
+        o.err = s.err * d.scale;
+        o.neval = s.neval;
+        o.status = s.done ? s.status : G3L_ERR_ROUNDS;
+        o.rounds = s.rounds;
+        o.result = host::apply_prefactor(d.kind, d.term, c->H0, c->Om, o.val);
+        pts += s.neval;
+        if (o.status && !first_bad) first_bad = o.status;
+    }
+    sx.points_evaluated = pts;
+    if (first_bad) host::set_error("g3l_eval: an integral ended with status " + std::to_string(first_bad));
+    return first_bad;
+}
+
+int g3l_submit(g3l_ctx *c, const g3l_integral *items, int n, int precision, int64_t *ticket)
+{
+    if (!c || !ticket) return G3L_ERR_INVALID;
+    std::vector<g3l_result> res(n > 0 ? n : 0);
+    int st = g3l_eval(c, items, n, precision, res.data());
+    *ticket = c->next_ticket++;
+    c->tickets[*ticket] = {st, std::move(res)};
+    return G3L_OK;
+}
+
+int g3l_poll(g3l_ctx *c, int64_t ticket, g3l_result *out, int wait)
+{
+    (void)wait;
+    if (!c) return G3L_ERR_INVALID;
+    auto it = c->tickets.find(ticket);
+    if (it == c->tickets.end()) return G3L_ERR_INVALID;
+    if (out) std::copy(it->second.second.begin(), it->second.second.end(), out);
+    int st = it->second.first;
+    c->tickets.erase(it);
+    return st;
+}
+
+int g3l_cancel(g3l_ctx *c, int64_t ticket)
+{
+    if (!c) return G3L_ERR_INVALID;
+    return c->tickets.count(ticket) ? G3L_OK : G3L_ERR_INVALID;
+}
+
+}  // extern "C"

@@ -1,0 +1,156 @@
+// host_model.cpp -- host parts of the model: binning, densities, prefactors, tie table.
+//
+// Everything here runs once per table set or per HOD vector, in FP64 with the
+// reference's expressions (compiled with -ffp-contract=off), so that rho_bar,
+// n_bar and the integration bounds equal the reference's bit for bit on the
+// same libm.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "host_internal.h"
+
+namespace g3l {
+namespace host {
+
+namespace {
+thread_local std::string g_last_error;
+constexpr double kPi = 3.14159;          // truncated pi (src/constants.h:15)
+constexpr double kC = 2.99792e5;         // km/s (src/constants.h:39)
+constexpr double kMpcInKm = 3.086e19;    // src/Cosmology.h:28
+constexpr double kG = 1.327e11;          // src/Cosmology.h:27
+}  // namespace
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+const char *last_error_cstr() { return g_last_error.c_str(); }
+
+double Binning::mmax_integral() const
+{
+    return std::exp(std::log(mmin) + std::log(mmax / mmin) * (Nm - 1) / Nm);
+}
+double Binning::zmax_integral() const { return zmax - (zmax - zmin) / Nz; }
+
+int Binning::bounds(int term, double *xmin, double *xmax) const
+{
+    const double lm0 = std::log10(mmin), lm1 = std::log10(mmax_integral());
+    int d = 0;
+    xmin[d] = std::log10(0.1); xmax[d++] = std::log10(1e6);
+    xmin[d] = std::log10(0.1); xmax[d++] = std::log10(1e6);
+    xmin[d] = 0; xmax[d++] = 2 * kPi;
+    for (int j = 0; j < term; ++j) {
+        xmin[d] = lm0;
+        xmax[d++] = lm1;
+    }
+    xmin[d] = zmin;
+    xmax[d++] = zmax_integral();
+    return d;
+}
+
+void rho_bar(const Binning &B, double Om, double OL, double H0, double *out)
+{
+    const double rho_crit = 3 * H0 * H0 * kMpcInKm / 8 / kPi / kG;
+    for (int i = 0; i < B.Nz; ++i) {
+        double z = B.zmin + i * (B.zmax - B.zmin) / B.Nz;
+        double E = Om * (1 + z) * (1 + z) * (1 + z) + OL;
+        out[i] = Om * (1 + z) * (1 + z) * (1 + z) / E * rho_crit;
+    }
+}
+
+namespace {
+struct NbarCtx {
+    const Binning *B;
+    const double *hmf;
+    const double *hod;  // f, alpha, Mth, sigma, M', beta
+    double z;
+};
+
+int nbar_integrand(unsigned ndim, size_t npt, const double *x, void *fdata, unsigned, double *fv)
+{
+    const NbarCtx *C = (const NbarCtx *)fdata;
+    const Binning &B = *C->B;
+    const double *h = C->hod;
+    for (size_t i = 0; i < npt; ++i) {
+        double m = std::pow(10, x[i * ndim]);
+        double Nc = 0.5 * h[1] * (1 + std::erf(std::log(m / h[2]) / h[3] / 1.414213562));
+        double Ns = 0.5 * (1 + std::erf(std::log(m / h[2]) / h[3] / 1.414213562)) *
+                    std::pow(m / h[4], h[5]);
+        int m_ix = (int)std::round(std::log(m / B.mmin) * B.Nm / std::log(B.mmax / B.mmin));
+        int z_ix = (int)std::round((C->z - B.zmin) * B.Nz / (B.zmax - B.zmin));
+        fv[i] = m * C->hmf[(int)(z_ix * B.Nm + m_ix)] * (Nc + Ns);
+    }
+    return 0;
+}
+}  // namespace
+
+int n_bar(const Binning &B, const double *hmf, const double hod[6], double *out)
+{
+    const double lo[1] = {std::log10(B.mmin)};
+    const double hi[1] = {std::log10(B.mmax_integral())};
+    const double ln10 = std::log(10.0);
+    for (int i = 0; i < B.Nz; ++i) {
+        NbarCtx C{&B, hmf, hod, B.zmin + i * (B.zmax - B.zmin) / B.Nz};
+        double val, err;
+        if (cubature(1, nbar_integrand, &C, lo, hi, 0, 0, 1e-4, &val, &err, nullptr)) return 1;
+        out[i] = ln10 * val;
+    }
+    return 0;
+}
+
+double apply_prefactor(int kind, int term, double H0, double Om, double raw)
+{
+    const double l10 = std::log(10.0);
+    double r;
+    if (kind == 0) r = raw * 3 * H0 * H0 * Om / 2 / kC / kC;
+    else r = raw * 9 * std::pow(H0, 4) * std::pow(Om, 2) / 4 / std::pow(kC, 4);
+    for (int i = 0; i < term + 2; ++i) r = r * l10;
+    return r / (2 * kPi) / (2 * kPi) / (2 * kPi);
+}
+
+// Region centres along a mass dimension are reached by repeated exact bisection of
+// [log10 mmin, log10 mmax_integral]; at depth L the centre sits at (2i+1)/2^(L+1) of
+// the range, i.e. at index argument (2i+1)(Nm-1)/2^(L+1).  With Nm-1 = 2^a b (b odd)
+// that argument is a half-integer (a tie of round()) at L = a and an integer (a tie
+// of the truncation) at L < a.  Those centres are enumerated with the same FP64
+// operations as the cut, and their indices evaluated with the reference's own
+// expression on this host.
+TieTable build_m_ties(const Binning &B)
+{
+    TieTable T;
+    int a = 0;
+    for (int v = B.Nm - 1; v > 0 && !(v & 1); v >>= 1) ++a;
+    if (a > 12) a = 12;
+    const double lo = std::log10(B.mmin), hi = std::log10(B.mmax_integral());
+    struct Node { double c; int L; };
+    std::vector<Node> stack{{0.5 * (lo + hi), 0}};
+    const double hw0 = 0.5 * (hi - lo);
+    std::vector<std::pair<unsigned long long, std::pair<int, int>>> rows;
+    while (!stack.empty()) {
+        Node nd = stack.back();
+        stack.pop_back();
+        double m = std::pow(10, nd.c);
+        double arg = std::log(m / B.mmin) * B.Nm / std::log(B.mmax / B.mmin);
+        unsigned long long bits;
+        std::memcpy(&bits, &nd.c, sizeof bits);
+        rows.push_back({bits, {(int)std::round(arg), (int)arg}});
+        if (nd.L < a) {
+            double hwc = std::ldexp(hw0, -(nd.L + 1));
+            stack.push_back({nd.c - hwc, nd.L + 1});
+            stack.push_back({nd.c + hwc, nd.L + 1});
+        }
+    }
+    std::sort(rows.begin(), rows.end());
+    rows.erase(std::unique(rows.begin(), rows.end(),
+                           [](const auto &x, const auto &y) { return x.first == y.first; }),
+               rows.end());
+    for (auto &r : rows) {
+        T.bits.push_back(r.first);
+        T.round_ix.push_back(r.second.first);
+        T.trunc_ix.push_back(r.second.second);
+    }
+    return T;
+}
+
+}  // namespace host
+}  // namespace g3l

@@ -1,0 +1,168 @@
+/*
+ * g3l_gpu.h -- C ABI of libg3lgpu.so, the GB300 (sm_103a) engine for the
+ * halo-model aperture statistics <N N M_ap> (NNMap) and <N M_ap M_ap> (NMapMap).
+ *
+ * The reference computes each term by calling the host cubature hcubature_v
+ * (src/hcubature.cpp:1059-1067) with a vectorised integrand callback that
+ * copies the points to the GPU every refinement round
+ * (src/NNMap_Model.cu:418-542).  This library keeps the whole adaptive
+ * Genz-Malik cubature on the device: region pools, rule evaluation,
+ * bisection, error bookkeeping and the refinement loop (a CUDA-graph
+ * conditional WHILE node) never return to the host until every integral of a
+ * call is finished.
+ *
+ * Conventions
+ *  - Plain C types only; all pointers are host pointers unless stated.
+ *  - Every entry point returns an int status (G3L_OK = 0); the library never
+ *    calls exit() (the reference does, src/cuda_helpers.h:11-19).
+ *    g3l_last_error() returns a thread-local message for the last failure.
+ *  - Thread safety: one context may be used by one host thread at a time;
+ *    distinct contexts are independent.
+ */
+#ifndef G3L_GPU_H
+#define G3L_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define G3L_ABI_VERSION 1
+
+enum g3l_status {
+    G3L_OK = 0,
+    G3L_ERR_INVALID = 1,    /* bad argument */
+    G3L_ERR_CUDA = 2,       /* CUDA runtime error (see g3l_last_error) */
+    G3L_ERR_NOMEM = 3,      /* device or host allocation failed */
+    G3L_ERR_POOL = 4,       /* region pool exhausted (maxEval == 0 beyond the pool cap) */
+    G3L_ERR_NONFINITE = 5,  /* an integral's running value or error became NaN/Inf */
+    G3L_ERR_CANCELLED = 6,  /* the call was cancelled through g3l_cancel */
+    G3L_ERR_ROUNDS = 7,     /* refinement-round cap reached */
+    G3L_ERR_NO_DEVICE = 8,  /* no usable CUDA device */
+    G3L_ERR_BUSY = 9        /* serving queue full */
+};
+
+enum g3l_kind { G3L_NNMAP = 0, G3L_NMAPMAP = 1 };
+
+enum g3l_precision {
+    G3L_FP64 = 0,  /* all-FP64 integrand, same operation order as the reference */
+    G3L_MIXED = 1  /* FP32 integrand, FP64-class accumulation and decisions */
+};
+
+/* Lookup tables and binning (src/NNMap_Model.h:36-58).  The reference uses one
+ * Nbins for z, m and k; Nz, Nm and Nk may differ here.  Grids:
+ *   z_i = zmin + i (zmax-zmin)/Nz,   m_j = mmin (mmax/mmin)^(j/Nm),
+ *   k_j = kmin (kmax/kmin)^(j/Nk).
+ * 2-D tables are z-major: hmf[i*Nm + j], P_lin[i*Nk + j].  The arrays are
+ * copied at creation; the caller keeps ownership. */
+typedef struct g3l_tables {
+    int Nz, Nm, Nk;
+    double zmin, zmax, mmin, mmax, kmin, kmax;
+    const double *g, *p_lens1, *p_lens2, *w, *dwdz; /* [Nz] */
+    const double *hmf, *b_h, *conc;                 /* [Nz*Nm] */
+    const double *P_lin;                            /* [Nz*Nk] */
+    double Om, OL, Ob, sigma8, H0, ns;              /* flat LCDM (src/Cosmology.h:18-24) */
+    int clamp_k; /* nonzero: clamp the P_lin k index at Nk-1.  The reference reads
+                    past the row instead (src/NNMap_Model.cu:826-839). */
+} g3l_tables;
+
+/* One integral: a term of NNMap or NMapMap for one aperture triplet. */
+typedef struct g3l_integral {
+    int kind;          /* G3L_NNMAP or G3L_NMAPMAP */
+    int term;          /* 1, 2 or 3 (1-, 2-, 3-halo: 5, 6, 7 dimensions) */
+    int hod1, hod2;    /* HOD slots of the two lens populations (NMapMap: hod1 only).
+                          hod1 == hod2 selects the same-population satellite-pair
+                          branch, as the reference's pointer test does (src/HOD.cu:82). */
+    double theta[3];   /* aperture radii [rad] */
+    double rtol;       /* relative tolerance */
+    uint64_t max_eval; /* evaluation cap; 0 = unlimited (bounded by the pool cap) */
+} g3l_integral;
+
+typedef struct g3l_result {
+    double val, err;   /* raw integral and error estimate (before the prefactor) */
+    double result;     /* val times the reference's prefactor chain */
+    uint64_t neval;    /* integrand evaluations */
+    int32_t status;    /* g3l_status of this integral */
+    int32_t rounds;    /* refinement rounds */
+} g3l_result;
+
+typedef struct g3l_ctx g3l_ctx;
+
+/* Create a context on `device`: copies the tables to device memory and sets up
+ * one stream.  Replaces the table uploads in the NNMap_Model / NMapMap_Model
+ * constructors (src/NNMap_Model.cu:15-101, src/NMapMap_Model.cu:14-91). */
+int g3l_ctx_create(const g3l_tables *tables, int device, g3l_ctx **out);
+void g3l_ctx_destroy(g3l_ctx *ctx);
+
+/* Set HOD slot `slot` (0 <= slot < g3l_max_hod_slots()) to
+ * params = {f, alpha, Mth, sigma, M', beta} (the reference's device order,
+ * src/HOD.cu:15-20) and compute rho_bar(z) and n_bar(z) for it with the 1-D
+ * adaptive Gauss-Kronrod integral of the reference (updateDensities,
+ * src/NNMap_Model.cu:244-297). */
+int g3l_set_hod(g3l_ctx *ctx, int slot, const double params[6]);
+int g3l_max_hod_slots(void);
+/* Satellite-pair correlation parameters A, epsilon (src/HOD.cu:90). */
+int g3l_set_correlation(g3l_ctx *ctx, double A, double epsilon);
+/* n_bar(z) of a slot and rho_bar(z) as computed by g3l_set_hod ([Nz] each). */
+int g3l_get_densities(g3l_ctx *ctx, int slot, double *rho_bar, double *n_bar);
+
+/* Integrate n items in one device-resident launch (all items refine
+ * concurrently; the host waits once at the end).  Replaces the per-term
+ * methods NNMap_1h/2h/3h and NMapMap_1h/2h/3h (src/NNMap_Model.cu:299-373,
+ * src/NMapMap_Model.cu:169-238) and the batch loop calculateAll
+ * (src/NNMap_Model.cu:382-415).  Returns the first non-OK item status, or OK. */
+int g3l_eval(g3l_ctx *ctx, const g3l_integral *items, int n, int precision,
+             g3l_result *out);
+
+/* Asynchronous form for serving: enqueue on the context's stream and return a
+ * ticket; g3l_poll returns G3L_OK with results when done, G3L_ERR_BUSY while
+ * running.  g3l_cancel stops the refinement loop of a running ticket. */
+int g3l_submit(g3l_ctx *ctx, const g3l_integral *items, int n, int precision,
+               int64_t *ticket);
+int g3l_poll(g3l_ctx *ctx, int64_t ticket, g3l_result *out, int wait);
+int g3l_cancel(g3l_ctx *ctx, int64_t ticket);
+
+/* Engine options. */
+typedef struct g3l_options {
+    int eval_blocks_per_sm;  /* 0 = automatic */
+    int eval_warps_per_block;/* 0 = automatic */
+    int use_graph;           /* 1 (default): device-resident loop in a CUDA graph;
+                                0: host-driven rounds (diagnostics only) */
+    int max_rounds;          /* refinement-round cap (default 4096) */
+    uint64_t unlimited_pool; /* region-pool capacity per integral when max_eval == 0 */
+} g3l_options;
+int g3l_get_options(g3l_ctx *ctx, g3l_options *opt);
+int g3l_set_options(g3l_ctx *ctx, const g3l_options *opt);
+
+/* Per-call diagnostics of the last g3l_eval: kernel launches, rounds, regions,
+ * device time, and counters of the exact-index fallbacks. */
+typedef struct g3l_stats {
+    uint64_t kernel_launches;
+    uint64_t rounds;
+    uint64_t regions_evaluated;
+    uint64_t points_evaluated;
+    uint64_t tie_fallbacks;   /* nearest-bin indices resolved by the exact FP64 path */
+    uint64_t small_arg_fp64;  /* NFW profile evaluations on the small-k r_s FP64 branch */
+    double device_ms;         /* device time of the whole call (CUDA events) */
+    double eval_ms;           /* of which in the rule-evaluation kernels */
+} g3l_stats;
+int g3l_get_stats(g3l_ctx *ctx, g3l_stats *st);
+
+const char *g3l_last_error(void);
+int g3l_abi_version(void);
+
+/* The reference's cubature entry point for host integrands (the 1-D
+ * precomputations and Cosmology::comovingDistance call it), with the same
+ * contract as src/cubature.h:55-57 and :90-94. */
+typedef int (*g3l_integrand_v)(unsigned ndim, size_t npt, const double *x, void *fdata,
+                               unsigned fdim, double *fval);
+int g3l_hcubature_v(unsigned fdim, g3l_integrand_v f, void *fdata, unsigned dim,
+                    const double *xmin, const double *xmax, size_t maxEval, double reqAbsError,
+                    double reqRelError, int norm, double *val, double *err);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* G3L_GPU_H */

@@ -180,8 +180,12 @@ static double plin(const orc_model *M, int z_ix, double k)
 {
     int k_ix = (int)round(k_arg(M, k));
     if (k_ix >= 0) {
+        /* clamp_k: stay in the z row.  Otherwise read the flat array as the
+         * reference does, stopping at its last element instead of past it. */
         if (M->clamp_k && k_ix > M->Nk - 1) k_ix = M->Nk - 1;
-        return M->P_lin[z_ix * M->Nk + k_ix];
+        long flat = (long)z_ix * M->Nk + k_ix;
+        if (flat > (long)M->Nz * M->Nk - 1) flat = (long)M->Nz * M->Nk - 1;
+        return M->P_lin[flat];
     }
     return M->P_lin[z_ix * M->Nk] / M->kmin * k;
 }

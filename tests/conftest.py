@@ -22,13 +22,16 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def golden():
+    return load_golden()
+
+
+def load_golden():
     return dict(np.load(GOLDEN))
 
 
-@pytest.fixture(scope="session")
-def golden_tables(golden):
+def tables_from_golden(g):
+    """The N=64 tables the golden vectors were computed on."""
     from g3lhalo_gb300.tables import Cosmology, Tables
-    g = golden
     meta = g["tab_meta"]
     c = g["cosmo"]
     cos = Cosmology(Om=c[0], OL=c[1], Ob=c[2], s8=c[3], h=c[4] / 100.0, ns=c[5])
@@ -37,6 +40,11 @@ def golden_tables(golden):
                   g=g["tab_g"], p_lens1=g["tab_p_lens1"], p_lens2=g["tab_p_lens2"], w=g["tab_w"],
                   dwdz=g["tab_dwdz"], hmf=g["tab_hmf"], P_lin=g["tab_P_lin"], b_h=g["tab_b_h"],
                   conc=g["tab_conc"])
+
+
+@pytest.fixture(scope="session")
+def golden_tables(golden):
+    return tables_from_golden(golden)
 
 
 def assert_close(a, b, rtol_exact=0.0, rtol_other=1e-9):
