@@ -54,7 +54,8 @@ class Result(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("eval_blocks_per_sm", C.c_int), ("eval_warps_per_block", C.c_int),
-                ("use_graph", C.c_int), ("max_rounds", C.c_int), ("unlimited_pool", C.c_uint64)]
+                ("use_graph", C.c_int), ("max_rounds", C.c_int), ("unlimited_pool", C.c_uint64),
+                ("small_arg", C.c_double)]
 
 
 class Stats(C.Structure):

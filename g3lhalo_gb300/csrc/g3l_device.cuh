@@ -54,14 +54,17 @@ struct DevTables {
     const unsigned long long *tie_m_bits;
     const int *tie_m_round, *tie_m_trunc;
     int n_tie_m;
-    // FP32 tables of the mixed-precision path (scaled; see eval_mixed.cu)
-    const float *f_hmf, *f_bh, *f_conc, *f_plin, *f_lnplin;
-    const float *f_zA, *f_zB;       // per-z factors of NNMap / NMapMap
-    const float *f_w, *f_invw, *f_rho, *f_rhot, *f_nbar; // [Nz] / [slot][Nz]
-    const float2 *f_kb;             // per-z double-float (ln(w kmin)) * Nk / ln(kmax/kmin)
-    float2 k_a;                     // double-float ln(10) * Nk / ln(kmax/kmin)
-    float2 m_s2, m_x02;             // double-float m_scale, m_x0
-    float2 z_s2, z_02;              // double-float Nz/(zmax-zmin), zmin
+    // mixed-precision path: FP32 tables in scaled units (see eval_mixed.cu)
+    const float *f_hmf, *f_bh, *f_conc, *f_plin;  // [Nz*Nm] x3, [Nz*Nk]
+    const float *f_zA, *f_zB, *f_kw, *f_k200;      // [Nz]
+    const float *f_nbar;                           // [slot][Nz]
+    const float *f_hodp;                           // [slot][8]
+    const float2 *f_kb;                            // [Nz] (ln w + ln kmin) Nk / ln(kmax/kmin)
+    float2 k_a, m_s2, m_x02, z_s2, z_02, lnkmin2, kscale2;  // double-float constants
+    float fA, feps, small_arg;
+    const unsigned long long *tie_z_bits;
+    const int *tie_z_round, *tie_z_trunc;
+    int n_tie_z;
 };
 
 struct IntDesc {
@@ -77,6 +80,8 @@ struct IntDesc {
     int hod1, hod2, same; // HOD slots; same = same-population branch
     int kind, term, dim, npts;
     int pad;
+    float2 hwl[MAX_DIM][3];  // mixed path: hw0 * {lambda2, lambda4, lambda5} as double-floats
+    float th_s[3];           // mixed path: theta * 1e3 (l in units of 1e3)
 };
 
 struct IntState {

@@ -89,6 +89,10 @@ struct g3l_ctx {
     DevTables T{};
     std::vector<void *> allocs;
     double *d_hod = nullptr, *d_nbar = nullptr;
+    // mixed path
+    float *d_fnbar = nullptr, *d_fhodp = nullptr;
+    std::vector<double> sn;  // per-slot n_bar scale
+    double SH = 1, SP = 1, SZA = 1, SZB = 1;
     Workspace W;
     std::vector<GraphEntry> graphs;
     g3l_options opt{};
@@ -110,6 +114,119 @@ int upload(g3l_ctx *c, const double *src, size_t n, const double **dst)
     G3L_CK(cudaMemcpy(p, src, n * sizeof(double), cudaMemcpyHostToDevice));
     *dst = p;
     return G3L_OK;
+}
+
+float2 dsplit(double x)
+{
+    float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+
+template <typename T>
+int upload_t(g3l_ctx *c, const std::vector<T> &src, const T **dst)
+{
+    T *p;
+    int st = dalloc(&p, src.size());
+    if (st) return st;
+    c->allocs.push_back(p);
+    G3L_CK(cudaMemcpy(p, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+    *dst = p;
+    return G3L_OK;
+}
+
+constexpr double kL0 = 1e3;   // l unit of the FP32 integrand
+constexpr double kM0 = 1e12;  // m unit of the FP32 integrand
+
+// Mixed-path tables: FP32 in scaled units plus double-float constants.
+int prepare_mixed(g3l_ctx *c, const g3l_tables *t)
+{
+    DevTables &T = c->T;
+    const int Nz = t->Nz, Nm = t->Nm, Nk = t->Nk;
+    double mh = 0, mp = 0, mza = 0, mzb = 0;
+    for (size_t i = 0; i < (size_t)Nz * Nm; ++i) mh = std::max(mh, std::fabs(t->hmf[i]));
+    for (size_t i = 0; i < (size_t)Nz * Nk; ++i) mp = std::max(mp, std::fabs(t->P_lin[i]));
+    std::vector<double> zA(Nz), zB(Nz);
+    for (int i = 0; i < Nz; ++i) {
+        const double w = t->w[i], rho = c->rho_h[i];
+        zA[i] = t->g[i] * t->p_lens1[i] * t->p_lens2[i] / (t->dwdz[i] * w * w * w * rho);
+        zB[i] = t->g[i] * t->g[i] * t->p_lens1[i] / (t->dwdz[i] * w * w * rho * rho);
+        if (std::isfinite(zA[i])) mza = std::max(mza, std::fabs(zA[i]));
+        if (std::isfinite(zB[i])) mzb = std::max(mzb, std::fabs(zB[i]));
+    }
+    c->SH = mh > 0 ? 1 / mh : 1;
+    c->SP = mp > 0 ? 1 / mp : 1;
+    c->SZA = mza > 0 ? 1 / mza : 1;
+    c->SZB = mzb > 0 ? 1 / mzb : 1;
+    std::vector<float> fh(Nz * (size_t)Nm), fb(Nz * (size_t)Nm), fc(Nz * (size_t)Nm),
+        fp(Nz * (size_t)Nk);
+    for (size_t i = 0; i < fh.size(); ++i) {
+        fh[i] = (float)(t->hmf[i] * c->SH);
+        fb[i] = (float)t->b_h[i];
+        fc[i] = (float)t->conc[i];
+    }
+    for (size_t i = 0; i < fp.size(); ++i) fp[i] = (float)(t->P_lin[i] * c->SP);
+    std::vector<float> fza(Nz), fzb(Nz), fkw(Nz), fk200(Nz);
+    std::vector<float2> fkb(Nz);
+    const double kscale = Nk / std::log(t->kmax / t->kmin);
+    for (int i = 0; i < Nz; ++i) {
+        fza[i] = std::isfinite(zA[i]) ? (float)(zA[i] * c->SZA) : 0.f;
+        fzb[i] = std::isfinite(zB[i]) ? (float)(zB[i] * c->SZB) : 0.f;
+        fkw[i] = (float)(kL0 / t->w[i]);
+        fk200[i] = (float)(0.239 * kM0 / (200 * c->rho_h[i]));
+        fkb[i] = dsplit((std::log(t->w[i]) + std::log(t->kmin)) * kscale);
+    }
+    int st = 0;
+    st |= upload_t(c, fh, &T.f_hmf);
+    st |= upload_t(c, fb, &T.f_bh);
+    st |= upload_t(c, fc, &T.f_conc);
+    st |= upload_t(c, fp, &T.f_plin);
+    st |= upload_t(c, fza, &T.f_zA);
+    st |= upload_t(c, fzb, &T.f_zB);
+    st |= upload_t(c, fkw, &T.f_kw);
+    st |= upload_t(c, fk200, &T.f_k200);
+    st |= upload_t(c, fkb, &T.f_kb);
+    if (st) return st;
+    T.k_a = dsplit(std::log(10.0) * kscale);
+    T.kscale2 = dsplit(kscale);
+    T.lnkmin2 = dsplit(std::log(t->kmin));
+    T.m_x02 = dsplit(std::log10(t->mmin));
+    T.m_s2 = dsplit(Nm / std::log10(t->mmax / t->mmin));
+    T.z_02 = dsplit(t->zmin);
+    T.z_s2 = dsplit(Nz / (t->zmax - t->zmin));
+    T.small_arg = (float)c->opt.small_arg;
+    st |= dalloc(&c->d_fnbar, (size_t)MAX_HOD_SLOTS * Nz);
+    st |= dalloc(&c->d_fhodp, (size_t)MAX_HOD_SLOTS * 8);
+    if (st) return st;
+    c->allocs.push_back(c->d_fnbar);
+    c->allocs.push_back(c->d_fhodp);
+    G3L_CK(cudaMemset(c->d_fnbar, 0, sizeof(float) * MAX_HOD_SLOTS * Nz));
+    G3L_CK(cudaMemset(c->d_fhodp, 0, sizeof(float) * MAX_HOD_SLOTS * 8));
+    T.f_nbar = c->d_fnbar;
+    T.f_hodp = c->d_fhodp;
+    c->sn.assign(MAX_HOD_SLOTS, 1.0);
+    host::TieTable tz = host::build_z_ties(c->B);
+    std::vector<unsigned long long> zb(tz.bits);
+    const unsigned long long *pb;
+    const int *pr, *pt;
+    st |= upload_t(c, zb, &pb);
+    st |= upload_t(c, tz.round_ix, &pr);
+    st |= upload_t(c, tz.trunc_ix, &pt);
+    if (st) return st;
+    T.tie_z_bits = pb;
+    T.tie_z_round = pr;
+    T.tie_z_trunc = pt;
+    T.n_tie_z = (int)tz.bits.size();
+    return G3L_OK;
+}
+
+// scale of the FP32 integrand of a term: true value = scaled value * scale
+double mixed_scale(const g3l_ctx *c, int kind, int term, int h1, int h2)
+{
+    const int nm = kind == 0 ? term + 1 : term + 2;
+    const double snf = kind == 0 ? c->sn[h1] * c->sn[h2] : c->sn[h1] * c->sn[h1];
+    const double sz = kind == 0 ? c->SZA : c->SZB;
+    return std::pow(kL0, 4) * std::pow(kM0, nm) * snf /
+           (std::pow(c->SH, term) * std::pow(c->SP, term - 1) * sz);
 }
 
 bool finite_all(const double *a, size_t n)
@@ -354,6 +471,7 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
     c->opt.use_graph = 1;
     c->opt.max_rounds = 4096;
     c->opt.unlimited_pool = 1 << 20;
+    c->opt.small_arg = 1e-7;
 
     DevTables &T = c->T;
     T.Nz = t->Nz;
@@ -409,6 +527,8 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
     T.tie_m_round = tr;
     T.tie_m_trunc = tq;
     T.n_tie_m = (int)tt.bits.size();
+    st = prepare_mixed(c.get(), t);
+    if (st) return st;
     *out = c.release();
     return G3L_OK;
 }
@@ -464,6 +584,20 @@ int g3l_set_hod(g3l_ctx *c, int slot, const double params[6])
                            c->stream));
     G3L_CK(cudaMemcpyAsync(c->d_nbar + (size_t)Nz * slot, c->nbar_h.data() + (size_t)Nz * slot,
                            Nz * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    // mixed path: n_bar scaled to max 1 and the occupation constants in FP32
+    double mx = 0;
+    for (double v : nb) mx = std::max(mx, std::fabs(v));
+    c->sn[slot] = mx > 0 ? 1 / mx : 1;
+    std::vector<float> fnb(Nz);
+    for (int i = 0; i < Nz; ++i) fnb[i] = (float)(nb[i] * c->sn[slot]);
+    const float2 lmth = dsplit(std::log10(params[2])), lmp = dsplit(std::log10(params[4]));
+    float hp[8] = {(float)params[0], (float)params[1], lmth.x, lmth.y,
+                   (float)(std::log(10.0) / (params[3] * 1.414213562)), lmp.x, lmp.y,
+                   (float)params[5]};
+    G3L_CK(cudaMemcpyAsync(c->d_fnbar + (size_t)Nz * slot, fnb.data(), Nz * sizeof(float),
+                           cudaMemcpyHostToDevice, c->stream));
+    G3L_CK(cudaMemcpyAsync(c->d_fhodp + 8 * slot, hp, sizeof hp, cudaMemcpyHostToDevice,
+                           c->stream));
     G3L_CK(cudaStreamSynchronize(c->stream));
     return G3L_OK;
 }
@@ -475,6 +609,8 @@ int g3l_set_correlation(g3l_ctx *c, double A, double eps)
     c->eps = eps;
     c->T.A = A;
     c->T.eps = eps;
+    c->T.fA = (float)A;
+    c->T.feps = (float)eps;
     for (auto &g : c->graphs) {  // the tables struct is baked into the graph's kernel args
         cudaGraphExecDestroy(g.exec);
         cudaGraphDestroy(g.graph);
@@ -501,8 +637,10 @@ int g3l_get_options(g3l_ctx *c, g3l_options *o)
 
 int g3l_set_options(g3l_ctx *c, const g3l_options *o)
 {
-    if (!c || !o || o->max_rounds < 1 || o->unlimited_pool < 16) return G3L_ERR_INVALID;
+    if (!c || !o || o->max_rounds < 1 || o->unlimited_pool < 16 || !(o->small_arg >= 0))
+        return G3L_ERR_INVALID;
     c->opt = *o;
+    c->T.small_arg = (float)o->small_arg;
     for (auto &g : c->graphs) {
         cudaGraphExecDestroy(g.exec);
         cudaGraphDestroy(g.graph);
@@ -569,6 +707,14 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
         double vol = 1;
         for (int k = 0; k < d.dim; ++k) vol *= 2 * d.hw0[k];
         d.rootvol = vol;
+        if (precision == G3L_MIXED) {
+            static const double lam[3] = {G3L_LAMBDA2, G3L_LAMBDA4, G3L_LAMBDA5};
+            for (int k = 0; k < d.dim; ++k)
+                for (int q = 0; q < 3; ++q) d.hwl[k][q] = dsplit(d.hw0[k] * lam[q]);
+            for (int k = 0; k < 3; ++k) d.th_s[k] = (float)(it.theta[k] * kL0);
+            const int h2 = it.kind == G3L_NNMAP ? it.hod2 : it.hod1;
+            d.rootvol = vol * mixed_scale(c, it.kind, it.term, it.hod1, h2);
+        }
         d.rtol = it.rtol;
         d.scale = 1.0;
         d.max_eval = it.max_eval;

@@ -39,6 +39,7 @@ struct TieTable {
     std::vector<int> round_ix, trunc_ix;
 };
 TieTable build_m_ties(const Binning &B);
+TieTable build_z_ties(const Binning &B);
 
 }  // namespace host
 }  // namespace g3l

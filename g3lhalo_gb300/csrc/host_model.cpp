@@ -152,5 +152,43 @@ TieTable build_m_ties(const Binning &B)
     return T;
 }
 
+// The same enumeration for the redshift axis [zmin, zmax_integral]; its index
+// arguments (z - zmin) Nz / (zmax - zmin) are exact FP64 expressions.
+TieTable build_z_ties(const Binning &B)
+{
+    TieTable T;
+    int a = 0;
+    for (int v = B.Nz - 1; v > 0 && !(v & 1); v >>= 1) ++a;
+    if (a > 12) a = 12;
+    const double lo = B.zmin, hi = B.zmax_integral();
+    struct Node { double c; int L; };
+    std::vector<Node> stack{{0.5 * (lo + hi), 0}};
+    const double hw0 = 0.5 * (hi - lo);
+    std::vector<std::pair<unsigned long long, std::pair<int, int>>> rows;
+    while (!stack.empty()) {
+        Node nd = stack.back();
+        stack.pop_back();
+        double arg = (nd.c - B.zmin) * B.Nz / (B.zmax - B.zmin);
+        unsigned long long bits;
+        std::memcpy(&bits, &nd.c, sizeof bits);
+        rows.push_back({bits, {(int)std::round(arg), (int)arg}});
+        if (nd.L < a) {
+            double hwc = std::ldexp(hw0, -(nd.L + 1));
+            stack.push_back({nd.c - hwc, nd.L + 1});
+            stack.push_back({nd.c + hwc, nd.L + 1});
+        }
+    }
+    std::sort(rows.begin(), rows.end());
+    rows.erase(std::unique(rows.begin(), rows.end(),
+                           [](const auto &x, const auto &y) { return x.first == y.first; }),
+               rows.end());
+    for (auto &r : rows) {
+        T.bits.push_back(r.first);
+        T.round_ix.push_back(r.second.first);
+        T.trunc_ix.push_back(r.second.second);
+    }
+    return T;
+}
+
 }  // namespace host
 }  // namespace g3l

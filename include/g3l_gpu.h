@@ -132,6 +132,8 @@ typedef struct g3l_options {
                                 0: host-driven rounds (diagnostics only) */
     int max_rounds;          /* refinement-round cap (default 4096) */
     uint64_t unlimited_pool; /* region-pool capacity per integral when max_eval == 0 */
+    double small_arg;        /* mixed precision: NFW profile arguments k r_s below this
+                                are evaluated in FP64 (default 1e-7) */
 } g3l_options;
 int g3l_get_options(g3l_ctx *ctx, g3l_options *opt);
 int g3l_set_options(g3l_ctx *ctx, const g3l_options *opt);
