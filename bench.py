@@ -1,0 +1,312 @@
+"""Benchmark: NNMap model evaluations per second on one GB300.
+
+One step = one model evaluation of <N N M_ap>: the 1-, 2- and 3-halo terms of
+all 220 aperture triplets theta1 <= theta2 <= theta3 from 10 log-spaced radii in
+[0.5', 16'] (660 adaptive Genz-Malik integrals over 5/6/7 dimensions), rtol 1e-4,
+an evaluation cap of 1e6 per integral (the reference's integrals never reach
+rtol 1e-4, so the cap decides the work), on synthetic tables (64 z x 128 m x
+256 k bins) and one HOD vector per step (seeded draws from the fit-sweep box).
+
+Reported (one JSON line on rank 0):
+  value       mixed-precision evals/s, device time (CUDA events) of the whole
+              refinement loop, inputs resident
+  e2e         the same through the public call (HOD update + descriptors in,
+              results out, host wall clock)
+  fp64        the plain all-FP64 form on the same device (the >= 5x comparison)
+  parity      max relative deviation of every mixed term from the FP64 form
+  roofline    the dominant rule kernel (NNMap 2-halo) against the measured FP32
+              FMA rate of this device
+  cpu_baseline the CPU oracle (restated reference CPU path, OpenMP over all host
+              cores) on a bounded sample, extrapolated to one evaluation
+--impl reference times the reference's CPU path alone (oracle/_ref where the
+reference compiled, else the oracle restatement) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "NNMap evals/s (220 triplets,1h+2h+3h,rtol 1e-4) mixed vs FP64; p50/p99 ms"
+MAX_EVAL = 1_000_000
+RTOL = 1e-4
+# FP32 operations per integrand point of the NNMap 2-halo rule kernel, from the ncu
+# instruction counts (fadd + fmul + 2 ffma, thread-level) of one launch divided by
+# the points it evaluated; see profiles/k_evalmx_nnmap2h.md.
+FLOPS_PER_POINT = {"nnmap_2h": None}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--max-eval", type=int, default=MAX_EVAL)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def workload():
+    from g3lhalo_gb300 import workloads as W
+    from g3lhalo_gb300.tables import make_tables
+    T = make_tables(Nz=64, Nm=128, Nk=256)
+    trip = W.triplets_all()
+    hods = W.hod_sweep(64, seed=12345)
+    return T, trip, hods
+
+
+def config(n_trip, me, extra=None):
+    c = {"workload": "NNMap <N1 N2 Map> 1h+2h+3h, 220 triplets theta1<=theta2<=theta3 from 10 "
+                     "log-spaced radii in [0.5,16] arcmin, rtol 1e-4, maxEval %d per integral, "
+                     "tables 64 z x 128 m x 256 k, one HOD vector per step" % me,
+         "integrals_per_step": 3 * n_trip, "max_eval": me, "rtol": RTOL,
+         "tables": {"Nz": 64, "Nm": 128, "Nk": 256, "zmin": 0.001, "zmax": 2.0,
+                    "mmin": 1e10, "mmax": 1e17, "k_h_per_mpc": [1e-4, 1e3]},
+         "l2": "no flush: each step rewrites ~0.3 GB of region pools (> 129 MB L2)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.rows, self.proc = [], None
+        self.device = device
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample(T, trip, hod, me, n_trip):
+    """Oracle on the host cores: n_trip triplets x 3 terms, extrapolated to 220."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as P
+    O = P.Oracle(T, hod, hod, clamp_k=True)
+    idx = np.linspace(0, len(trip) - 1, n_trip).astype(int)
+    t0 = time.perf_counter()
+    pts = 0
+    for i in idx:
+        for t in (1, 2, 3):
+            pts += O.term(0, t, trip[i], 1, 2, maxEval=me, rtol=RTOL)[2]
+    dt = time.perf_counter() - t0
+    per_eval = dt * len(trip) / n_trip
+    return {"value": 1.0 / per_eval, "unit": "evals/s", "cores": os.cpu_count(),
+            "kind": "port", "seconds": dt, "points_per_s": pts / dt,
+            "sample": "%d of 220 triplets x 3 terms at maxEval %d (oracle restatement of the "
+                      "reference CPU path, OpenMP over all host cores), extrapolated linearly "
+                      "to 220 triplets" % (n_trip, me)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    T, trip, hods = workload()
+    ref_kind = "port"
+    res = []
+    n_trip = 6
+    for _ in range(args.warmup):
+        pass  # the CPU path has no warm-up state; every step is measured
+    for s in range(args.steps):
+        r = cpu_sample(T, trip, hods[s % len(hods)], args.max_eval, n_trip)
+        res.append(1.0 / r["value"])
+    ms = 1000.0 * float(np.mean(res))
+    value = 1000.0 / ms
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": config(len(trip), args.max_eval),
+            "p50_ms": float(np.percentile(np.array(res) * 1e3, 50)),
+            "p99_ms": float(np.percentile(np.array(res) * 1e3, 99)),
+            "cpu_baseline": {"value": value, "unit": "evals/s", "cores": os.cpu_count(),
+                             "kind": ref_kind,
+                             "sample": "per step %d of 220 triplets x 3 terms, extrapolated" % n_trip},
+            "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist:
+            dist.barrier()
+        return
+
+    import g3lhalo_gb300 as G
+    T, trip, hods = workload()
+    ctx = G.Context(T, device=local)
+    ctx.set_hod(1, hods[0])
+
+    def specs(slot):
+        return [(G.NNMAP, t, slot, slot, tuple(th), RTOL, args.max_eval) for th in trip
+                for t in (1, 2, 3)]
+
+    # the fit loop: each step sets a new HOD vector and evaluates the model
+    def step(s, precision):
+        ctx.set_hod(0, hods[s % len(hods)])
+        return ctx.eval(specs(0), precision)
+
+    for s in range(args.warmup):
+        step(s, G.MIXED)
+    # timed region
+    clocks = Clocks(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    dev_ms, wall_ms, launches = [], [], 0
+    results = []
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        w0 = time.perf_counter()
+        r = step(args.warmup + s, G.MIXED)
+        wall_ms.append((time.perf_counter() - w0) * 1e3)
+        st = ctx.stats()
+        dev_ms.append(st["device_ms"])
+        launches += int(st["kernel_launches"])
+        results.append(r)
+    total = time.perf_counter() - t0
+    if dist:
+        import torch
+        tt = torch.tensor([sum(dev_ms), total], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_total, total = float(tt[0]) / 1e3, float(tt[1])
+    else:
+        dev_total = sum(dev_ms) / 1e3
+    clk = clocks.stop()
+    st_last = ctx.stats()
+    value = world * args.steps / dev_total
+    e2e = world * args.steps / total
+    out = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * dev_total / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 integrand, f64 accumulation/decisions",
+           "data": "synthetic: seeded tables (Sheth-Tormen, Eisenstein-Hu no-wiggle) and HOD "
+                   "vectors; no public dataset",
+           "p50_ms": float(np.percentile(dev_ms, 50)), "p99_ms": float(np.percentile(dev_ms, 99)),
+           "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": int(st_last["h2d_bytes"]),
+                   "d2h_bytes_per_step": int(st_last["d2h_bytes"]),
+                   "p50_ms": float(np.percentile(wall_ms, 50)),
+                   "p99_ms": float(np.percentile(wall_ms, 99)),
+                   "includes": "HOD update (host n_bar integrals + upload), descriptor H2D, "
+                               "device loop, result D2H"},
+           "gpu_launches": launches, "clocks": clk,
+           "stats_last_step": {k: st_last[k] for k in ("rounds", "regions_evaluated",
+                                                        "points_evaluated", "escalated",
+                                                        "deferred", "tie_fallbacks",
+                                                        "small_arg_fp64")}}
+    if rank == 0:
+        # peaks of this device
+        p32, p64 = ctx.measure_peaks()
+        # FP64 form on the same HOD vector as the last step, and parity of every term
+        last_hod = (args.warmup + args.steps - 1) % len(hods)
+        if not args.no_fp64:
+            ctx.set_hod(0, hods[last_hod])
+            r64 = ctx.eval(specs(0), G.FP64)
+            s64 = ctx.stats()
+            rel = np.abs(results[-1]["val"] - r64["val"]) / np.abs(r64["val"])
+            out["fp64"] = {"value": 1e3 / s64["device_ms"], "unit": "evals/s",
+                           "ms_per_step": s64["device_ms"],
+                           "mixed_over_fp64": (1e3 / (dev_total * 1e3 / args.steps)) /
+                                              (1e3 / s64["device_ms"])}
+            out["parity_vs_fp64"] = {
+                "max_rel": {"1h": float(rel[0::3].max()), "2h": float(rel[1::3].max()),
+                            "3h": float(rel[2::3].max())},
+                "median_rel": float(np.median(rel)), "terms_over_1e-4": int((rel > 1e-4).sum()),
+                "neval_identical": bool(np.array_equal(results[-1]["neval"], r64["neval"]))}
+        # roofline of the dominant rule kernel from a host-driven pass (per-kernel events)
+        ctx.set_options(use_graph=0)
+        ctx.set_hod(0, hods[last_hod])
+        ctx.eval(specs(0), G.MIXED)
+        sr = ctx.stats()
+        ctx.set_options(use_graph=1)
+        g = 1  # NNMap 2-halo
+        fpp = FLOPS_PER_POINT["nnmap_2h"]
+        ms_g = sr["group_ms"][g]
+        pts_g = sr["group_points"][g]
+        kern = {"kernel": "k_evalmx<NNMap,2h>", "ms": ms_g, "points": pts_g,
+                "points_per_s": pts_g / (ms_g * 1e-3) if ms_g else None,
+                "share_of_loop": ms_g / max(1e-9, sum(sr["group_ms"]) + sr["reeval_ms"] +
+                                            sr["select_ms"]),
+                "group_ms": sr["group_ms"], "reeval_ms": sr["reeval_ms"],
+                "select_ms": sr["select_ms"]}
+        if fpp:
+            ach = pts_g * fpp / (ms_g * 1e-3) / 1e12
+            out["roofline"] = {"bound": "fp32", "achieved": ach, "peak": p32, "unit": "TFLOP/s",
+                               "frac": ach / p32, "traffic": None,
+                               "peak_source": "measured FP32 FMA rate of this device "
+                                              "(g3l_measure_peaks); MEASURED_PEAKS.json holds "
+                                              "only HBM and bf16 figures", **kern}
+        else:
+            out["roofline"] = {"bound": "fp32", "achieved": None, "peak": p32, "unit": "TFLOP/s",
+                               "frac": None, "traffic": None, **kern}
+        out["peaks_measured"] = {"fp32_tflops": p32, "fp64_tflops": p64}
+        if not args.no_cpu:
+            out["cpu_baseline"] = cpu_sample(T, trip, hods[last_hod], args.max_eval, 4)
+        out["config"] = config(len(trip), args.max_eval)
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.barrier()
+
+
+if __name__ == "__main__":
+    main()

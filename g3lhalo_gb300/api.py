@@ -55,14 +55,20 @@ class Result(C.Structure):
 class Options(C.Structure):
     _fields_ = [("eval_blocks_per_sm", C.c_int), ("eval_warps_per_block", C.c_int),
                 ("use_graph", C.c_int), ("max_rounds", C.c_int), ("unlimited_pool", C.c_uint64),
-                ("small_arg", C.c_double)]
+                ("small_arg", C.c_double), ("unc_eps_rel", C.c_double),
+                ("unc_tau_abs", C.c_double), ("unc_tau_impact", C.c_double),
+                ("unc_tau_sel", C.c_double)]
 
 
 class Stats(C.Structure):
     _fields_ = [("kernel_launches", C.c_uint64), ("rounds", C.c_uint64),
                 ("regions_evaluated", C.c_uint64), ("points_evaluated", C.c_uint64),
                 ("tie_fallbacks", C.c_uint64), ("small_arg_fp64", C.c_uint64),
-                ("device_ms", C.c_double), ("eval_ms", C.c_double)]
+                ("device_ms", C.c_double), ("eval_ms", C.c_double),
+                ("escalated", C.c_uint64), ("deferred", C.c_uint64),
+                ("group_ms", C.c_double * 6), ("group_points", C.c_uint64 * 6),
+                ("reeval_ms", C.c_double), ("select_ms", C.c_double),
+                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64)]
 
 
 INTEGRAND_V = C.CFUNCTYPE(C.c_int, C.c_uint, C.c_size_t, _dp, C.c_void_p, C.c_uint, _dp)
@@ -97,6 +103,9 @@ def lib():
             L.g3l_set_options.argtypes = [C.c_void_p, C.POINTER(Options)]
             L.g3l_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
             L.g3l_last_error.restype = C.c_char_p
+            L.g3l_measure_peaks.argtypes = [C.c_void_p, _dp, _dp]
+            L.g3l_debug_region.argtypes = [C.c_void_p, C.POINTER(Integral), _dp,
+                                           C.POINTER(C.c_int), C.c_int, _dp, _dp]
             L.g3l_host_densities.argtypes = [C.POINTER(Tables), _dp, _dp, _dp]
             L.g3l_hcubature_v.argtypes = [C.c_uint, C.c_void_p, C.c_void_p, C.c_uint, _dp, _dp,
                                           C.c_size_t, C.c_double, C.c_double, C.c_int, _dp, _dp]
@@ -207,7 +216,30 @@ class Context:
     def stats(self):
         s = Stats()
         _check(lib().g3l_get_stats(self.h, C.byref(s)))
-        return {f: getattr(s, f) for f, _ in Stats._fields_}
+        out = {}
+        for f, _ in Stats._fields_:
+            v = getattr(s, f)
+            out[f] = list(v) if f in ("group_ms", "group_points") else v
+        return out
+
+    def measure_peaks(self):
+        """(fp32, fp64) FMA throughput of this device in TFLOP/s."""
+        a, b = C.c_double(), C.c_double()
+        _check(lib().g3l_measure_peaks(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def debug_region(self, spec, center, levels, precision=FP64):
+        """Integrand values at the rule points of one region, and (val, err, split)."""
+        items, n = self.make_items([spec])
+        dim = spec[1] + 4
+        npts = 1 + 4 * dim + 2 * dim * (dim - 1) + (1 << dim)
+        c = np.ascontiguousarray(center, dtype=np.float64)
+        lv = (C.c_int * dim)(*[int(x) for x in levels])
+        vals = np.zeros(npts)
+        out = np.zeros(3)
+        _check(lib().g3l_debug_region(self.h, items, _ptr(c), lv, precision, _ptr(vals),
+                                      _ptr(out)))
+        return vals, out
 
     @staticmethod
     def make_items(specs):

@@ -27,6 +27,7 @@ UNITS = {
     "eval_fp64.cu": ["-fmad=false"],
     "eval_mixed.cu": ["-fmad=true"],
     "host_api.cu": ["-fmad=false"],
+    "probe.cu": ["-fmad=true"],
 }
 HOST_UNITS = ["host_cubature.cpp", "host_model.cpp"]
 

@@ -67,6 +67,22 @@ __device__ int block_flag_scan(int flag, int *sh, int &total)
     return off + pre;
 }
 
+__device__ float block_max(float v, float *sh)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float r = 0.f;
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < SEL_WARPS; ++w) r = fmaxf(r, sh[w]);
+        sh[0] = r;
+    }
+    __syncthreads();
+    r = sh[0];
+    __syncthreads();
+    return r;
+}
+
 struct SelShared {
     unsigned int cnt[256];
     unsigned long long sum[256];
@@ -77,6 +93,7 @@ struct SelShared {
     double dred[SEL_WARPS];
     unsigned long long ured[SEL_WARPS];
     int ired[SEL_WARPS];
+    float fred[SEL_WARPS];
 };
 
 // MSD radix select over the live errors of one integral, descending.  by_sum:
@@ -182,7 +199,8 @@ __device__ void radix_select(const double *err, const unsigned long long *q, lon
 }
 
 __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D,
-                                                   IntState *__restrict__ S, Pool P, BatchHdr *H)
+                                                   IntState *__restrict__ S, Pool P, BatchHdr *H,
+                                                   double tau_sel)
 {
     __shared__ SelShared sh;
     __shared__ int s_flag[4];
@@ -309,6 +327,44 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
                 tneed = K - cnt_above;
             }
         }
+        // Mixed precision: if the boundary of this round's selection sits among regions
+        // whose FP32-derived errors are uncertain (overlapping bounds), re-evaluate those
+        // regions in FP64 first and select again next round.
+        if (H->mixed && K < (unsigned long long)R) {
+            const double b = __longlong_as_double((long long)bkey);
+            if (b > tau_sel * fabs(V)) {
+                float ub = 0.f;
+                for (int j = threadIdx.x; j < R; j += SEL_BS)
+                    if (ekey(P.err, base + j) == bkey) ub = fmaxf(ub, P.unc[base + j]);
+                ub = block_max(ub, sh.fred);
+                const double blo = b * (1.0 - ub), bhi = b * (1.0 + ub);
+                int amb = 0;
+                for (int j = threadIdx.x; j < R; j += SEL_BS) {
+                    const unsigned long long k = ekey(P.err, base + j);
+                    if (k == bkey) continue;
+                    const double e = P.err[base + j];
+                    const float u = P.unc[base + j];
+                    if ((u > 0.f || ub > 0.f) && e * (1.0 + u) >= blo && e * (1.0 - u) <= bhi) ++amb;
+                }
+                amb = block_sum(amb, sh.ired);
+                if (amb > 0) {
+                    for (int j = threadIdx.x; j < R; j += SEL_BS) {
+                        const double e = P.err[base + j];
+                        const float u = P.unc[base + j];
+                        if (u > 0.f && e * (1.0 + u) >= blo && e * (1.0 - u) <= bhi) {
+                            const int k = atomicAdd(&H->n_esc, 1);
+                            if (k < H->esc_cap) P.esc[k] = make_int2(i, j | (1 << 30));
+                        }
+                    }
+                    if (threadIdx.x == 0) {
+                        S[i].K = 0;
+                        atomicAdd(&H->deferred, 1ull);
+                    }
+                    __syncthreads();
+                    continue;
+                }
+            }
+        }
         // pool capacity
         if ((long long)R + (long long)K > (long long)d.cap) {
             if (threadIdx.x == 0) {
@@ -373,10 +429,12 @@ __global__ void __launch_bounds__(1024) k_scan(IntState *__restrict__ S, long lo
         long long tot = part[blockDim.x - 1];
         woff[n] = tot;
         H->total_work = tot;
-        H->any_active = tot > 0;
+        // keep looping while there is work or a deferred FP64 re-evaluation
+        const int more = tot > 0 || H->n_esc > 0;
+        H->any_active = more;
         H->regions += 2ull * (unsigned long long)tot;
-        if (tot > 0) H->rounds_done += 1;
-        if (use_cond) cudaGraphSetConditional(handle, tot > 0 ? 1u : 0u);
+        if (more) H->rounds_done += 1;
+        if (use_cond) cudaGraphSetConditional(handle, more ? 1u : 0u);
     }
 }
 
@@ -412,9 +470,21 @@ __global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, 
         H->rounds_done = 0;
         H->ties = 0;
         H->small_arg = 0;
+        H->n_esc = 0;
+        H->escalated = 0;
+        H->deferred = 0;
     }
 }
 
+// end of a mixed-precision round: the FP64 re-evaluation queue has been consumed
+__global__ void k_round_end(BatchHdr *H)
+{
+    const int n = H->n_esc;
+    H->escalated += (unsigned long long)(n < H->esc_cap ? n : H->esc_cap);
+    H->n_esc = 0;
+}
+
+void *round_end_kernel() { return (void *)k_round_end; }
 void *select_kernel() { return (void *)k_select; }
 void *scan_kernel() { return (void *)k_scan; }
 void *init_kernel() { return (void *)k_init; }

@@ -238,6 +238,97 @@ __device__ void combine64(const double *v, double vol, double &val, double &err,
     split = dimDiffMax;
 }
 
+// One work item on one warp: `cut` = bisect the region at pslot along its split
+// dimension into pslot (lower half) and qslot (upper half) and evaluate both;
+// otherwise evaluate the region at pslot in place (roots, FP64 re-evaluation).
+template <int KIND, int TERM>
+__device__ void warp_item64(const DevTables &T, const IntDesc &d, const Pool &P, long long pslot,
+                            long long qslot, bool cut, Slot64 *slots, double *vals,
+                            const uint32_t *sdesc, unsigned long long *ties, double *dbg)
+{
+    constexpr int DIM = TERM + 4;
+    constexpr int NP = rule_points(DIM);
+    const int lane = threadIdx.x & 31;
+    const long long stride = P.stride;
+    const int sdim = cut ? P.split[pslot] : 0;
+    const int nchild = cut ? 2 : 1;
+    double c_l = 0;
+    int lev = 0;
+    if (lane < DIM) {
+        c_l = P.center[lane * stride + pslot];
+        lev = P.level[lane * stride + pslot];
+    }
+    double cL = 0, cR = 0;
+    const int levs = __shfl_sync(0xffffffffu, lev, sdim) + (cut ? 1 : 0);
+    const double cs = __shfl_sync(0xffffffffu, c_l, sdim);
+    const double hws = ldexp(d.hw0[sdim], -levs);
+    if (cut) {
+        cL = cs - hws;
+        cR = cs + hws;
+    }
+    const int levsum = __reduce_add_sync(0xffffffffu, lane < DIM ? lev : 0) + (cut ? 1 : 0);
+    // coordinate variant slots: dims 0..DIM-1 of child 0, then dim sdim of child 1
+    const int nslot = (DIM + nchild - 1) * NVAR;
+    for (int t = lane; t < nslot; t += 32) {
+        int dd = t / NVAR, v = t - dd * NVAR;
+        int dim = dd < DIM ? dd : sdim;
+        double c = P.center[dim * stride + pslot];
+        int L = P.level[dim * stride + pslot];
+        if (cut && dim == sdim) {
+            L += 1;
+            c = (dd < DIM) ? cL : cR;
+        }
+        double hw = ldexp(d.hw0[dim], -L);
+        double x = c;
+        if (v > 0) {
+            double lam = (v <= 2) ? G3L_LAMBDA2 : (v <= 4 ? G3L_LAMBDA4 : G3L_LAMBDA5);
+            double r = hw * lam;
+            x = (v & 1) ? c - r : c + r;
+        }
+        Model64<KIND, TERM>::fill(T, d, dim, x, slots[t], ties);
+    }
+    __syncwarp();
+    for (int p = lane; p < nchild * NP; p += 32) {
+        int ch = p >= NP ? 1 : 0;
+        int pp = p - ch * NP;
+        uint32_t vv = sdesc[pp];
+        const Slot64 *sp[DIM];
+#pragma unroll
+        for (int dd = 0; dd < DIM; ++dd) {
+            int v = (vv >> (3 * dd)) & 7;
+            sp[dd] = (ch && dd == sdim) ? &slots[DIM * NVAR + v] : &slots[dd * NVAR + v];
+        }
+        vals[p] = Model64<KIND, TERM>::point(T, d, sp);
+        if (dbg) dbg[p] = vals[p];
+    }
+    __syncwarp();
+    // rule sums: lane 0 -> child 0, lane 1 -> child 1
+    if (lane < nchild) {
+        double vol = ldexp(d.rootvol, -levsum);
+        double val, err;
+        int split;
+        combine64<DIM>(vals + lane * NP, vol, val, err, split);
+        long long slot = lane == 0 ? pslot : qslot;
+        P.val[slot] = val;
+        P.err[slot] = err;
+        P.split[slot] = (unsigned char)split;
+        if (P.unc) P.unc[slot] = 0.f;
+    }
+    if (cut && lane < DIM) {
+        double cnew = c_l;
+        int lnew = lev;
+        if (lane == sdim) {
+            lnew = levs;
+            cnew = cL;
+        }
+        P.center[lane * stride + pslot] = cnew;
+        P.level[lane * stride + pslot] = (unsigned char)lnew;
+        P.center[lane * stride + qslot] = lane == sdim ? cR : c_l;
+        P.level[lane * stride + qslot] = (unsigned char)lnew;
+    }
+    __syncwarp();
+}
+
 template <int KIND, int TERM>
 __global__ void __launch_bounds__(128) k_eval64(DevTables T, const IntDesc *__restrict__ D,
                                                 IntState *__restrict__ S, Pool P, BatchHdr *H,
@@ -253,13 +344,10 @@ __global__ void __launch_bounds__(128) k_eval64(DevTables T, const IntDesc *__re
     const int g = KIND * 3 + TERM - 1;
     for (int p = threadIdx.x; p < NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
     __syncthreads();
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int wib = threadIdx.x >> 5;
     const int gb = H->gbeg[g], ge = H->gbeg[g + 1];
     if (gb >= ge) return;
     const long long wbeg = woff[gb], wend = woff[ge];
-    unsigned long long *ties = &H->ties;
-    Slot64 *slots = sslot[wib];
-    double *vals = svals[wib];
     const long long nwarps = (long long)gridDim.x * WPB;
     for (long long w = wbeg + (long long)blockIdx.x * WPB + wib; w < wend; w += nwarps) {
         int lo = gb, hi = ge - 1;  // last integral i with woff[i] <= w
@@ -271,104 +359,121 @@ __global__ void __launch_bounds__(128) k_eval64(DevTables T, const IntDesc *__re
         const int i = lo;
         const long long j = w - woff[i];
         const IntDesc &d = D[i];
-        const long long stride = P.stride;
         const int cj = P.cand[d.base + j];
-        const bool root = cj < 0;  // a fresh integral's root region
-        long long pslot = d.base + (root ? 0 : cj), qslot = -1;
-        int sdim = 0;
-        if (!root) {
-            qslot = d.base + (S[i].nR - S[i].K) + j;
-            sdim = P.split[pslot];
+        const bool cut = cj >= 0;  // cj < 0: a fresh integral's root region
+        const long long pslot = d.base + (cut ? cj : 0);
+        const long long qslot = cut ? d.base + (S[i].nR - S[i].K) + j : -1;
+        warp_item64<KIND, TERM>(T, d, P, pslot, qslot, cut, sslot[wib], svals[wib], sdesc,
+                                &H->ties, H->dbg);
+    }
+}
+
+// FP64 split decision of the region at slot: only the centre and the 4 dim axis
+// points enter the fourth differences (src/hcubature.cpp:527-575), so only those
+// are evaluated.
+template <int KIND, int TERM>
+__device__ void warp_split64(const DevTables &T, const IntDesc &d, const Pool &P, long long slot,
+                             Slot64 *slots, double *vals, const uint32_t *sdesc,
+                             unsigned long long *ties)
+{
+    constexpr int DIM = TERM + 4;
+    constexpr int NAX = 1 + 4 * DIM;
+    const int lane = threadIdx.x & 31;
+    const long long stride = P.stride;
+    for (int t = lane; t < DIM * 5; t += 32) {  // variants 0..4 (c, -+r2, -+r4) only
+        const int dim = t / 5, v = t - dim * 5;
+        const double c = P.center[dim * stride + slot];
+        const double hw = ldexp(d.hw0[dim], -(int)P.level[dim * stride + slot]);
+        double x = c;
+        if (v > 0) {
+            double r = hw * ((v <= 2) ? G3L_LAMBDA2 : G3L_LAMBDA4);
+            x = (v & 1) ? c - r : c + r;
         }
-        const int nchild = root ? 1 : 2;
-        // parent geometry
-        double c_l = 0;
-        int lev = 0;
-        if (lane < DIM) {
-            c_l = P.center[lane * stride + pslot];
-            lev = P.level[lane * stride + pslot];
-        }
-        double cL = 0, cR = 0;
-        int levs = __shfl_sync(0xffffffffu, lev, sdim) + (root ? 0 : 1);
-        double cs = __shfl_sync(0xffffffffu, c_l, sdim);
-        double hws = ldexp(d.hw0[sdim], -levs);
-        if (!root) {
-            cL = cs - hws;
-            cR = cs + hws;
-        }
-        int levsum = __reduce_add_sync(0xffffffffu, lane < DIM ? lev : 0) + (root ? 0 : 1);
-        // coordinate variant slots: dims 0..DIM-1 of child 0, then dim sdim of child 1
-        const int nslot = (DIM + nchild - 1) * NVAR;
-        for (int t = lane; t < nslot; t += 32) {
-            int dd = t / NVAR, v = t - dd * NVAR;
-            int dim = dd < DIM ? dd : sdim;
-            double c = P.center[dim * stride + pslot];
-            int L = P.level[dim * stride + pslot];
-            if (!root && dim == sdim) {
-                L += 1;
-                c = (dd < DIM) ? cL : cR;
-            }
-            double hw = ldexp(d.hw0[dim], -L);
-            double x = c;
-            if (v > 0) {
-                double lam = (v <= 2) ? G3L_LAMBDA2 : (v <= 4 ? G3L_LAMBDA4 : G3L_LAMBDA5);
-                double r = hw * lam;
-                x = (v & 1) ? c - r : c + r;
-            }
-            Model64<KIND, TERM>::fill(T, d, dim, x, slots[t], ties);
-        }
-        __syncwarp();
-        // points
-        for (int p = lane; p < nchild * NP; p += 32) {
-            int ch = p >= NP ? 1 : 0;
-            int pp = p - ch * NP;
-            uint32_t vv = sdesc[pp];
-            const Slot64 *sp[DIM];
+        Model64<KIND, TERM>::fill(T, d, dim, x, slots[dim * NVAR + v], ties);
+    }
+    __syncwarp();
+    for (int p = lane; p < NAX; p += 32) {
+        const uint32_t vv = sdesc[p];
+        const Slot64 *sp[DIM];
 #pragma unroll
-            for (int dd = 0; dd < DIM; ++dd) {
-                int v = (vv >> (3 * dd)) & 7;
-                sp[dd] = (ch && dd == sdim) ? &slots[DIM * NVAR + v] : &slots[dd * NVAR + v];
+        for (int dd = 0; dd < DIM; ++dd) sp[dd] = &slots[dd * NVAR + ((vv >> (3 * dd)) & 7)];
+        vals[p] = Model64<KIND, TERM>::point(T, d, sp);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        const double ratio = (G3L_LAMBDA2 * G3L_LAMBDA2) / (G3L_LAMBDA4 * G3L_LAMBDA4);
+        const double val0 = vals[0];
+        double maxdiff = 0;
+        int dimDiffMax = 0;
+        for (int k = 0; k < DIM; ++k) {
+            double v0 = vals[1 + 4 * k], v1 = vals[2 + 4 * k];
+            double v2 = vals[3 + 4 * k], v3 = vals[4 + 4 * k];
+            double diff = 0;
+            diff += fabs(v0 + v1 - 2 * val0 - ratio * (v2 + v3 - 2 * val0));
+            if (diff > maxdiff) {
+                maxdiff = diff;
+                dimDiffMax = k;
             }
-            vals[p] = Model64<KIND, TERM>::point(T, d, sp);
         }
-        __syncwarp();
-        // rule sums: lane 0 -> child 0, lane 1 -> child 1
-        if (lane < nchild) {
-            double vol = ldexp(d.rootvol, -levsum);
-            double val, err;
-            int split;
-            combine64<DIM>(vals + lane * NP, vol, val, err, split);
-            long long slot = lane == 0 ? pslot : qslot;
-            P.val[slot] = val;
-            P.err[slot] = err;
-            P.split[slot] = (unsigned char)split;
-        }
-        // child geometry
-        if (!root && lane < DIM) {
-            double cnew = c_l;
-            int lnew = lev;
-            if (lane == sdim) {
-                lnew = levs;
-                cnew = cL;
-            }
-            P.center[lane * stride + pslot] = cnew;
-            P.level[lane * stride + pslot] = (unsigned char)lnew;
-            P.center[lane * stride + qslot] = lane == sdim ? cR : c_l;
-            P.level[lane * stride + qslot] = (unsigned char)lnew;
-        }
-        __syncwarp();
+        P.split[slot] = (unsigned char)dimDiffMax;
+    }
+    __syncwarp();
+}
+
+// FP64 re-evaluation of the regions the mixed-precision pass escalated; each entry is
+// (integral, local slot | kind << 30): kind 0 = split decision only, 1 = whole rule
+// (value, error and split; for selection boundaries).
+template <int KIND, int TERM>
+__global__ void __launch_bounds__(128) k_reeval64(DevTables T, const IntDesc *__restrict__ D,
+                                                  IntState *__restrict__ S, Pool P, BatchHdr *H,
+                                                  const long long *__restrict__ woff)
+{
+    constexpr int DIM = TERM + 4;
+    constexpr int NP = rule_points(DIM);
+    constexpr int NSLOT = (DIM + 1) * NVAR;
+    constexpr int WPB = 4;
+    __shared__ uint32_t sdesc[NP];
+    __shared__ Slot64 sslot[WPB][NSLOT];
+    __shared__ double svals[WPB][2 * NP];
+    const int n = H->n_esc;
+    if (n == 0) return;
+    for (int p = threadIdx.x; p < NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
+    __syncthreads();
+    const int g = KIND * 3 + TERM - 1;
+    const int wib = threadIdx.x >> 5;
+    const int nmax = n < H->esc_cap ? n : H->esc_cap;
+    for (int e = blockIdx.x * WPB + wib; e < nmax; e += gridDim.x * WPB) {
+        const int2 ent = P.esc[e];
+        const IntDesc &d = D[ent.x];
+        if (d.kind * 3 + d.term - 1 != g) continue;
+        const long long slot = d.base + (ent.y & 0x3FFFFFFF);
+        if (ent.y >> 30)
+            warp_item64<KIND, TERM>(T, d, P, slot, -1, false, sslot[wib], svals[wib], sdesc,
+                                    &H->ties, nullptr);
+        else
+            warp_split64<KIND, TERM>(T, d, P, slot, sslot[wib], svals[wib], sdesc, &H->ties);
     }
 }
 
 #define G3L_INST64(K, Tm)                                                                        \
     template __global__ void k_eval64<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,      \
-                                             BatchHdr *, const long long *);
+                                             BatchHdr *, const long long *);                     \
+    template __global__ void k_reeval64<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,    \
+                                               BatchHdr *, const long long *);
 G3L_INST64(0, 1)
 G3L_INST64(0, 2)
 G3L_INST64(0, 3)
 G3L_INST64(1, 1)
 G3L_INST64(1, 2)
 G3L_INST64(1, 3)
+
+void *reeval64_kernel(int kind, int term)
+{
+    static void *tab[2][3] = {
+        {(void *)k_reeval64<0, 1>, (void *)k_reeval64<0, 2>, (void *)k_reeval64<0, 3>},
+        {(void *)k_reeval64<1, 1>, (void *)k_reeval64<1, 2>, (void *)k_reeval64<1, 3>}};
+    return tab[kind][term - 1];
+}
 
 void *eval64_kernel(int kind, int term)
 {

@@ -618,6 +618,206 @@ __device__ __forceinline__ df hw_sum(df a)
     return a;
 }
 
+// The bound on the FP32 error of one point value has a relative part (the FP32
+// chain) and an absolute part (values so small that intermediate products may
+// have lost range): T.unc_eps |v| + T.unc_abs.  A decision is escalated to FP64
+// only if its region could move the integral by more than T.tau_impact of it.
+
+template <int KIND, int TERM>
+__device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, double Vcur,
+                           const Pool &P, BatchHdr *H, long long pslot, long long qslot, bool cut,
+                           SlotF *slots, float *vals, Child &C, const uint32_t *sdesc,
+                           unsigned &ties, int &small)
+{
+    constexpr int DIM = TERM + 4;
+    constexpr int NP = rule_points(DIM);
+    constexpr int NRR = 2 * DIM * (DIM - 1);
+    using W = RuleW<DIM>;
+    const int lane = threadIdx.x & 31;
+    const long long stride = P.stride;
+    const int sdim = cut ? P.split[pslot] : 0;
+    const int nchild = cut ? 2 : 1;
+    // parent geometry -> child centres (FP64: one add per child)
+    double c_l = 0;
+    int lev = 0;
+    if (lane < DIM) {
+        c_l = P.center[lane * stride + pslot];
+        lev = P.level[lane * stride + pslot];
+    }
+    const int levs = __shfl_sync(0xffffffffu, lev, sdim) + (cut ? 1 : 0);
+    const double cs = __shfl_sync(0xffffffffu, c_l, sdim);
+    double cchild = cs;
+    if (cut && lane < 2) {
+        const double hws = ldexp(d.hw0[sdim], -levs);
+        cchild = lane == 0 ? __dsub_rn(cs, hws) : __dadd_rn(cs, hws);
+    }
+    const double cL = __shfl_sync(0xffffffffu, cchild, 0);
+    const double cR = __shfl_sync(0xffffffffu, cchild, 1);
+    const int levsum = __reduce_add_sync(0xffffffffu, lane < DIM ? lev : 0) + (cut ? 1 : 0);
+    if (lane < DIM) {
+        C.c64[lane] = (cut && lane == sdim) ? cL : c_l;
+        C.lev[lane] = (cut && lane == sdim) ? levs : lev;
+    }
+    if (lane == DIM) {
+        C.c64[DIM] = cR;
+        C.lev[DIM] = levs;
+    }
+    __syncwarp();
+    // coordinate-variant slots
+    const int nslot = (DIM + nchild - 1) * NVAR;
+    for (int t = lane; t < nslot; t += 32) {
+        const int sd = t / NVAR, v = t - sd * NVAR;
+        const int dim = sd < DIM ? sd : sdim;
+        df x = df_from_double(C.c64[sd]);
+        if (v > 0) {
+            const int li = (v <= 2) ? 0 : (v <= 4 ? 1 : 2);
+            df r = df_ldexp({d.hwl[dim][li].x, d.hwl[dim][li].y}, -C.lev[sd]);
+            x = (v & 1) ? df_add(x, df_neg(r)) : df_add(x, r);
+        }
+        ModelF<KIND, TERM>::fill(T, d, C, sd, dim, v, x, slots[t], ties);
+    }
+    __syncwarp();
+    // points
+    for (int p = lane; p < nchild * NP; p += 32) {
+        const int ch = p >= NP ? 1 : 0;
+        const int pp = p - ch * NP;
+        const uint32_t vv = sdesc[pp];
+        const SlotF *sp[DIM];
+#pragma unroll
+        for (int dd = 0; dd < DIM; ++dd) {
+            const int v = (vv >> (3 * dd)) & 7;
+            sp[dd] = (ch && dd == sdim) ? &slots[DIM * NVAR + v] : &slots[dd * NVAR + v];
+        }
+        vals[p] = ModelF<KIND, TERM>::point(T, d, sp, C, ch, sdim, vv, ties, small);
+        if (H->dbg) H->dbg[p] = (double)vals[p];
+    }
+    __syncwarp();
+    // rule sums in double-float, uncertainty sums in FP32: half-warp hh serves child hh
+    const int hh = lane >> 4, hl = lane & 15;
+    const bool active = hh < nchild;
+    const float *v = vals + hh * NP;
+    df s2 = {0.f, 0.f}, s3 = {0.f, 0.f}, s45 = {0.f, 0.f}, s4 = {0.f, 0.f};
+    float u2 = 0.f, u3 = 0.f, u4 = 0.f, u5 = 0.f;
+    df diff = {-1.f, 0.f};
+    float udiff = 0.f;
+    const float val0 = active ? v[0] : 0.f;
+    const float EPS_REL = T.unc_eps, TAU_ABS = T.unc_abs;
+    const float u0 = fmaf(EPS_REL, fabsf(val0), TAU_ABS);
+    constexpr float RATIO = (float)((G3L_LAMBDA2 * G3L_LAMBDA2) / (G3L_LAMBDA4 * G3L_LAMBDA4));
+    if (active && hl < DIM) {
+        const float a0 = v[1 + 4 * hl], a1 = v[2 + 4 * hl], b0 = v[3 + 4 * hl], b1 = v[4 + 4 * hl];
+        const df a = df_two_sum(a0, a1);
+        const df b = df_two_sum(b0, b1);
+        s2 = a;
+        s3 = b;
+        const float ua = fmaf(EPS_REL, fabsf(a0), TAU_ABS) + fmaf(EPS_REL, fabsf(a1), TAU_ABS);
+        const float ub = fmaf(EPS_REL, fabsf(b0), TAU_ABS) + fmaf(EPS_REL, fabsf(b1), TAU_ABS);
+        u2 = ua;
+        u3 = ub;
+        const df tv = {-2.f * val0, 0.f};
+        const df da = df_add(a, tv), db = df_add(b, tv);
+        df dd = df_add(da, df_neg(df_mul(db, {df_hi_of((G3L_LAMBDA2 * G3L_LAMBDA2) /
+                                                       (G3L_LAMBDA4 * G3L_LAMBDA4)),
+                                              df_lo_of((G3L_LAMBDA2 * G3L_LAMBDA2) /
+                                                       (G3L_LAMBDA4 * G3L_LAMBDA4))})));
+        diff = dd.hi < 0.f ? df_neg(dd) : dd;
+        udiff = ua + RATIO * ub + (2.f - 2.f * RATIO) * u0;
+    }
+    if (active) {
+        for (int k = hl; k < NRR; k += 16) {
+            const float x = v[1 + 4 * DIM + k];
+            s4 = df_add_f(s4, x);
+            u4 += fmaf(EPS_REL, fabsf(x), TAU_ABS);
+        }
+        for (int k = hl; k < (1 << DIM); k += 16) {
+            const float x = v[1 + 4 * DIM + NRR + k];
+            s45 = df_add_f(s45, x);
+            u5 += fmaf(EPS_REL, fabsf(x), TAU_ABS);
+        }
+    }
+    s2 = hw_sum(s2);
+    s3 = hw_sum(s3);
+    s4 = hw_sum(s4);
+    s45 = hw_sum(s45);
+    for (int m = 8; m > 0; m >>= 1) {
+        u2 += __shfl_xor_sync(0xffffffffu, u2, m);
+        u3 += __shfl_xor_sync(0xffffffffu, u3, m);
+        u4 += __shfl_xor_sync(0xffffffffu, u4, m);
+        u5 += __shfl_xor_sync(0xffffffffu, u5, m);
+    }
+    // split dimension: first maximum of the fourth differences, and the runner-up
+    int sidx = hl;
+    df best = diff;
+    float ubest = udiff;
+    for (int m = 8; m > 0; m >>= 1) {
+        df od = shfl_xor_df(best, m);
+        int oi = __shfl_xor_sync(0xffffffffu, sidx, m);
+        float ou = __shfl_xor_sync(0xffffffffu, ubest, m);
+        if (df_gt(od, best) || (od.hi == best.hi && od.lo == best.lo && oi < sidx)) {
+            best = od;
+            sidx = oi;
+            ubest = ou;
+        }
+    }
+    df second = (hl == sidx) ? df{-1.f, 0.f} : diff;
+    float usecond = (hl == sidx) ? 0.f : udiff;
+    for (int m = 8; m > 0; m >>= 1) {
+        df od = shfl_xor_df(second, m);
+        float ou = __shfl_xor_sync(0xffffffffu, usecond, m);
+        if (df_gt(od, second)) {
+            second = od;
+            usecond = ou;
+        }
+    }
+    // decisive when the gap between the two largest differences exceeds both bounds
+    const bool split_sure = (best.hi - fmaxf(second.hi, 0.f)) > (ubest + usecond) &&
+                            best.hi > ubest;
+    // 7th- and 5th-degree brackets (double-float), then FP64 on four lanes
+    df b7 = df_mul_f({df_hi_of(W::w1), df_lo_of(W::w1)}, val0);
+    b7 = df_add(b7, df_mul(s2, {df_hi_of(W::w2), df_lo_of(W::w2)}));
+    b7 = df_add(b7, df_mul(s3, {df_hi_of(W::w3), df_lo_of(W::w3)}));
+    b7 = df_add(b7, df_mul(s4, {df_hi_of(W::w4), df_lo_of(W::w4)}));
+    df b5 = df_mul_f({df_hi_of(W::wE1), df_lo_of(W::wE1)}, val0);
+    b5 = df_add(b5, df_mul(s2, {df_hi_of(W::wE2), df_lo_of(W::wE2)}));
+    b5 = df_add(b5, df_mul(s3, {df_hi_of(W::wE3), df_lo_of(W::wE3)}));
+    b5 = df_add(b5, df_mul(s4, {df_hi_of(W::wE4), df_lo_of(W::wE4)}));
+    df e = df_add(b5, df_neg(df_add(b7, df_mul(s45, {df_hi_of(W::w5), df_lo_of(W::w5)}))));
+    b7 = df_add(b7, df_mul(s45, {df_hi_of(W::w5), df_lo_of(W::w5)}));
+    if (e.hi < 0.f) e = df_neg(e);
+    // bound on the error of e from the point-value bounds (weights of res7 - res5)
+    const float ue = fabsf((float)(W::w1 - W::wE1)) * u0 + fabsf((float)(W::w2 - W::wE2)) * u2 +
+                     fabsf((float)(W::w3 - W::wE3)) * u3 + fabsf((float)(W::w4 - W::wE4)) * u4 +
+                     fabsf((float)W::w5) * u5;
+    const float urel = e.hi > 0.f ? fminf(ue / e.hi, 1e30f) : (ue > 0.f ? 1e30f : 0.f);
+    // lane 16h+0 -> value, 16h+1 -> error of child h
+    const df q = hl == 1 ? e : b7;
+    if (active && hl < 2) {
+        const double vol = ldexp(d.rootvol_mx, -levsum);
+        const double out = ((double)q.hi + (double)q.lo) * vol;
+        const long long slot = hh == 0 ? pslot : qslot;
+        if (hl == 0) {
+            P.val[slot] = out;
+            P.split[slot] = (unsigned char)sidx;
+        } else {
+            P.err[slot] = out;
+            P.unc[slot] = urel;
+            // an uncertain split of a region that matters: re-evaluate in FP64
+            if (!split_sure && out > T.tau_impact * fabs(Vcur)) {
+                const int k = atomicAdd(&H->n_esc, 1);
+                if (k < H->esc_cap) P.esc[k] = make_int2(iint, (int)(slot - d.base));
+            }
+        }
+    }
+    // child geometry
+    if (cut && lane < DIM) {
+        P.center[lane * stride + pslot] = C.c64[lane];
+        P.level[lane * stride + pslot] = (unsigned char)C.lev[lane];
+        P.center[lane * stride + qslot] = lane == sdim ? cR : c_l;
+        P.level[lane * stride + qslot] = (unsigned char)C.lev[lane];
+    }
+    __syncwarp();
+}
+
 template <int KIND, int TERM>
 __global__ void __launch_bounds__(128) k_evalmx(DevTables T, const IntDesc *__restrict__ D,
                                                 IntState *__restrict__ S, Pool P, BatchHdr *H,
@@ -627,8 +827,6 @@ __global__ void __launch_bounds__(128) k_evalmx(DevTables T, const IntDesc *__re
     constexpr int NP = rule_points(DIM);
     constexpr int NSLOT = (DIM + 1) * NVAR;
     constexpr int WPB = 4;
-    constexpr int NRR = 2 * DIM * (DIM - 1);
-    using W = RuleW<DIM>;
     __shared__ uint32_t sdesc[NP];
     __shared__ SlotF sslot[WPB][NSLOT];
     __shared__ float svals[WPB][2 * NP];
@@ -640,9 +838,6 @@ __global__ void __launch_bounds__(128) k_evalmx(DevTables T, const IntDesc *__re
     const int gb = H->gbeg[g], ge = H->gbeg[g + 1];
     if (gb >= ge) return;
     const long long wbeg = woff[gb], wend = woff[ge];
-    SlotF *slots = sslot[wib];
-    float *vals = svals[wib];
-    Child &C = schild[wib];
     unsigned ties = 0;
     int small = 0;
     const long long nwarps = (long long)gridDim.x * WPB;
@@ -656,142 +851,12 @@ __global__ void __launch_bounds__(128) k_evalmx(DevTables T, const IntDesc *__re
         const int i = lo;
         const long long j = w - woff[i];
         const IntDesc &d = D[i];
-        const long long stride = P.stride;
         const int cj = P.cand[d.base + j];
-        const bool root = cj < 0;
-        const long long pslot = d.base + (root ? 0 : cj);
-        long long qslot = -1;
-        int sdim = 0;
-        if (!root) {
-            qslot = d.base + (S[i].nR - S[i].K) + j;
-            sdim = P.split[pslot];
-        }
-        const int nchild = root ? 1 : 2;
-        // parent geometry -> child centres (FP64: one add per child)
-        double c_l = 0;
-        int lev = 0;
-        if (lane < DIM) {
-            c_l = P.center[lane * stride + pslot];
-            lev = P.level[lane * stride + pslot];
-        }
-        const int levs = __shfl_sync(0xffffffffu, lev, sdim) + (root ? 0 : 1);
-        const double cs = __shfl_sync(0xffffffffu, c_l, sdim);
-        double cchild = cs;
-        if (!root && lane < 2) {
-            const double hws = ldexp(d.hw0[sdim], -levs);
-            cchild = lane == 0 ? __dsub_rn(cs, hws) : __dadd_rn(cs, hws);
-        }
-        const double cL = __shfl_sync(0xffffffffu, cchild, 0);
-        const double cR = __shfl_sync(0xffffffffu, cchild, 1);
-        const int levsum = __reduce_add_sync(0xffffffffu, lane < DIM ? lev : 0) + (root ? 0 : 1);
-        if (lane < DIM) {
-            C.c64[lane] = (!root && lane == sdim) ? cL : c_l;
-            C.lev[lane] = (!root && lane == sdim) ? levs : lev;
-        }
-        if (lane == DIM) {
-            C.c64[DIM] = cR;
-            C.lev[DIM] = levs;
-        }
-        __syncwarp();
-        // coordinate-variant slots
-        const int nslot = (DIM + nchild - 1) * NVAR;
-        for (int t = lane; t < nslot; t += 32) {
-            const int sd = t / NVAR, v = t - sd * NVAR;
-            const int dim = sd < DIM ? sd : sdim;
-            df x = df_from_double(C.c64[sd]);
-            if (v > 0) {
-                const int li = (v <= 2) ? 0 : (v <= 4 ? 1 : 2);
-                df r = df_ldexp({d.hwl[dim][li].x, d.hwl[dim][li].y}, -C.lev[sd]);
-                x = (v & 1) ? df_add(x, df_neg(r)) : df_add(x, r);
-            }
-            ModelF<KIND, TERM>::fill(T, d, C, sd, dim, v, x, slots[t], ties);
-        }
-        __syncwarp();
-        // points
-        for (int p = lane; p < nchild * NP; p += 32) {
-            const int ch = p >= NP ? 1 : 0;
-            const int pp = p - ch * NP;
-            const uint32_t vv = sdesc[pp];
-            const SlotF *sp[DIM];
-#pragma unroll
-            for (int dd = 0; dd < DIM; ++dd) {
-                const int v = (vv >> (3 * dd)) & 7;
-                sp[dd] = (ch && dd == sdim) ? &slots[DIM * NVAR + v] : &slots[dd * NVAR + v];
-            }
-            vals[p] = ModelF<KIND, TERM>::point(T, d, sp, C, ch, sdim, vv, ties, small);
-        }
-        __syncwarp();
-        // rule sums in double-float: half-warp hh serves child hh
-        const int hh = lane >> 4, hl = lane & 15;
-        const bool active = hh < nchild;
-        const float *v = vals + hh * NP;
-        df s2 = {0.f, 0.f}, s3 = {0.f, 0.f}, s45 = {0.f, 0.f}, s4 = {0.f, 0.f};
-        df diff = {-1.f, 0.f};
-        const float val0 = active ? v[0] : 0.f;
-        if (active && hl < DIM) {
-            const df a = df_two_sum(v[1 + 4 * hl], v[2 + 4 * hl]);
-            const df b = df_two_sum(v[3 + 4 * hl], v[4 + 4 * hl]);
-            s2 = a;
-            s3 = b;
-            const df tv = {-2.f * val0, 0.f};
-            const df da = df_add(a, tv), db = df_add(b, tv);
-            df dd = df_add(da, df_neg(df_mul(db, {df_hi_of((G3L_LAMBDA2 * G3L_LAMBDA2) /
-                                                           (G3L_LAMBDA4 * G3L_LAMBDA4)),
-                                                  df_lo_of((G3L_LAMBDA2 * G3L_LAMBDA2) /
-                                                           (G3L_LAMBDA4 * G3L_LAMBDA4))})));
-            diff = dd.hi < 0.f ? df_neg(dd) : dd;
-        }
-        if (active) {
-            for (int k = hl; k < NRR; k += 16) s4 = df_add_f(s4, v[1 + 4 * DIM + k]);
-            for (int k = hl; k < (1 << DIM); k += 16) s45 = df_add_f(s45, v[1 + 4 * DIM + NRR + k]);
-        }
-        s2 = hw_sum(s2);
-        s3 = hw_sum(s3);
-        s4 = hw_sum(s4);
-        s45 = hw_sum(s45);
-        // split dimension: first maximum of the fourth differences
-        int sidx = hl;
-        for (int m = 8; m > 0; m >>= 1) {
-            df od = shfl_xor_df(diff, m);
-            int oi = __shfl_xor_sync(0xffffffffu, sidx, m);
-            if (df_gt(od, diff) || (od.hi == diff.hi && od.lo == diff.lo && oi < sidx)) {
-                diff = od;
-                sidx = oi;
-            }
-        }
-        // 7th- and 5th-degree brackets (double-float), then FP64 on four lanes
-        df b7 = df_mul_f({df_hi_of(W::w1), df_lo_of(W::w1)}, val0);
-        b7 = df_add(b7, df_mul(s2, {df_hi_of(W::w2), df_lo_of(W::w2)}));
-        b7 = df_add(b7, df_mul(s3, {df_hi_of(W::w3), df_lo_of(W::w3)}));
-        b7 = df_add(b7, df_mul(s4, {df_hi_of(W::w4), df_lo_of(W::w4)}));
-        df b5 = df_mul_f({df_hi_of(W::wE1), df_lo_of(W::wE1)}, val0);
-        b5 = df_add(b5, df_mul(s2, {df_hi_of(W::wE2), df_lo_of(W::wE2)}));
-        b5 = df_add(b5, df_mul(s3, {df_hi_of(W::wE3), df_lo_of(W::wE3)}));
-        b5 = df_add(b5, df_mul(s4, {df_hi_of(W::wE4), df_lo_of(W::wE4)}));
-        df e = df_add(b5, df_neg(df_add(b7, df_mul(s45, {df_hi_of(W::w5), df_lo_of(W::w5)}))));
-        b7 = df_add(b7, df_mul(s45, {df_hi_of(W::w5), df_lo_of(W::w5)}));
-        if (e.hi < 0.f) e = df_neg(e);
-        // lane 16h+0 -> value, 16h+1 -> error of child h
-        const df q = hl == 1 ? e : b7;
-        if (active && hl < 2) {
-            const double vol = ldexp(d.rootvol, -levsum);
-            const double out = ((double)q.hi + (double)q.lo) * vol;
-            const long long slot = hh == 0 ? pslot : qslot;
-            if (hl == 0) {
-                P.val[slot] = out;
-                P.split[slot] = (unsigned char)sidx;
-            } else {
-                P.err[slot] = out;
-            }
-        }
-        // child geometry
-        if (!root && lane < DIM) {
-            P.center[lane * stride + pslot] = C.c64[lane];
-            P.level[lane * stride + pslot] = (unsigned char)C.lev[lane];
-            P.center[lane * stride + qslot] = lane == sdim ? cR : c_l;
-            P.level[lane * stride + qslot] = (unsigned char)C.lev[lane];
-        }
-        __syncwarp();
+        const bool cut = cj >= 0;
+        const long long pslot = d.base + (cut ? cj : 0);
+        const long long qslot = cut ? d.base + (S[i].nR - S[i].K) + j : -1;
+        warp_itemF<KIND, TERM>(T, d, i, S[i].val, P, H, pslot, qslot, cut, sslot[wib],
+                               svals[wib], schild[wib], sdesc, ties, small);
     }
     // warp-aggregated diagnostics
     unsigned tw = __reduce_add_sync(0xffffffffu, ties);

@@ -62,6 +62,8 @@ struct DevTables {
     const float2 *f_kb;                            // [Nz] (ln w + ln kmin) Nk / ln(kmax/kmin)
     float2 k_a, m_s2, m_x02, z_s2, z_02, lnkmin2, kscale2;  // double-float constants
     float fA, feps, small_arg;
+    float unc_eps, unc_abs;        // FP32 point-value error bound
+    double tau_impact, tau_sel;    // escalation thresholds (fraction of the integral)
     const unsigned long long *tie_z_bits;
     const int *tie_z_round, *tie_z_trunc;
     int n_tie_z;
@@ -71,7 +73,8 @@ struct IntDesc {
     double theta[3];
     double c0[MAX_DIM];   // root centre
     double hw0[MAX_DIM];  // root half-widths
-    double rootvol;
+    double rootvol;       // product of the root widths (FP64 rule)
+    double rootvol_mx;    // mixed path: rootvol * FP32 integrand scale
     double rtol;
     double scale;         // mixed path: true value = scaled value * scale
     unsigned long long max_eval;
@@ -97,6 +100,8 @@ struct Pool {
     unsigned char *split;
     unsigned long long *q;  // fixed-point errors (selection scratch)
     int *cand;              // selected parents, per-integral segment at base
+    float *unc;             // mixed path: bound on the FP32 error of err (0 = FP64 value)
+    int2 *esc;              // regions queued for FP64 re-evaluation: (integral, local slot)
     long long stride;
 };
 
@@ -113,6 +118,11 @@ struct BatchHdr {
     unsigned long long small_arg;
     unsigned long long regions;
     int rounds_done;
+    int mixed;                   // 1: mixed-precision pass (uncertainty bookkeeping on)
+    int n_esc, esc_cap;          // FP64 re-evaluation queue fill / capacity
+    unsigned long long escalated;// statistics: regions re-evaluated in FP64
+    unsigned long long deferred; // statistics: selections deferred for re-evaluation
+    double *dbg;                 // debug: per-point integrand values of one work item
 };
 
 // Point p of a dim-dimensional Genz-Malik rule -> coordinate variant of dim d,

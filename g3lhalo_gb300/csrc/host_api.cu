@@ -23,6 +23,8 @@
 
 namespace g3l {
 void *eval64_kernel(int kind, int term);
+void *reeval64_kernel(int kind, int term);
+void *round_end_kernel();
 void *evalmx_kernel(int kind, int term);
 void *select_kernel();
 void *scan_kernel();
@@ -98,7 +100,12 @@ struct g3l_ctx {
     g3l_options opt{};
     g3l_stats stats{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t tev[16] = {};
+    // pinned staging for the per-call descriptor and result copies
+    void *stage = nullptr;
+    size_t stage_bytes = 0;
     long long *h_pinned = nullptr;
+    size_t last_h2d = 0, last_d2h = 0;
     int64_t next_ticket = 1;
     std::map<int64_t, std::pair<int, std::vector<g3l_result>>> tickets;
 };
@@ -194,6 +201,10 @@ int prepare_mixed(g3l_ctx *c, const g3l_tables *t)
     T.z_02 = dsplit(t->zmin);
     T.z_s2 = dsplit(Nz / (t->zmax - t->zmin));
     T.small_arg = (float)c->opt.small_arg;
+    T.unc_eps = (float)c->opt.unc_eps_rel;
+    T.unc_abs = (float)c->opt.unc_tau_abs;
+    T.tau_impact = c->opt.unc_tau_impact;
+    T.tau_sel = c->opt.unc_tau_sel;
     st |= dalloc(&c->d_fnbar, (size_t)MAX_HOD_SLOTS * Nz);
     st |= dalloc(&c->d_fhodp, (size_t)MAX_HOD_SLOTS * 8);
     if (st) return st;
@@ -246,7 +257,7 @@ int ensure_workspace(g3l_ctx *c, int n, size_t pool)
     if (n > W.n_cap) ncap = std::max(ncap, (int)(n * 1.25) + 16);
     if (pool > W.pool_cap) pcap = std::max(pcap, (size_t)(pool * 1.25) + 1024);
     void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.q, W.P.cand,
-                    W.D,        W.S,       W.woff,  W.H};
+                    W.P.unc,    W.P.esc,   W.D,     W.S,     W.woff,    W.H};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     W = Workspace{W.pool_cap, W.n_cap, Pool{}, nullptr, nullptr, nullptr, nullptr, W.gen};
@@ -260,6 +271,8 @@ int ensure_workspace(g3l_ctx *c, int n, size_t pool)
     st |= dalloc(&W.P.split, pcap);
     st |= dalloc(&W.P.q, pcap);
     st |= dalloc(&W.P.cand, pcap);
+    st |= dalloc(&W.P.unc, pcap);
+    st |= dalloc(&W.P.esc, pcap);
     st |= dalloc(&W.D, (size_t)ncap);
     st |= dalloc(&W.S, (size_t)ncap);
     st |= dalloc(&W.woff, (size_t)ncap + 1);
@@ -300,6 +313,7 @@ struct KernelArgs {
     long long *woff;
     cudaGraphConditionalHandle handle;
     int use_cond;
+    double tau_sel;
 };
 
 int add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *deps, size_t ndeps,
@@ -318,7 +332,7 @@ int add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *deps
 int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
 {
     Workspace &W = c->W;
-    KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 1};
+    KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 1, c->T.tau_sel};
     cudaGraph_t g;
     G3L_CK(cudaGraphCreate(&g, 0));
     cudaGraphNode_t n_init;
@@ -338,7 +352,7 @@ int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     cudaGraphNode_t n_sel, n_scan, prev;
     {
-        void *args[] = {&a.D, &a.S, &a.P, &a.H};
+        void *args[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel};
         int st = add_kernel(body, &n_sel, nullptr, 0, select_kernel(), c->nsm * 8, 256, args);
         if (st) return st;
     }
@@ -357,39 +371,133 @@ int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
         if (st) return st;
         prev = n_ev;
     }
+    if (precision == G3L_MIXED) {
+        for (int grp = 0; grp < NGROUPS; ++grp) {
+            if (!(gmask & (1 << grp))) continue;
+            void *fn = reeval64_kernel(grp / 3, grp % 3 + 1);
+            void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
+            cudaGraphNode_t n_re;
+            int st = add_kernel(body, &n_re, &prev, 1, fn, eval_grid(c, fn), 128, args);
+            if (st) return st;
+            prev = n_re;
+        }
+        void *args[] = {&a.H};
+        cudaGraphNode_t n_end;
+        int st = add_kernel(body, &n_end, &prev, 1, round_end_kernel(), 1, 1, args);
+        if (st) return st;
+    }
     cudaGraphExec_t ex;
     G3L_CK(cudaGraphInstantiate(&ex, g, 0));
     out = GraphEntry{W.gen, precision, gmask, g, ex};
     return G3L_OK;
 }
 
+// descriptor of one integral: bounds and root geometry as the reference computes them
+// (src/NNMap_Model.cu:46-49, 313-314; src/hcubature.cpp:160-172), plus the
+// mixed-precision constants
+bool item_ok(const g3l_ctx *c, const g3l_integral &it)
+{
+    bool ok = (it.kind == G3L_NNMAP || it.kind == G3L_NMAPMAP) && it.term >= 1 && it.term <= 3 &&
+              it.hod1 >= 0 && it.hod1 < MAX_HOD_SLOTS && c->hod_set[it.hod1] &&
+              std::isfinite(it.rtol) && it.rtol >= 0;
+    if (ok && it.kind == G3L_NNMAP)
+        ok = it.hod2 >= 0 && it.hod2 < MAX_HOD_SLOTS && c->hod_set[it.hod2];
+    for (int k = 0; k < 3 && ok; ++k) ok = std::isfinite(it.theta[k]) && it.theta[k] > 0;
+    return ok;
+}
+
+void fill_desc(const g3l_ctx *c, const g3l_integral &it, int precision, IntDesc &d)
+{
+    std::memset(&d, 0, sizeof d);
+    for (int k = 0; k < 3; ++k) d.theta[k] = it.theta[k];
+    double lo[MAX_DIM], hi[MAX_DIM];
+    d.dim = c->B.bounds(it.term, lo, hi);
+    for (int k = 0; k < d.dim; ++k) {
+        d.c0[k] = 0.5 * (lo[k] + hi[k]);
+        d.hw0[k] = 0.5 * (hi[k] - lo[k]);
+    }
+    double vol = 1;
+    for (int k = 0; k < d.dim; ++k) vol *= 2 * d.hw0[k];
+    d.rootvol = vol;
+    if (precision == G3L_MIXED) {
+        static const double lam[3] = {G3L_LAMBDA2, G3L_LAMBDA4, G3L_LAMBDA5};
+        for (int k = 0; k < d.dim; ++k)
+            for (int q = 0; q < 3; ++q) d.hwl[k][q] = dsplit(d.hw0[k] * lam[q]);
+        for (int k = 0; k < 3; ++k) d.th_s[k] = (float)(it.theta[k] * kL0);
+        const int h2 = it.kind == G3L_NNMAP ? it.hod2 : it.hod1;
+        d.rootvol_mx = vol * mixed_scale(c, it.kind, it.term, it.hod1, h2);
+    }
+    d.rtol = it.rtol;
+    d.scale = 1.0;
+    d.max_eval = it.max_eval;
+    d.kind = it.kind;
+    d.term = it.term;
+    d.npts = rule_points(d.dim);
+    d.hod1 = it.hod1;
+    d.hod2 = it.kind == G3L_NNMAP ? it.hod2 : it.hod1;
+    d.same = d.hod1 == d.hod2;
+}
+
 int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
 {
     Workspace &W = c->W;
-    KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 0};
+    KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 0, c->T.tau_sel};
     cudaStream_t s = c->stream;
     {
         void *args[] = {&a.D, &a.S, &a.P, &a.H};
         G3L_CK(cudaLaunchKernel(init_kernel(), dim3(c->nsm * 4), dim3(256), args, 0, s));
         ++*launches;
     }
+    for (int g = 0; g < NGROUPS; ++g) c->stats.group_ms[g] = 0;
+    c->stats.reeval_ms = 0;
+    c->stats.select_ms = 0;
     for (int r = 0; r < c->opt.max_rounds + 4; ++r) {
-        void *sargs[] = {&a.D, &a.S, &a.P, &a.H};
+        void *sargs[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel};
+        G3L_CK(cudaEventRecord(c->tev[14], s));
         G3L_CK(cudaLaunchKernel(select_kernel(), dim3(c->nsm * 8), dim3(256), sargs, 0, s));
         void *cargs[] = {&a.S, &a.woff, &a.H, &a.handle, &a.use_cond};
         G3L_CK(cudaLaunchKernel(scan_kernel(), dim3(1), dim3(1024), cargs, 0, s));
+        G3L_CK(cudaEventRecord(c->tev[15], s));
         *launches += 2;
         for (int grp = 0; grp < NGROUPS; ++grp) {
             if (!(gmask & (1 << grp))) continue;
             void *fn = eval_fn(precision, grp);
             void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
+            G3L_CK(cudaEventRecord(c->tev[2 * grp], s));
             G3L_CK(cudaLaunchKernel(fn, dim3(eval_grid(c, fn)), dim3(128), args, 0, s));
+            G3L_CK(cudaEventRecord(c->tev[2 * grp + 1], s));
             ++*launches;
         }
-        G3L_CK(cudaMemcpyAsync(c->h_pinned, &W.H->total_work, sizeof(long long),
+        if (precision == G3L_MIXED) {
+            G3L_CK(cudaEventRecord(c->tev[12], s));
+            for (int grp = 0; grp < NGROUPS; ++grp) {
+                if (!(gmask & (1 << grp))) continue;
+                void *fn = reeval64_kernel(grp / 3, grp % 3 + 1);
+                void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
+                G3L_CK(cudaLaunchKernel(fn, dim3(eval_grid(c, fn)), dim3(128), args, 0, s));
+                ++*launches;
+            }
+            G3L_CK(cudaEventRecord(c->tev[13], s));
+            void *eargs[] = {&a.H};
+            G3L_CK(cudaLaunchKernel(round_end_kernel(), dim3(1), dim3(1), eargs, 0, s));
+            ++*launches;
+        }
+        G3L_CK(cudaMemcpyAsync(c->h_pinned, &W.H->any_active, sizeof(int),
                                cudaMemcpyDeviceToHost, s));
         G3L_CK(cudaStreamSynchronize(s));
-        if (*c->h_pinned == 0) break;
+        float ms;
+        for (int grp = 0; grp < NGROUPS; ++grp)
+            if (gmask & (1 << grp)) {
+                cudaEventElapsedTime(&ms, c->tev[2 * grp], c->tev[2 * grp + 1]);
+                c->stats.group_ms[grp] += ms;
+            }
+        if (precision == G3L_MIXED) {
+            cudaEventElapsedTime(&ms, c->tev[12], c->tev[13]);
+            c->stats.reeval_ms += ms;
+        }
+        cudaEventElapsedTime(&ms, c->tev[14], c->tev[15]);
+        c->stats.select_ms += ms;
+        if (*(int *)c->h_pinned == 0) break;
     }
     return G3L_OK;
 }
@@ -452,6 +560,7 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
     G3L_CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     G3L_CK(cudaEventCreate(&c->ev0));
     G3L_CK(cudaEventCreate(&c->ev1));
+    for (auto &e : c->tev) G3L_CK(cudaEventCreate(&e));
     G3L_CK(cudaMallocHost(&c->h_pinned, 64));
     c->B = host::Binning{t->Nz, t->Nm, t->Nk, t->zmin, t->zmax, t->mmin, t->mmax, t->kmin, t->kmax};
     c->Om = t->Om;
@@ -472,6 +581,10 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
     c->opt.max_rounds = 4096;
     c->opt.unlimited_pool = 1 << 20;
     c->opt.small_arg = 1e-7;
+    c->opt.unc_eps_rel = 5e-7;
+    c->opt.unc_tau_abs = 1e-34;
+    c->opt.unc_tau_impact = 1e-7;
+    c->opt.unc_tau_sel = 1e-7;
 
     DevTables &T = c->T;
     T.Nz = t->Nz;
@@ -544,13 +657,16 @@ void g3l_ctx_destroy(g3l_ctx *c)
     }
     Workspace &W = c->W;
     void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.q, W.P.cand,
-                    W.D,        W.S,       W.woff,  W.H};
+                    W.P.unc,    W.P.esc,   W.D,     W.S,     W.woff,    W.H};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : c->allocs) cudaFree(p);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    for (auto &e : c->tev)
+        if (e) cudaEventDestroy(e);
+    if (c->stage) cudaFreeHost(c->stage);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -641,6 +757,10 @@ int g3l_set_options(g3l_ctx *c, const g3l_options *o)
         return G3L_ERR_INVALID;
     c->opt = *o;
     c->T.small_arg = (float)o->small_arg;
+    c->T.unc_eps = (float)o->unc_eps_rel;
+    c->T.unc_abs = (float)o->unc_tau_abs;
+    c->T.tau_impact = o->unc_tau_impact;
+    c->T.tau_sel = o->unc_tau_sel;
     for (auto &g : c->graphs) {
         cudaGraphExecDestroy(g.exec);
         cudaGraphDestroy(g.graph);
@@ -669,14 +789,7 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
         return G3L_ERR_INVALID;
     }
     for (int i = 0; i < n; ++i) {
-        const g3l_integral &it = items[i];
-        bool ok = (it.kind == G3L_NNMAP || it.kind == G3L_NMAPMAP) && it.term >= 1 && it.term <= 3 &&
-                  it.hod1 >= 0 && it.hod1 < MAX_HOD_SLOTS && c->hod_set[it.hod1] &&
-                  std::isfinite(it.rtol) && it.rtol >= 0;
-        if (ok && it.kind == G3L_NNMAP)
-            ok = it.hod2 >= 0 && it.hod2 < MAX_HOD_SLOTS && c->hod_set[it.hod2];
-        for (int k = 0; k < 3 && ok; ++k) ok = std::isfinite(it.theta[k]) && it.theta[k] > 0;
-        if (!ok) {
+        if (!item_ok(c, items[i])) {
             host::set_error("g3l_eval: invalid integral " + std::to_string(i) +
                             " (kind, term, unset HOD slot, theta or rtol)");
             return G3L_ERR_INVALID;
@@ -696,34 +809,7 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
     for (int r = 0; r < n; ++r) {
         const g3l_integral &it = items[order[r]];
         IntDesc &d = D[r];
-        std::memset(&d, 0, sizeof d);
-        for (int k = 0; k < 3; ++k) d.theta[k] = it.theta[k];
-        double lo[MAX_DIM], hi[MAX_DIM];
-        d.dim = c->B.bounds(it.term, lo, hi);
-        for (int k = 0; k < d.dim; ++k) {
-            d.c0[k] = 0.5 * (lo[k] + hi[k]);
-            d.hw0[k] = 0.5 * (hi[k] - lo[k]);
-        }
-        double vol = 1;
-        for (int k = 0; k < d.dim; ++k) vol *= 2 * d.hw0[k];
-        d.rootvol = vol;
-        if (precision == G3L_MIXED) {
-            static const double lam[3] = {G3L_LAMBDA2, G3L_LAMBDA4, G3L_LAMBDA5};
-            for (int k = 0; k < d.dim; ++k)
-                for (int q = 0; q < 3; ++q) d.hwl[k][q] = dsplit(d.hw0[k] * lam[q]);
-            for (int k = 0; k < 3; ++k) d.th_s[k] = (float)(it.theta[k] * kL0);
-            const int h2 = it.kind == G3L_NNMAP ? it.hod2 : it.hod1;
-            d.rootvol = vol * mixed_scale(c, it.kind, it.term, it.hod1, h2);
-        }
-        d.rtol = it.rtol;
-        d.scale = 1.0;
-        d.max_eval = it.max_eval;
-        d.kind = it.kind;
-        d.term = it.term;
-        d.npts = rule_points(d.dim);
-        d.hod1 = it.hod1;
-        d.hod2 = it.kind == G3L_NNMAP ? it.hod2 : it.hod1;
-        d.same = d.hod1 == d.hod2;
+        fill_desc(c, it, precision, d);
         unsigned long long cap;
         if (it.max_eval) {
             unsigned long long np = d.npts;
@@ -746,11 +832,33 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
     }
     H.gbeg[NGROUPS] = n;
     H.max_rounds = c->opt.max_rounds;
+    H.mixed = precision == G3L_MIXED ? 1 : 0;
     int st = ensure_workspace(c, n, (size_t)base);
     if (st) return st;
     Workspace &W = c->W;
-    G3L_CK(cudaMemcpyAsync(W.D, D.data(), sizeof(IntDesc) * n, cudaMemcpyHostToDevice, c->stream));
-    G3L_CK(cudaMemcpyAsync(W.H, &H, sizeof(BatchHdr), cudaMemcpyHostToDevice, c->stream));
+    H.esc_cap = (int)std::min<size_t>(W.pool_cap, 0x7fffffff);
+    H.dbg = nullptr;
+    // stage through pinned host memory: descriptors + header in, states + header out
+    const size_t in_bytes = sizeof(IntDesc) * n + sizeof(BatchHdr);
+    const size_t out_bytes = sizeof(IntState) * n + sizeof(BatchHdr);
+    if (c->stage_bytes < in_bytes + out_bytes) {
+        if (c->stage) cudaFreeHost(c->stage);
+        c->stage_bytes = (in_bytes + out_bytes) * 5 / 4 + 4096;
+        if (cudaMallocHost(&c->stage, c->stage_bytes) != cudaSuccess) {
+            c->stage = nullptr;
+            c->stage_bytes = 0;
+            host::set_error("g3l_eval: pinned staging allocation failed");
+            return G3L_ERR_NOMEM;
+        }
+    }
+    char *stg = (char *)c->stage;
+    std::memcpy(stg, D.data(), sizeof(IntDesc) * n);
+    std::memcpy(stg + sizeof(IntDesc) * n, &H, sizeof(BatchHdr));
+    c->last_h2d = in_bytes;
+    c->last_d2h = out_bytes;
+    G3L_CK(cudaMemcpyAsync(W.D, stg, sizeof(IntDesc) * n, cudaMemcpyHostToDevice, c->stream));
+    G3L_CK(cudaMemcpyAsync(W.H, stg + sizeof(IntDesc) * n, sizeof(BatchHdr),
+                           cudaMemcpyHostToDevice, c->stream));
     int launches = 0;
     G3L_CK(cudaEventRecord(c->ev0, c->stream));
     if (c->opt.use_graph) {
@@ -771,29 +879,48 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
         if (st) return st;
     }
     G3L_CK(cudaEventRecord(c->ev1, c->stream));
-    std::vector<IntState> S(n);
-    G3L_CK(cudaMemcpyAsync(S.data(), W.S, sizeof(IntState) * n, cudaMemcpyDeviceToHost, c->stream));
-    BatchHdr Hout;
-    G3L_CK(cudaMemcpyAsync(&Hout, W.H, sizeof(BatchHdr), cudaMemcpyDeviceToHost, c->stream));
+    char *ostg = stg + in_bytes;
+    G3L_CK(cudaMemcpyAsync(ostg, W.S, sizeof(IntState) * n, cudaMemcpyDeviceToHost, c->stream));
+    G3L_CK(cudaMemcpyAsync(ostg + sizeof(IntState) * n, W.H, sizeof(BatchHdr),
+                           cudaMemcpyDeviceToHost, c->stream));
     G3L_CK(cudaStreamSynchronize(c->stream));
+    std::vector<IntState> S(n);
+    std::memcpy(S.data(), ostg, sizeof(IntState) * n);
+    BatchHdr Hout;
+    std::memcpy(&Hout, ostg + sizeof(IntState) * n, sizeof(BatchHdr));
     G3L_CK(cudaGetLastError());
     float ms = 0;
     cudaEventElapsedTime(&ms, c->ev0, c->ev1);
     int ngroups = __builtin_popcount((unsigned)gmask);
     g3l_stats &sx = c->stats;
-    sx = g3l_stats{};
+    {
+        g3l_stats keep = sx;
+        sx = g3l_stats{};
+        if (!c->opt.use_graph) {
+            for (int g = 0; g < NGROUPS; ++g) sx.group_ms[g] = keep.group_ms[g];
+            sx.reeval_ms = keep.reeval_ms;
+            sx.select_ms = keep.select_ms;
+        }
+    }
     sx.rounds = (uint64_t)Hout.rounds_done;
     sx.kernel_launches = launches >= 0 ? (uint64_t)launches
-                                       : (uint64_t)(1 + (Hout.rounds_done + 1) * (2 + ngroups));
+                                       : (uint64_t)(1 + (Hout.rounds_done + 1) *
+                                                           (2 + ngroups +
+                                                            (precision == G3L_MIXED ? ngroups + 1 : 0)));
     sx.regions_evaluated = Hout.regions;
     sx.tie_fallbacks = Hout.ties;
     sx.small_arg_fp64 = Hout.small_arg;
+    sx.escalated = Hout.escalated;
+    sx.h2d_bytes = c->last_h2d;
+    sx.d2h_bytes = c->last_d2h;
+    sx.deferred = Hout.deferred;
     sx.device_ms = ms;
     int first_bad = G3L_OK;
     uint64_t pts = 0;
     for (int r = 0; r < n; ++r) {
         const IntDesc &d = D[r];
         const IntState &s = S[r];
+        sx.group_points[d.kind * 3 + d.term - 1] += s.neval;
         g3l_result &o = out[order[r]];
         o.val = s.val * d.scale;
         o.err = s.err * d.scale;
@@ -807,6 +934,98 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
     sx.points_evaluated = pts;
     if (first_bad) host::set_error("g3l_eval: an integral ended with status " + std::to_string(first_bad));
     return first_bad;
+}
+
+int g3l_debug_region(g3l_ctx *c, const g3l_integral *item, const double *center,
+                     const int *levels, int precision, double *values, double out[3])
+{
+    if (!c || !item || !center || !levels || !values || !out ||
+        (precision != G3L_FP64 && precision != G3L_MIXED) || !item_ok(c, *item)) {
+        host::set_error("g3l_debug_region: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    G3L_CK(cudaSetDevice(c->device));
+    IntDesc d;
+    fill_desc(c, *item, precision, d);
+    for (int k = 0; k < d.dim; ++k)
+        if (levels[k] < 0 || levels[k] > 60 || !std::isfinite(center[k])) {
+            host::set_error("g3l_debug_region: invalid region");
+            return G3L_ERR_INVALID;
+        }
+    d.base = 0;
+    d.cap = 2;
+    int st = ensure_workspace(c, 1, 4);
+    if (st) return st;
+    Workspace &W = c->W;
+    const int grp = item->kind * 3 + item->term - 1;
+    double *dbg;
+    st = dalloc(&dbg, 2 * (size_t)d.npts);
+    if (st) return st;
+    BatchHdr H{};
+    H.n = 1;
+    for (int g = 0; g <= NGROUPS; ++g) H.gbeg[g] = g <= grp ? 0 : 1;
+    H.max_rounds = 1;
+    H.mixed = precision == G3L_MIXED;
+    H.esc_cap = 2;
+    H.dbg = dbg;
+    IntState S{};
+    S.nR = 1;
+    S.K = 1;
+    long long woff[2] = {0, 1};
+    const int cand = -1;
+    cudaStream_t s = c->stream;
+    int rc = G3L_OK;
+    do {
+        if (cudaMemcpyAsync(W.D, &d, sizeof d, cudaMemcpyHostToDevice, s) ||
+            cudaMemcpyAsync(W.H, &H, sizeof H, cudaMemcpyHostToDevice, s) ||
+            cudaMemcpyAsync(W.S, &S, sizeof S, cudaMemcpyHostToDevice, s) ||
+            cudaMemcpyAsync(W.woff, woff, sizeof woff, cudaMemcpyHostToDevice, s) ||
+            cudaMemcpyAsync(W.P.cand, &cand, sizeof cand, cudaMemcpyHostToDevice, s)) {
+            rc = G3L_ERR_CUDA;
+            break;
+        }
+        for (int k = 0; k < d.dim; ++k) {
+            unsigned char lv = (unsigned char)levels[k];
+            if (cudaMemcpyAsync(W.P.center + (size_t)k * W.P.stride, center + k, sizeof(double),
+                                cudaMemcpyHostToDevice, s) ||
+                cudaMemcpyAsync(W.P.level + (size_t)k * W.P.stride, &lv, 1, cudaMemcpyHostToDevice,
+                                s)) {
+                rc = G3L_ERR_CUDA;
+                break;
+            }
+        }
+        if (rc) break;
+        KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 0, 0.0};
+        void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
+        if (cudaLaunchKernel(eval_fn(precision, grp), dim3(1), dim3(128), args, 0, s)) {
+            rc = G3L_ERR_CUDA;
+            break;
+        }
+        double vv[2];
+        unsigned char sp = 0;
+        if (cudaMemcpyAsync(values, dbg, sizeof(double) * d.npts, cudaMemcpyDeviceToHost, s) ||
+            cudaMemcpyAsync(&vv[0], W.P.val, sizeof(double), cudaMemcpyDeviceToHost, s) ||
+            cudaMemcpyAsync(&vv[1], W.P.err, sizeof(double), cudaMemcpyDeviceToHost, s) ||
+            cudaMemcpyAsync(&sp, W.P.split, 1, cudaMemcpyDeviceToHost, s) ||
+            cudaStreamSynchronize(s)) {
+            rc = G3L_ERR_CUDA;
+            break;
+        }
+        out[0] = vv[0];
+        out[1] = vv[1];
+        out[2] = sp;
+    } while (0);
+    if (rc) host::set_error(std::string("g3l_debug_region: ") + cudaGetErrorString(cudaGetLastError()));
+    cudaFree(dbg);
+    return rc;
+}
+
+int g3l_measure_peaks(g3l_ctx *c, double *fp32_tflops, double *fp64_tflops)
+{
+    if (!c || !fp32_tflops || !fp64_tflops) return G3L_ERR_INVALID;
+    G3L_CK(cudaSetDevice(c->device));
+    extern int g3l_probe_peaks(int, cudaStream_t, double *, double *);
+    return g3l_probe_peaks(c->device, c->stream, fp32_tflops, fp64_tflops);
 }
 
 int g3l_submit(g3l_ctx *c, const g3l_integral *items, int n, int precision, int64_t *ticket)

@@ -134,6 +134,12 @@ typedef struct g3l_options {
     uint64_t unlimited_pool; /* region-pool capacity per integral when max_eval == 0 */
     double small_arg;        /* mixed precision: NFW profile arguments k r_s below this
                                 are evaluated in FP64 (default 1e-7) */
+    /* Mixed precision: every FP32 point value v carries the error bound
+     * unc_eps_rel |v| + unc_tau_abs.  A region whose split decision is not settled
+     * under these bounds, or that sits on an unsettled selection boundary, is
+     * re-evaluated in FP64 when its error exceeds unc_tau_impact (split) or
+     * unc_tau_sel (selection) times the integral's running value. */
+    double unc_eps_rel, unc_tau_abs, unc_tau_impact, unc_tau_sel;
 } g3l_options;
 int g3l_get_options(g3l_ctx *ctx, g3l_options *opt);
 int g3l_set_options(g3l_ctx *ctx, const g3l_options *opt);
@@ -149,8 +155,30 @@ typedef struct g3l_stats {
     uint64_t small_arg_fp64;  /* NFW profile evaluations on the small-k r_s FP64 branch */
     double device_ms;         /* device time of the whole call (CUDA events) */
     double eval_ms;           /* of which in the rule-evaluation kernels */
+    uint64_t escalated;       /* mixed precision: regions re-evaluated in FP64 */
+    uint64_t deferred;        /* mixed precision: selections deferred for re-evaluation */
+    /* host-driven rounds only (use_graph = 0): device time and points of the
+     * rule-evaluation kernel of each group (kind * 3 + term - 1), CUDA events */
+    double group_ms[6];
+    uint64_t group_points[6];
+    double reeval_ms;         /* FP64 re-evaluation kernels */
+    double select_ms;         /* selection + scan kernels */
+    uint64_t h2d_bytes, d2h_bytes; /* bytes copied in / out by the call */
 } g3l_stats;
 int g3l_get_stats(g3l_ctx *ctx, g3l_stats *st);
+
+/* Evaluate the Genz-Malik rule of one region of one integral on the device and
+ * return its integrand values at the rule points, in the reference's point order
+ * (src/hcubature.cpp:476-503), plus {val, err, split}.  center[dim] is the region
+ * centre, levels[dim] its bisection depth per dimension (half-width = root
+ * half-width * 2^-level).  Used by the parity tests to compare the device
+ * integrand with the CPU oracle point by point. */
+int g3l_debug_region(g3l_ctx *ctx, const g3l_integral *item, const double *center,
+                     const int *levels, int precision, double *values, double out[3]);
+
+/* Issue-rate probe on the context's device: FP32 and FP64 fused multiply-add
+ * throughput in TFLOP/s (2 flops per FMA), measured with CUDA events. */
+int g3l_measure_peaks(g3l_ctx *ctx, double *fp32_tflops, double *fp64_tflops);
 
 const char *g3l_last_error(void);
 int g3l_abi_version(void);
