@@ -57,7 +57,8 @@ class Options(C.Structure):
                 ("use_graph", C.c_int), ("max_rounds", C.c_int), ("unlimited_pool", C.c_uint64),
                 ("small_arg", C.c_double), ("unc_eps_rel", C.c_double),
                 ("unc_tau_abs", C.c_double), ("unc_tau_impact", C.c_double),
-                ("unc_tau_sel", C.c_double)]
+                ("unc_tau_sel", C.c_double), ("unc_tau_val", C.c_double),
+                ("unc_tau_bsel", C.c_double), ("unc_eps_val", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -65,7 +66,7 @@ class Stats(C.Structure):
                 ("regions_evaluated", C.c_uint64), ("points_evaluated", C.c_uint64),
                 ("tie_fallbacks", C.c_uint64), ("small_arg_fp64", C.c_uint64),
                 ("device_ms", C.c_double), ("eval_ms", C.c_double),
-                ("escalated", C.c_uint64), ("deferred", C.c_uint64),
+                ("escalated", C.c_uint64), ("deferred", C.c_uint64), ("polished", C.c_uint64),
                 ("group_ms", C.c_double * 6), ("group_points", C.c_uint64 * 6),
                 ("reeval_ms", C.c_double), ("select_ms", C.c_double),
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64)]
@@ -106,6 +107,9 @@ def lib():
             L.g3l_measure_peaks.argtypes = [C.c_void_p, _dp, _dp]
             L.g3l_debug_region.argtypes = [C.c_void_p, C.POINTER(Integral), _dp,
                                            C.POINTER(C.c_int), C.c_int, _dp, _dp]
+            L.g3l_debug_pool.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp,
+                                         C.POINTER(C.c_int), _dp, _dp, C.POINTER(C.c_int),
+                                         C.POINTER(C.c_float), C.POINTER(C.c_int)]
             L.g3l_host_densities.argtypes = [C.POINTER(Tables), _dp, _dp, _dp]
             L.g3l_hcubature_v.argtypes = [C.c_uint, C.c_void_p, C.c_void_p, C.c_uint, _dp, _dp,
                                           C.c_size_t, C.c_double, C.c_double, C.c_int, _dp, _dp]
@@ -240,6 +244,27 @@ class Context:
         _check(lib().g3l_debug_region(self.h, items, _ptr(c), lv, precision, _ptr(vals),
                                       _ptr(out)))
         return vals, out
+
+    def debug_pool(self, index):
+        """Live regions of item `index` of the last eval: dict of centers [n, dim],
+        levels [n, dim], val, err, split."""
+        n = C.c_int()
+        _check(lib().g3l_debug_pool(self.h, index, 0, None, None, None, None, None, None,
+                                    C.byref(n)))
+        nr = n.value
+        # dimension from the centre count is unknown here; ask with the largest dim
+        cen = np.zeros(7 * max(nr, 1))
+        lev = np.zeros(7 * max(nr, 1), dtype=np.int32)
+        val = np.zeros(max(nr, 1))
+        err = np.zeros(max(nr, 1))
+        spl = np.zeros(max(nr, 1), dtype=np.int32)
+        unc = np.zeros(2 * max(nr, 1), dtype=np.float32)
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+        _check(lib().g3l_debug_pool(self.h, index, nr, _ptr(cen), ip(lev), _ptr(val), _ptr(err),
+                                    ip(spl), unc.ctypes.data_as(C.POINTER(C.c_float)),
+                                    C.byref(n)))
+        return {"n": nr, "centers": cen, "levels": lev, "val": val[:nr], "err": err[:nr],
+                "split": spl[:nr], "unc": unc[:nr], "uval": unc[nr:2 * nr]}
 
     @staticmethod
     def make_items(specs):

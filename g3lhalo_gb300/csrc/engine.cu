@@ -200,10 +200,10 @@ __device__ void radix_select(const double *err, const unsigned long long *q, lon
 
 __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D,
                                                    IntState *__restrict__ S, Pool P, BatchHdr *H,
-                                                   double tau_sel)
+                                                   double tau_sel, double tau_val)
 {
     __shared__ SelShared sh;
-    __shared__ int s_flag[4];
+    __shared__ int s_flag[4];  // fin, status, polish passes
     __shared__ double s_tot[2];
     const int n = H->n;
     for (int i = blockIdx.x; i < n; i += gridDim.x) {
@@ -250,23 +250,67 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
                 fin = 1;
                 status = ST_ROUNDS;
             }
-            st.val = V;
-            st.err = E;
-            if (fin) {
-                st.done = 1;
-                st.status = status;
-                st.K = 0;
-                S[i] = st;
-            } else {
-                S[i].val = V;
-                S[i].err = E;
-            }
+            S[i].val = V;
+            S[i].err = E;
             s_flag[0] = fin;
+            s_flag[1] = status;
+            s_flag[2] = st.pad;  // polish passes so far
             s_tot[0] = V;
             s_tot[1] = E;
         }
         __syncthreads();
         if (s_flag[0]) {
+            // Mixed precision: before reporting, bound the FP32 noise left in the value.
+            // If the regions' value bounds sum to more than tau_val |V|, re-evaluate in
+            // FP64 the regions with the largest bounds until the rest is below half of it.
+            bool polish = false;
+            if (H->mixed && tau_val > 0.0 && s_flag[1] == ST_OK && s_flag[2] < 2) {
+                const double Vt = s_tot[0];
+                double uloc = 0;
+                for (int j = threadIdx.x; j < R; j += SEL_BS) {
+                    const double kj = fabs(P.val[base + j]) * (double)P.uval[base + j];
+                    P.key[base + j] = kj;
+                    uloc += kj;
+                }
+                const double U = block_sum(uloc, sh.dred);
+                if (U > tau_val * fabs(Vt) && U > 0) {
+                    polish = true;
+                    const double sc = 1152921504606846976.0 / U;
+                    unsigned long long ql = 0;
+                    for (int j = threadIdx.x; j < R; j += SEL_BS) {
+                        double t = P.key[base + j] * sc;
+                        unsigned long long qq = t >= 1.8e19 ? 0xFFFFFFFFFFFFFFFFull : (unsigned long long)t;
+                        P.q[base + j] = qq;
+                        ql += qq;
+                    }
+                    const unsigned long long Qk = block_sum(ql, sh.ured);
+                    const double keep = 0.5 * tau_val * fabs(Vt) * sc;
+                    const unsigned long long qk = keep >= 1.8e19 ? 0xFFFFFFFFFFFFFFFFull : (unsigned long long)keep;
+                    const unsigned long long needp = Qk > qk ? Qk - qk : 1;
+                    unsigned long long pb;
+                    unsigned int pc;
+                    unsigned long long ps;
+                    radix_select(P.key, P.q, base, R, true, needp, sh, pb, pc, ps);
+                    for (int j = threadIdx.x; j < R; j += SEL_BS) {
+                        const unsigned long long kb =
+                            (unsigned long long)__double_as_longlong(P.key[base + j]);
+                        if (kb >= pb && P.uval[base + j] > 0.f) {
+                            const int k = atomicAdd(&H->n_esc, 1);
+                            if (k < H->esc_cap) P.esc[k] = make_int2(i, j | (1 << 30));
+                        }
+                    }
+                    if (threadIdx.x == 0) {
+                        S[i].K = 0;
+                        S[i].pad += 1;
+                        atomicAdd(&H->polished, 1ull);
+                    }
+                }
+            }
+            if (!polish && threadIdx.x == 0) {
+                S[i].done = 1;
+                S[i].status = s_flag[1];
+                S[i].K = 0;
+            }
             __syncthreads();
             continue;
         }
@@ -393,6 +437,7 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
         }
         if (threadIdx.x == 0) {
             S[i].K = (int)K;
+            S[i].bsel = K == (unsigned long long)R ? 0.0 : __longlong_as_double((long long)bkey);
             S[i].neval = neval + twoNp * K;
             S[i].nR = R + (int)K;
             S[i].rounds += 1;
@@ -461,6 +506,7 @@ __global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, 
         st.status = ST_OK;
         st.rounds = 0;
         st.pad = 0;
+        st.bsel = 0;
         S[i] = st;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -473,6 +519,7 @@ __global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, 
         H->n_esc = 0;
         H->escalated = 0;
         H->deferred = 0;
+        H->polished = 0;
     }
 }
 

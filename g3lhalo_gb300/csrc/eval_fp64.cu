@@ -313,6 +313,7 @@ __device__ void warp_item64(const DevTables &T, const IntDesc &d, const Pool &P,
         P.err[slot] = err;
         P.split[slot] = (unsigned char)split;
         if (P.unc) P.unc[slot] = 0.f;
+        if (P.uval) P.uval[slot] = 0.f;
     }
     if (cut && lane < DIM) {
         double cnew = c_l;
@@ -368,90 +369,90 @@ __global__ void __launch_bounds__(128) k_eval64(DevTables T, const IntDesc *__re
     }
 }
 
-// FP64 split decision of the region at slot: only the centre and the 4 dim axis
-// points enter the fourth differences (src/hcubature.cpp:527-575), so only those
-// are evaluated.
-template <int KIND, int TERM>
-__device__ void warp_split64(const DevTables &T, const IntDesc &d, const Pool &P, long long slot,
-                             Slot64 *slots, double *vals, const uint32_t *sdesc,
-                             unsigned long long *ties)
-{
-    constexpr int DIM = TERM + 4;
-    constexpr int NAX = 1 + 4 * DIM;
-    const int lane = threadIdx.x & 31;
-    const long long stride = P.stride;
-    for (int t = lane; t < DIM * 5; t += 32) {  // variants 0..4 (c, -+r2, -+r4) only
-        const int dim = t / 5, v = t - dim * 5;
-        const double c = P.center[dim * stride + slot];
-        const double hw = ldexp(d.hw0[dim], -(int)P.level[dim * stride + slot]);
-        double x = c;
-        if (v > 0) {
-            double r = hw * ((v <= 2) ? G3L_LAMBDA2 : G3L_LAMBDA4);
-            x = (v & 1) ? c - r : c + r;
-        }
-        Model64<KIND, TERM>::fill(T, d, dim, x, slots[dim * NVAR + v], ties);
-    }
-    __syncwarp();
-    for (int p = lane; p < NAX; p += 32) {
-        const uint32_t vv = sdesc[p];
-        const Slot64 *sp[DIM];
-#pragma unroll
-        for (int dd = 0; dd < DIM; ++dd) sp[dd] = &slots[dd * NVAR + ((vv >> (3 * dd)) & 7)];
-        vals[p] = Model64<KIND, TERM>::point(T, d, sp);
-    }
-    __syncwarp();
-    if (lane == 0) {
-        const double ratio = (G3L_LAMBDA2 * G3L_LAMBDA2) / (G3L_LAMBDA4 * G3L_LAMBDA4);
-        const double val0 = vals[0];
-        double maxdiff = 0;
-        int dimDiffMax = 0;
-        for (int k = 0; k < DIM; ++k) {
-            double v0 = vals[1 + 4 * k], v1 = vals[2 + 4 * k];
-            double v2 = vals[3 + 4 * k], v3 = vals[4 + 4 * k];
-            double diff = 0;
-            diff += fabs(v0 + v1 - 2 * val0 - ratio * (v2 + v3 - 2 * val0));
-            if (diff > maxdiff) {
-                maxdiff = diff;
-                dimDiffMax = k;
-            }
-        }
-        P.split[slot] = (unsigned char)dimDiffMax;
-    }
-    __syncwarp();
-}
-
 // FP64 re-evaluation of the regions the mixed-precision pass escalated; each entry is
-// (integral, local slot | kind << 30): kind 0 = split decision only, 1 = whole rule
-// (value, error and split; for selection boundaries).
+// (integral, local slot | kind << 30): kind 0 = split decision only (the centre and
+// the 4 dim axis points enter the fourth differences, src/hcubature.cpp:527-575),
+// kind 1 = whole rule (value, error and split; for selection boundaries).  One
+// 256-thread block per region, one point per thread: few regions are escalated per
+// round, so latency rather than FP64 throughput decides the cost.
 template <int KIND, int TERM>
-__global__ void __launch_bounds__(128) k_reeval64(DevTables T, const IntDesc *__restrict__ D,
+__global__ void __launch_bounds__(256) k_reeval64(DevTables T, const IntDesc *__restrict__ D,
                                                   IntState *__restrict__ S, Pool P, BatchHdr *H,
                                                   const long long *__restrict__ woff)
 {
     constexpr int DIM = TERM + 4;
     constexpr int NP = rule_points(DIM);
-    constexpr int NSLOT = (DIM + 1) * NVAR;
-    constexpr int WPB = 4;
+    constexpr int NAX = 1 + 4 * DIM;
     __shared__ uint32_t sdesc[NP];
-    __shared__ Slot64 sslot[WPB][NSLOT];
-    __shared__ double svals[WPB][2 * NP];
+    __shared__ Slot64 slots[DIM * NVAR];
+    __shared__ double vals[NP];
     const int n = H->n_esc;
     if (n == 0) return;
     for (int p = threadIdx.x; p < NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
     __syncthreads();
     const int g = KIND * 3 + TERM - 1;
-    const int wib = threadIdx.x >> 5;
     const int nmax = n < H->esc_cap ? n : H->esc_cap;
-    for (int e = blockIdx.x * WPB + wib; e < nmax; e += gridDim.x * WPB) {
+    const long long stride = P.stride;
+    for (int e = blockIdx.x; e < nmax; e += gridDim.x) {
         const int2 ent = P.esc[e];
         const IntDesc &d = D[ent.x];
         if (d.kind * 3 + d.term - 1 != g) continue;
         const long long slot = d.base + (ent.y & 0x3FFFFFFF);
-        if (ent.y >> 30)
-            warp_item64<KIND, TERM>(T, d, P, slot, -1, false, sslot[wib], svals[wib], sdesc,
-                                    &H->ties, nullptr);
-        else
-            warp_split64<KIND, TERM>(T, d, P, slot, sslot[wib], svals[wib], sdesc, &H->ties);
+        const bool full = (ent.y >> 30) != 0;
+        const int nv = full ? NVAR : 5;  // split only: variants c, -+r2, -+r4
+        for (int t = threadIdx.x; t < DIM * nv; t += blockDim.x) {
+            const int dim = t / nv, v = t - dim * nv;
+            const double c = P.center[dim * stride + slot];
+            const double hw = ldexp(d.hw0[dim], -(int)P.level[dim * stride + slot]);
+            double x = c;
+            if (v > 0) {
+                double lam = (v <= 2) ? G3L_LAMBDA2 : (v <= 4 ? G3L_LAMBDA4 : G3L_LAMBDA5);
+                double r = hw * lam;
+                x = (v & 1) ? c - r : c + r;
+            }
+            Model64<KIND, TERM>::fill(T, d, dim, x, slots[dim * NVAR + v], &H->ties);
+        }
+        __syncthreads();
+        const int np = full ? NP : NAX;
+        for (int p = threadIdx.x; p < np; p += blockDim.x) {
+            const uint32_t vv = sdesc[p];
+            const Slot64 *sp[DIM];
+#pragma unroll
+            for (int dd = 0; dd < DIM; ++dd) sp[dd] = &slots[dd * NVAR + ((vv >> (3 * dd)) & 7)];
+            vals[p] = Model64<KIND, TERM>::point(T, d, sp);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (full) {
+                int lsum = 0;
+                for (int k = 0; k < DIM; ++k) lsum += P.level[k * stride + slot];
+                double val, err;
+                int split;
+                combine64<DIM>(vals, ldexp(d.rootvol, -lsum), val, err, split);
+                P.val[slot] = val;
+                P.err[slot] = err;
+                P.split[slot] = (unsigned char)split;
+                P.unc[slot] = 0.f;
+                P.uval[slot] = 0.f;
+            } else {
+                const double ratio = (G3L_LAMBDA2 * G3L_LAMBDA2) / (G3L_LAMBDA4 * G3L_LAMBDA4);
+                const double val0 = vals[0];
+                double maxdiff = 0;
+                int dimDiffMax = 0;
+                for (int k = 0; k < DIM; ++k) {
+                    double v0 = vals[1 + 4 * k], v1 = vals[2 + 4 * k];
+                    double v2 = vals[3 + 4 * k], v3 = vals[4 + 4 * k];
+                    double diff = 0;
+                    diff += fabs(v0 + v1 - 2 * val0 - ratio * (v2 + v3 - 2 * val0));
+                    if (diff > maxdiff) {
+                        maxdiff = diff;
+                        dimDiffMax = k;
+                    }
+                }
+                P.split[slot] = (unsigned char)dimDiffMax;
+            }
+        }
+        __syncthreads();
     }
 }
 

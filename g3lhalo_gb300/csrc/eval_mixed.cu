@@ -624,7 +624,7 @@ __device__ __forceinline__ df hw_sum(df a)
 // only if its region could move the integral by more than T.tau_impact of it.
 
 template <int KIND, int TERM>
-__device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, double Vcur,
+__device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, double Vcur, double Bcur,
                            const Pool &P, BatchHdr *H, long long pslot, long long qslot, bool cut,
                            SlotF *slots, float *vals, Child &C, const uint32_t *sdesc,
                            unsigned &ties, int &small)
@@ -789,6 +789,13 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
                      fabsf((float)(W::w3 - W::wE3)) * u3 + fabsf((float)(W::w4 - W::wE4)) * u4 +
                      fabsf((float)W::w5) * u5;
     const float urel = e.hi > 0.f ? fminf(ue / e.hi, 1e30f) : (ue > 0.f ? 1e30f : 0.f);
+    // and of the value (weights of res7)
+    const float uv = fabsf((float)W::w1) * u0 + fabsf((float)W::w2) * u2 +
+                     fabsf((float)W::w3) * u3 + fabsf((float)W::w4) * u4 +
+                     fabsf((float)W::w5) * u5;
+    const float ab7 = fabsf(b7.hi);
+    const float uvrel =
+        ab7 > 0.f ? fminf(T.unc_val_ratio * uv / ab7, 1e30f) : (uv > 0.f ? 1e30f : 0.f);
     // lane 16h+0 -> value, 16h+1 -> error of child h
     const df q = hl == 1 ? e : b7;
     if (active && hl < 2) {
@@ -798,11 +805,15 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
         if (hl == 0) {
             P.val[slot] = out;
             P.split[slot] = (unsigned char)sidx;
+            P.uval[slot] = uvrel;
         } else {
             P.err[slot] = out;
             P.unc[slot] = urel;
-            // an uncertain split of a region that matters: re-evaluate in FP64
-            if (!split_sure && out > T.tau_impact * fabs(Vcur)) {
+            // an uncertain split of a region that matters: re-evaluate in FP64.  A region
+            // matters if its error is a visible part of the integral, or if it can reach
+            // the selection boundary (Bcur = 0 while every region is still being cut).
+            if (!split_sure && (out > T.tau_impact * fabs(Vcur) ||
+                                (T.tau_bsel > 0.0 && out > T.tau_bsel * Bcur))) {
                 const int k = atomicAdd(&H->n_esc, 1);
                 if (k < H->esc_cap) P.esc[k] = make_int2(iint, (int)(slot - d.base));
             }
@@ -855,7 +866,7 @@ __global__ void __launch_bounds__(128) k_evalmx(DevTables T, const IntDesc *__re
         const bool cut = cj >= 0;
         const long long pslot = d.base + (cut ? cj : 0);
         const long long qslot = cut ? d.base + (S[i].nR - S[i].K) + j : -1;
-        warp_itemF<KIND, TERM>(T, d, i, S[i].val, P, H, pslot, qslot, cut, sslot[wib],
+        warp_itemF<KIND, TERM>(T, d, i, S[i].val, S[i].bsel, P, H, pslot, qslot, cut, sslot[wib],
                                svals[wib], schild[wib], sdesc, ties, small);
     }
     // warp-aggregated diagnostics

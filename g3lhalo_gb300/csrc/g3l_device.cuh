@@ -62,8 +62,11 @@ struct DevTables {
     const float2 *f_kb;                            // [Nz] (ln w + ln kmin) Nk / ln(kmax/kmin)
     float2 k_a, m_s2, m_x02, z_s2, z_02, lnkmin2, kscale2;  // double-float constants
     float fA, feps, small_arg;
-    float unc_eps, unc_abs;        // FP32 point-value error bound
+    float unc_eps, unc_abs;        // FP32 point-value error bound (decisions)
+    float unc_val_ratio;           // value-noise bound / decision bound
     double tau_impact, tau_sel;    // escalation thresholds (fraction of the integral)
+    double tau_bsel;               // split escalation threshold (fraction of the last boundary)
+    double tau_val;                // bound on the FP32 noise left in a finished integral
     const unsigned long long *tie_z_bits;
     const int *tie_z_round, *tie_z_trunc;
     int n_tie_z;
@@ -91,6 +94,7 @@ struct IntState {
     double val, err;
     unsigned long long neval;
     int nR, K, done, status, rounds, pad;
+    double bsel;  // error at the last selection boundary (0 while every region is cut)
 };
 
 struct Pool {
@@ -100,7 +104,9 @@ struct Pool {
     unsigned char *split;
     unsigned long long *q;  // fixed-point errors (selection scratch)
     int *cand;              // selected parents, per-integral segment at base
-    float *unc;             // mixed path: bound on the FP32 error of err (0 = FP64 value)
+    float *unc;             // mixed path: bound on the FP32 error of err, relative (0 = FP64)
+    float *uval;            // mixed path: bound on the FP32 error of val, relative (0 = FP64)
+    double *key;            // selection scratch (polish keys |val| * uval)
     int2 *esc;              // regions queued for FP64 re-evaluation: (integral, local slot)
     long long stride;
 };
@@ -122,6 +128,7 @@ struct BatchHdr {
     int n_esc, esc_cap;          // FP64 re-evaluation queue fill / capacity
     unsigned long long escalated;// statistics: regions re-evaluated in FP64
     unsigned long long deferred; // statistics: selections deferred for re-evaluation
+    unsigned long long polished; // statistics: finished integrals polished in FP64
     double *dbg;                 // debug: per-point integrand values of one work item
 };
 

@@ -108,6 +108,9 @@ struct g3l_ctx {
     size_t last_h2d = 0, last_d2h = 0;
     int64_t next_ticket = 1;
     std::map<int64_t, std::pair<int, std::vector<g3l_result>>> tickets;
+    // last g3l_eval: descriptor, live region count and pool position of each item
+    std::vector<IntDesc> last_D;
+    std::vector<int> last_nR, last_pos;
 };
 
 namespace {
@@ -205,6 +208,9 @@ int prepare_mixed(g3l_ctx *c, const g3l_tables *t)
     T.unc_abs = (float)c->opt.unc_tau_abs;
     T.tau_impact = c->opt.unc_tau_impact;
     T.tau_sel = c->opt.unc_tau_sel;
+    T.tau_val = c->opt.unc_tau_val;
+    T.tau_bsel = c->opt.unc_tau_bsel;
+    T.unc_val_ratio = (float)(c->opt.unc_eps_val / c->opt.unc_eps_rel);
     st |= dalloc(&c->d_fnbar, (size_t)MAX_HOD_SLOTS * Nz);
     st |= dalloc(&c->d_fhodp, (size_t)MAX_HOD_SLOTS * 8);
     if (st) return st;
@@ -257,7 +263,7 @@ int ensure_workspace(g3l_ctx *c, int n, size_t pool)
     if (n > W.n_cap) ncap = std::max(ncap, (int)(n * 1.25) + 16);
     if (pool > W.pool_cap) pcap = std::max(pcap, (size_t)(pool * 1.25) + 1024);
     void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.q, W.P.cand,
-                    W.P.unc,    W.P.esc,   W.D,     W.S,     W.woff,    W.H};
+                    W.P.unc,    W.P.esc,   W.P.uval, W.P.key, W.D,  W.S,  W.woff, W.H};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     W = Workspace{W.pool_cap, W.n_cap, Pool{}, nullptr, nullptr, nullptr, nullptr, W.gen};
@@ -272,6 +278,8 @@ int ensure_workspace(g3l_ctx *c, int n, size_t pool)
     st |= dalloc(&W.P.q, pcap);
     st |= dalloc(&W.P.cand, pcap);
     st |= dalloc(&W.P.unc, pcap);
+    st |= dalloc(&W.P.uval, pcap);
+    st |= dalloc(&W.P.key, pcap);
     st |= dalloc(&W.P.esc, pcap);
     st |= dalloc(&W.D, (size_t)ncap);
     st |= dalloc(&W.S, (size_t)ncap);
@@ -304,6 +312,13 @@ int eval_grid(g3l_ctx *c, void *fn)
     return nb * c->nsm;
 }
 
+int reeval_grid(g3l_ctx *c, void *fn)
+{
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 256, 0) != cudaSuccess || nb < 1) nb = 1;
+    return nb * c->nsm;
+}
+
 struct KernelArgs {
     DevTables T;
     IntDesc *D;
@@ -314,6 +329,7 @@ struct KernelArgs {
     cudaGraphConditionalHandle handle;
     int use_cond;
     double tau_sel;
+    double tau_val;
 };
 
 int add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *deps, size_t ndeps,
@@ -332,7 +348,7 @@ int add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *deps
 int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
 {
     Workspace &W = c->W;
-    KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 1, c->T.tau_sel};
+    KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 1, c->T.tau_sel, c->T.tau_val};
     cudaGraph_t g;
     G3L_CK(cudaGraphCreate(&g, 0));
     cudaGraphNode_t n_init;
@@ -352,7 +368,7 @@ int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     cudaGraphNode_t n_sel, n_scan, prev;
     {
-        void *args[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel};
+        void *args[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val};
         int st = add_kernel(body, &n_sel, nullptr, 0, select_kernel(), c->nsm * 8, 256, args);
         if (st) return st;
     }
@@ -377,7 +393,7 @@ int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
             void *fn = reeval64_kernel(grp / 3, grp % 3 + 1);
             void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
             cudaGraphNode_t n_re;
-            int st = add_kernel(body, &n_re, &prev, 1, fn, eval_grid(c, fn), 128, args);
+            int st = add_kernel(body, &n_re, &prev, 1, fn, reeval_grid(c, fn), 256, args);
             if (st) return st;
             prev = n_re;
         }
@@ -441,7 +457,7 @@ void fill_desc(const g3l_ctx *c, const g3l_integral &it, int precision, IntDesc 
 int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
 {
     Workspace &W = c->W;
-    KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 0, c->T.tau_sel};
+    KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 0, c->T.tau_sel, c->T.tau_val};
     cudaStream_t s = c->stream;
     {
         void *args[] = {&a.D, &a.S, &a.P, &a.H};
@@ -452,7 +468,7 @@ int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
     c->stats.reeval_ms = 0;
     c->stats.select_ms = 0;
     for (int r = 0; r < c->opt.max_rounds + 4; ++r) {
-        void *sargs[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel};
+        void *sargs[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val};
         G3L_CK(cudaEventRecord(c->tev[14], s));
         G3L_CK(cudaLaunchKernel(select_kernel(), dim3(c->nsm * 8), dim3(256), sargs, 0, s));
         void *cargs[] = {&a.S, &a.woff, &a.H, &a.handle, &a.use_cond};
@@ -474,7 +490,7 @@ int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
                 if (!(gmask & (1 << grp))) continue;
                 void *fn = reeval64_kernel(grp / 3, grp % 3 + 1);
                 void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
-                G3L_CK(cudaLaunchKernel(fn, dim3(eval_grid(c, fn)), dim3(128), args, 0, s));
+                G3L_CK(cudaLaunchKernel(fn, dim3(reeval_grid(c, fn)), dim3(256), args, 0, s));
                 ++*launches;
             }
             G3L_CK(cudaEventRecord(c->tev[13], s));
@@ -581,10 +597,18 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
     c->opt.max_rounds = 4096;
     c->opt.unlimited_pool = 1 << 20;
     c->opt.small_arg = 1e-7;
-    c->opt.unc_eps_rel = 5e-7;
+    // Point-value bounds: FP32 chains with tail amplification (aperture filter,
+    // occupation tails) reach ~1e-5 relative, so decisions use 5e-5; the value-noise
+    // estimate uses the typical 5e-6.  Every unsettled split is re-evaluated
+    // (impact 0); finished integrals whose value noise may exceed 5e-5 of the value
+    // are polished in FP64.
+    c->opt.unc_eps_rel = 5e-5;
     c->opt.unc_tau_abs = 1e-34;
-    c->opt.unc_tau_impact = 1e-7;
+    c->opt.unc_tau_impact = 0.0;
     c->opt.unc_tau_sel = 1e-7;
+    c->opt.unc_tau_val = 5e-5;
+    c->opt.unc_tau_bsel = 0.0;
+    c->opt.unc_eps_val = 5e-6;
 
     DevTables &T = c->T;
     T.Nz = t->Nz;
@@ -657,7 +681,7 @@ void g3l_ctx_destroy(g3l_ctx *c)
     }
     Workspace &W = c->W;
     void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.q, W.P.cand,
-                    W.P.unc,    W.P.esc,   W.D,     W.S,     W.woff,    W.H};
+                    W.P.unc,    W.P.esc,   W.P.uval, W.P.key, W.D,  W.S,  W.woff, W.H};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : c->allocs) cudaFree(p);
@@ -753,14 +777,20 @@ int g3l_get_options(g3l_ctx *c, g3l_options *o)
 
 int g3l_set_options(g3l_ctx *c, const g3l_options *o)
 {
-    if (!c || !o || o->max_rounds < 1 || o->unlimited_pool < 16 || !(o->small_arg >= 0))
+    if (!c || !o || o->max_rounds < 1 || o->unlimited_pool < 16 || !(o->small_arg >= 0) ||
+        !(o->unc_eps_rel > 0) || !(o->unc_eps_val >= 0)) {
+        host::set_error("g3l_set_options: invalid option value");
         return G3L_ERR_INVALID;
+    }
     c->opt = *o;
     c->T.small_arg = (float)o->small_arg;
     c->T.unc_eps = (float)o->unc_eps_rel;
     c->T.unc_abs = (float)o->unc_tau_abs;
     c->T.tau_impact = o->unc_tau_impact;
     c->T.tau_sel = o->unc_tau_sel;
+    c->T.tau_val = o->unc_tau_val;
+    c->T.tau_bsel = o->unc_tau_bsel;
+    c->T.unc_val_ratio = (float)(o->unc_eps_val / o->unc_eps_rel);
     for (auto &g : c->graphs) {
         cudaGraphExecDestroy(g.exec);
         cudaGraphDestroy(g.graph);
@@ -914,6 +944,7 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
     sx.h2d_bytes = c->last_h2d;
     sx.d2h_bytes = c->last_d2h;
     sx.deferred = Hout.deferred;
+    sx.polished = Hout.polished;
     sx.device_ms = ms;
     int first_bad = G3L_OK;
     uint64_t pts = 0;
@@ -932,8 +963,57 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
         if (o.status && !first_bad) first_bad = o.status;
     }
     sx.points_evaluated = pts;
+    c->last_D = D;
+    c->last_nR.resize(n);
+    c->last_pos.resize(n);
+    for (int r = 0; r < n; ++r) {
+        c->last_nR[r] = S[r].nR;
+        c->last_pos[order[r]] = r;
+    }
     if (first_bad) host::set_error("g3l_eval: an integral ended with status " + std::to_string(first_bad));
     return first_bad;
+}
+
+int g3l_debug_pool(g3l_ctx *c, int index, int max_regions, double *centers, int *levels,
+                   double *val, double *err, int *split, float *unc, int *n_regions)
+{
+    if (!c || !n_regions || index < 0 || index >= (int)c->last_pos.size() || max_regions < 0) {
+        host::set_error("g3l_debug_pool: invalid arguments or no previous g3l_eval");
+        return G3L_ERR_INVALID;
+    }
+    const int r = c->last_pos[index];
+    const IntDesc &d = c->last_D[r];
+    const int nR = c->last_nR[r];
+    *n_regions = nR;
+    if (max_regions < nR) return G3L_OK;  // size query
+    if (!centers || !levels || !val || !err || !split) {
+        host::set_error("g3l_debug_pool: null output array");
+        return G3L_ERR_INVALID;
+    }
+    G3L_CK(cudaSetDevice(c->device));
+    G3L_CK(cudaStreamSynchronize(c->stream));
+    const Workspace &W = c->W;
+    const long long stride = W.P.stride;
+    std::vector<unsigned char> b(nR);
+    for (int k = 0; k < d.dim; ++k) {
+        G3L_CK(cudaMemcpy(centers + (size_t)k * nR, W.P.center + k * stride + d.base,
+                          nR * sizeof(double), cudaMemcpyDeviceToHost));
+        G3L_CK(cudaMemcpy(b.data(), W.P.level + k * stride + d.base, nR, cudaMemcpyDeviceToHost));
+        for (int j = 0; j < nR; ++j) levels[(size_t)k * nR + j] = b[j];
+    }
+    G3L_CK(cudaMemcpy(val, W.P.val + d.base, nR * sizeof(double), cudaMemcpyDeviceToHost));
+    G3L_CK(cudaMemcpy(err, W.P.err + d.base, nR * sizeof(double), cudaMemcpyDeviceToHost));
+    G3L_CK(cudaMemcpy(b.data(), W.P.split + d.base, nR, cudaMemcpyDeviceToHost));
+    for (int j = 0; j < nR; ++j) {
+        split[j] = b[j];
+        val[j] *= d.scale;
+        err[j] *= d.scale;
+    }
+    if (unc) {
+        G3L_CK(cudaMemcpy(unc, W.P.unc + d.base, nR * sizeof(float), cudaMemcpyDeviceToHost));
+        G3L_CK(cudaMemcpy(unc + nR, W.P.uval + d.base, nR * sizeof(float), cudaMemcpyDeviceToHost));
+    }
+    return G3L_OK;
 }
 
 int g3l_debug_region(g3l_ctx *c, const g3l_integral *item, const double *center,
@@ -995,7 +1075,7 @@ int g3l_debug_region(g3l_ctx *c, const g3l_integral *item, const double *center,
             }
         }
         if (rc) break;
-        KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 0, 0.0};
+        KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 0, 0.0, 0.0};
         void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
         if (cudaLaunchKernel(eval_fn(precision, grp), dim3(1), dim3(128), args, 0, s)) {
             rc = G3L_ERR_CUDA;

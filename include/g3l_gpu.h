@@ -135,11 +135,23 @@ typedef struct g3l_options {
     double small_arg;        /* mixed precision: NFW profile arguments k r_s below this
                                 are evaluated in FP64 (default 1e-7) */
     /* Mixed precision: every FP32 point value v carries the error bound
-     * unc_eps_rel |v| + unc_tau_abs.  A region whose split decision is not settled
-     * under these bounds, or that sits on an unsettled selection boundary, is
-     * re-evaluated in FP64 when its error exceeds unc_tau_impact (split) or
-     * unc_tau_sel (selection) times the integral's running value. */
+     * unc_eps_rel |v| + unc_tau_abs (defaults 5e-5, 1e-34).  A region whose split
+     * decision is not settled under these bounds, or that sits on an unsettled
+     * selection boundary, is re-evaluated in FP64 when its error exceeds
+     * unc_tau_impact (split, default 0: always) or unc_tau_sel (selection, default
+     * 1e-7) times the integral's running value. */
     double unc_eps_rel, unc_tau_abs, unc_tau_impact, unc_tau_sel;
+    /* A finished integral whose regions' value bounds sum to more than
+     * unc_tau_val |value| has its largest-bound regions re-evaluated in FP64, at
+     * most twice (default 5e-5; 0 = off). */
+    double unc_tau_val;
+    /* An unsettled split is also re-evaluated when the region's error exceeds
+     * unc_tau_bsel times the error at the integral's last selection boundary, or
+     * in any round that cuts every region (default 0 = off). */
+    double unc_tau_bsel;
+    /* Relative bound on the FP32 error of one point value used for the value-noise
+     * estimate of unc_tau_val (decisions use unc_eps_rel; default 5e-6). */
+    double unc_eps_val;
 } g3l_options;
 int g3l_get_options(g3l_ctx *ctx, g3l_options *opt);
 int g3l_set_options(g3l_ctx *ctx, const g3l_options *opt);
@@ -157,6 +169,7 @@ typedef struct g3l_stats {
     double eval_ms;           /* of which in the rule-evaluation kernels */
     uint64_t escalated;       /* mixed precision: regions re-evaluated in FP64 */
     uint64_t deferred;        /* mixed precision: selections deferred for re-evaluation */
+    uint64_t polished;        /* mixed precision: finished integrals polished in FP64 */
     /* host-driven rounds only (use_graph = 0): device time and points of the
      * rule-evaluation kernel of each group (kind * 3 + term - 1), CUDA events */
     double group_ms[6];
@@ -175,6 +188,16 @@ int g3l_get_stats(g3l_ctx *ctx, g3l_stats *st);
  * integrand with the CPU oracle point by point. */
 int g3l_debug_region(g3l_ctx *ctx, const g3l_integral *item, const double *center,
                      const int *levels, int precision, double *values, double out[3]);
+
+/* Copy the live regions of item `index` of the last g3l_eval (before any other
+ * call on the context): centres and levels dimension-major ([dim][n]), value and
+ * error in the integral's units, and the stored split dimension; unc (optional,
+ * [2][n]) receives the mixed path's relative bounds on the FP32 error of err and
+ * of val (0 for regions evaluated in FP64).  With max_regions below the region
+ * count only *n_regions is written.  Used by the tests to compare the region
+ * sets of the two precisions. */
+int g3l_debug_pool(g3l_ctx *ctx, int index, int max_regions, double *centers, int *levels,
+                   double *val, double *err, int *split, float *unc, int *n_regions);
 
 /* Issue-rate probe on the context's device: FP32 and FP64 fused multiply-add
  * throughput in TFLOP/s (2 flops per FMA), measured with CUDA events. */
