@@ -107,6 +107,8 @@ def lib():
             L.g3l_measure_peaks.argtypes = [C.c_void_p, _dp, _dp]
             L.g3l_debug_region.argtypes = [C.c_void_p, C.POINTER(Integral), _dp,
                                            C.POINTER(C.c_int), C.c_int, _dp, _dp]
+            L.g3l_eval_static.argtypes = [C.c_void_p, C.POINTER(Integral), C.c_int, C.c_int,
+                                          C.POINTER(Result)]
             L.g3l_debug_pool.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp,
                                          C.POINTER(C.c_int), _dp, _dp, C.POINTER(C.c_int),
                                          C.POINTER(C.c_float), C.POINTER(C.c_int)]

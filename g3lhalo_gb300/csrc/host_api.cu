@@ -1137,3 +1137,255 @@ int g3l_cancel(g3l_ctx *c, int64_t ticket)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------- fixed-scratch entry point
+//
+// g3l_eval_static runs the same device engine as g3l_eval, but every per-call device
+// buffer (batch header, descriptors, states, work offsets and the region pools) is
+// carved out of one file-scope __device__ array instead of the context's workspace,
+// and the refinement rounds are driven from the host with plain kernel launches.  The
+// call therefore allocates no device memory, no pinned host memory and no graph: it is
+// for callers that must not allocate at evaluation time (a process whose device memory
+// is owned by another allocator, or a latency-critical loop that cannot afford an
+// allocation's implicit synchronisation).
+namespace {
+
+constexpr size_t kStaticScratchBytes = 64ull << 20;  // 64 MiB per device
+constexpr int kStaticMaxItems = 1024;
+constexpr int kStaticMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g3l_static_scratch[kStaticScratchBytes];
+
+std::mutex g_static_mu;
+void *g_static_base[kStaticMaxDevices];  // device address of the scratch, per device
+
+// Host staging for one call (static: the entry point is not reentrant).
+IntDesc g_st_desc[kStaticMaxItems];
+IntState g_st_state[kStaticMaxItems];
+int g_st_order[kStaticMaxItems];
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Bytes of scratch a call with n integrals and `pool` region slots needs, and the
+// offsets of its arrays (same arrays as the context workspace).
+struct StaticLayout {
+    size_t H, D, S, woff, center, level, val, err, split, q, cand, unc, uval, key, esc, end;
+};
+
+StaticLayout static_layout(int n, size_t pool)
+{
+    StaticLayout L{};
+    size_t o = 0;
+    L.H = o;      o = align256(o + sizeof(BatchHdr));
+    L.D = o;      o = align256(o + sizeof(IntDesc) * (size_t)n);
+    L.S = o;      o = align256(o + sizeof(IntState) * (size_t)n);
+    L.woff = o;   o = align256(o + sizeof(long long) * ((size_t)n + 1));
+    L.center = o; o = align256(o + sizeof(double) * pool * MAX_DIM);
+    L.level = o;  o = align256(o + pool * MAX_DIM);
+    L.val = o;    o = align256(o + sizeof(double) * pool);
+    L.err = o;    o = align256(o + sizeof(double) * pool);
+    L.split = o;  o = align256(o + pool);
+    L.q = o;      o = align256(o + sizeof(unsigned long long) * pool);
+    L.cand = o;   o = align256(o + sizeof(int) * pool);
+    L.unc = o;    o = align256(o + sizeof(float) * pool);
+    L.uval = o;   o = align256(o + sizeof(float) * pool);
+    L.key = o;    o = align256(o + sizeof(double) * pool);
+    L.esc = o;    o = align256(o + sizeof(int2) * pool);
+    L.end = o;
+    return L;
+}
+
+// Resolve the scratch address on the current device (once per device).
+int static_scratch(int device, unsigned char **base)
+{
+    if (device < 0 || device >= kStaticMaxDevices) {
+        host::set_error("g3l_eval_static: device ordinal beyond the supported range");
+        return G3L_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_base[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g3l_static_scratch);
+        if (e != cudaSuccess || !p) {
+            host::set_error(std::string("g3l_eval_static: cudaGetSymbolAddress failed: ") +
+                            cudaGetErrorString(e));
+            return G3L_ERR_CUDA;
+        }
+        g_static_base[device] = p;
+    }
+    *base = (unsigned char *)g_static_base[device];
+    return G3L_OK;
+}
+
+}  // namespace
+
+extern "C" int g3l_eval_static(g3l_ctx *c, const g3l_integral *items, int n, int precision,
+                               g3l_result *out)
+{
+    if (!c || n < 0 || (n > 0 && (!items || !out)) ||
+        (precision != G3L_FP64 && precision != G3L_MIXED)) {
+        host::set_error("g3l_eval_static: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    if (n == 0) return G3L_OK;
+    if (n > kStaticMaxItems) {
+        host::set_error("g3l_eval_static: " + std::to_string(n) + " integrals exceed the limit of " +
+                        std::to_string(kStaticMaxItems) + " per call");
+        return G3L_ERR_INVALID;
+    }
+    for (int i = 0; i < n; ++i)
+        if (!item_ok(c, items[i])) {
+            host::set_error("g3l_eval_static: invalid integral " + std::to_string(i));
+            return G3L_ERR_INVALID;
+        }
+    // descriptors in group order (stable counting sort, no temporary buffer), pool
+    // capacities as g3l_eval
+    auto grp = [&](int i) { return items[i].kind * 3 + items[i].term - 1; };
+    {
+        int cnt[NGROUPS + 1] = {};
+        for (int i = 0; i < n; ++i) ++cnt[grp(i) + 1];
+        for (int g = 0; g < NGROUPS; ++g) cnt[g + 1] += cnt[g];
+        for (int i = 0; i < n; ++i) g_st_order[cnt[grp(i)]++] = i;
+    }
+    BatchHdr H{};  // zero: every counter of the header starts at zero
+    H.n = n;
+    int gmask = 0;
+    size_t pool = 0;
+    for (int r = 0; r < n; ++r) {
+        const g3l_integral &it = items[g_st_order[r]];
+        IntDesc &d = g_st_desc[r];
+        fill_desc(c, it, precision, d);
+        unsigned long long cap;
+        if (it.max_eval) {
+            unsigned long long np = d.npts;
+            cap = 3 + (it.max_eval + np) / (2 * np);
+        } else {
+            cap = c->opt.unlimited_pool;
+        }
+        if (cap > (1ull << 30)) {
+            host::set_error("g3l_eval_static: max_eval too large for one region pool");
+            return G3L_ERR_INVALID;
+        }
+        d.cap = (int)cap;
+        d.base = (long long)pool;
+        pool += cap;
+        gmask |= 1 << grp(g_st_order[r]);
+    }
+    const StaticLayout L = static_layout(n, pool);
+    if (L.end > kStaticScratchBytes) {
+        host::set_error("g3l_eval_static: the batch needs " + std::to_string(L.end) +
+                        " bytes of scratch (" + std::to_string(pool) +
+                        " region slots); the fixed scratch holds " +
+                        std::to_string(kStaticScratchBytes) + " bytes -- lower max_eval or split "
+                        "the batch");
+        return G3L_ERR_INVALID;
+    }
+    for (int g = 0, r = 0; g <= NGROUPS; ++g) {
+        while (r < n && grp(g_st_order[r]) < g) ++r;
+        H.gbeg[g] = r;
+    }
+    H.gbeg[NGROUPS] = n;
+    H.max_rounds = c->opt.max_rounds;
+    H.mixed = precision == G3L_MIXED ? 1 : 0;
+    H.esc_cap = (int)std::min<size_t>(pool, 0x7fffffff);
+    H.dbg = nullptr;
+
+    G3L_CK(cudaSetDevice(c->device));
+    unsigned char *base = nullptr;
+    int st = static_scratch(c->device, &base);
+    if (st) return st;
+    KernelArgs a{};
+    a.T = c->T;
+    a.H = (BatchHdr *)(base + L.H);
+    a.D = (IntDesc *)(base + L.D);
+    a.S = (IntState *)(base + L.S);
+    a.woff = (long long *)(base + L.woff);
+    a.P.center = (double *)(base + L.center);
+    a.P.level = base + L.level;
+    a.P.val = (double *)(base + L.val);
+    a.P.err = (double *)(base + L.err);
+    a.P.split = base + L.split;
+    a.P.q = (unsigned long long *)(base + L.q);
+    a.P.cand = (int *)(base + L.cand);
+    a.P.unc = (float *)(base + L.unc);
+    a.P.uval = (float *)(base + L.uval);
+    a.P.key = (double *)(base + L.key);
+    a.P.esc = (int2 *)(base + L.esc);
+    a.P.stride = (long long)pool;
+    a.handle = 0;
+    a.use_cond = 0;
+    a.tau_sel = c->T.tau_sel;
+    a.tau_val = c->T.tau_val;
+    cudaStream_t s = c->stream;
+    // The uploaded header and the init kernel's states are all that must start at a
+    // known value; the pools are written before they are read.
+    G3L_CK(cudaMemcpyAsync(a.D, g_st_desc, sizeof(IntDesc) * n, cudaMemcpyHostToDevice, s));
+    G3L_CK(cudaMemcpyAsync(a.H, &H, sizeof(BatchHdr), cudaMemcpyHostToDevice, s));
+    int launches = 0;
+    {
+        void *args[] = {&a.D, &a.S, &a.P, &a.H};
+        G3L_CK(cudaLaunchKernel(init_kernel(), dim3(c->nsm * 4), dim3(256), args, 0, s));
+        ++launches;
+    }
+    int active = 1;
+    for (int r = 0; r < c->opt.max_rounds + 4 && active; ++r) {
+        void *sargs[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val};
+        G3L_CK(cudaLaunchKernel(select_kernel(), dim3(c->nsm * 8), dim3(256), sargs, 0, s));
+        void *cargs[] = {&a.S, &a.woff, &a.H, &a.handle, &a.use_cond};
+        G3L_CK(cudaLaunchKernel(scan_kernel(), dim3(1), dim3(1024), cargs, 0, s));
+        launches += 2;
+        for (int g = 0; g < NGROUPS; ++g) {
+            if (!(gmask & (1 << g))) continue;
+            void *fn = eval_fn(precision, g);
+            void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
+            G3L_CK(cudaLaunchKernel(fn, dim3(eval_grid(c, fn)), dim3(128), args, 0, s));
+            ++launches;
+        }
+        if (precision == G3L_MIXED) {
+            for (int g = 0; g < NGROUPS; ++g) {
+                if (!(gmask & (1 << g))) continue;
+                void *fn = reeval64_kernel(g / 3, g % 3 + 1);
+                void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
+                G3L_CK(cudaLaunchKernel(fn, dim3(reeval_grid(c, fn)), dim3(256), args, 0, s));
+                ++launches;
+            }
+            void *eargs[] = {&a.H};
+            G3L_CK(cudaLaunchKernel(round_end_kernel(), dim3(1), dim3(1), eargs, 0, s));
+            ++launches;
+        }
+        G3L_CK(cudaMemcpyAsync(&active, &a.H->any_active, sizeof(int), cudaMemcpyDeviceToHost, s));
+        G3L_CK(cudaStreamSynchronize(s));
+    }
+    BatchHdr Hout;
+    G3L_CK(cudaMemcpyAsync(g_st_state, a.S, sizeof(IntState) * n, cudaMemcpyDeviceToHost, s));
+    G3L_CK(cudaMemcpyAsync(&Hout, a.H, sizeof(BatchHdr), cudaMemcpyDeviceToHost, s));
+    G3L_CK(cudaStreamSynchronize(s));
+    G3L_CK(cudaGetLastError());
+    int first_bad = G3L_OK;
+    for (int r = 0; r < n; ++r) {
+        const IntDesc &d = g_st_desc[r];
+        const IntState &sr = g_st_state[r];
+        g3l_result &o = out[g_st_order[r]];
+        o.val = sr.val * d.scale;
+        o.err = sr.err * d.scale;
+        o.neval = sr.neval;
+        o.status = sr.done ? sr.status : G3L_ERR_ROUNDS;
+        o.rounds = sr.rounds;
+        o.result = host::apply_prefactor(d.kind, d.term, c->H0, c->Om, o.val);
+        if (o.status && !first_bad) first_bad = o.status;
+    }
+    c->stats = g3l_stats{};
+    c->stats.kernel_launches = (uint64_t)launches;
+    c->stats.rounds = (uint64_t)Hout.rounds_done;
+    c->stats.regions_evaluated = Hout.regions;
+    c->stats.tie_fallbacks = Hout.ties;
+    c->stats.small_arg_fp64 = Hout.small_arg;
+    c->stats.escalated = Hout.escalated;
+    c->stats.deferred = Hout.deferred;
+    c->stats.polished = Hout.polished;
+    c->stats.h2d_bytes = sizeof(IntDesc) * n + sizeof(BatchHdr);
+    c->stats.d2h_bytes = sizeof(IntState) * n + sizeof(BatchHdr) + sizeof(int) * Hout.rounds_done;
+    if (first_bad)
+        host::set_error("g3l_eval_static: an integral ended with status " + std::to_string(first_bad));
+    return first_bad;
+}

@@ -189,6 +189,26 @@ int g3l_get_stats(g3l_ctx *ctx, g3l_stats *st);
 int g3l_debug_region(g3l_ctx *ctx, const g3l_integral *item, const double *center,
                      const int *levels, int precision, double *values, double out[3]);
 
+/* g3l_eval without allocation (no counterpart in the reference, whose term methods
+ * copy their points through a fresh device buffer every round).  Same items, results
+ * and statuses as g3l_eval, for callers that must not allocate device or pinned host
+ * memory while evaluating -- e.g. a process whose device memory is owned by another
+ * allocator, or a loop that cannot take an allocation's implicit synchronisation.
+ *  - Scratch: one fixed 64 MiB device array per device, built into the library.  A
+ *    call may hold at most 1024 integrals and as many region slots as fit beside them
+ *    (about 116 bytes per slot; each integral takes 3 + (max_eval + P) / (2 P) slots
+ *    for its P-point rule, so ~550k slots, e.g. 260 seven-dimensional integrals at
+ *    max_eval = 1e6).  Larger calls fail with G3L_ERR_INVALID and a message stating
+ *    the bytes needed; nothing is evaluated.
+ *  - Set-up: the first call on a device looks up the scratch's device address (with
+ *    that device current); make that first call before capturing any stream.
+ *  - The scratch is shared by every context on a device: calls must not overlap
+ *    (from several threads, contexts or streams); overlapping calls race.
+ *  - Rounds are driven from the host with plain kernel launches (one small
+ *    device-to-host read per round); the context's own workspace is not touched. */
+int g3l_eval_static(g3l_ctx *ctx, const g3l_integral *items, int n, int precision,
+                    g3l_result *out);
+
 /* Copy the live regions of item `index` of the last g3l_eval (before any other
  * call on the context): centres and levels dimension-major ([dim][n]), value and
  * error in the integral's units, and the stored split dimension; unc (optional,
