@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--max-eval", type=int, default=MAX_EVAL)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    # smaller cases for profiler captures: N evenly spaced triplets, host-driven rounds
+    ap.add_argument("--triplets", type=int, default=0)
+    ap.add_argument("--host-loop", action="store_true")
     return ap.parse_args()
 
 
@@ -193,8 +196,12 @@ def main():
 
     import g3lhalo_gb300 as G
     T, trip, hods = workload()
+    if args.triplets:
+        trip = [trip[i] for i in np.linspace(0, len(trip) - 1, args.triplets).astype(int)]
     ctx = G.Context(T, device=local)
     ctx.set_hod(1, hods[0])
+    if args.host_loop:
+        ctx.set_options(use_graph=0)
 
     def specs(slot):
         return [(G.NNMAP, t, slot, slot, tuple(th), RTOL, args.max_eval) for th in trip
@@ -252,8 +259,9 @@ def main():
            "gpu_launches": launches, "clocks": clk,
            "stats_last_step": {k: st_last[k] for k in ("rounds", "regions_evaluated",
                                                         "points_evaluated", "escalated",
-                                                        "deferred", "tie_fallbacks",
-                                                        "small_arg_fp64")}}
+                                                        "deferred", "polished",
+                                                        "tie_fallbacks", "small_arg_fp64",
+                                                        "group_points")}}
     if rank == 0:
         # peaks of this device
         p32, p64 = ctx.measure_peaks()
@@ -278,7 +286,7 @@ def main():
         ctx.set_hod(0, hods[last_hod])
         ctx.eval(specs(0), G.MIXED)
         sr = ctx.stats()
-        ctx.set_options(use_graph=1)
+        ctx.set_options(use_graph=0 if args.host_loop else 1)
         g = 1  # NNMap 2-halo
         fpp = FLOPS_PER_POINT["nnmap_2h"]
         ms_g = sr["group_ms"][g]

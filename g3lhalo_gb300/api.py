@@ -58,7 +58,7 @@ class Options(C.Structure):
                 ("small_arg", C.c_double), ("unc_eps_rel", C.c_double),
                 ("unc_tau_abs", C.c_double), ("unc_tau_impact", C.c_double),
                 ("unc_tau_sel", C.c_double), ("unc_tau_val", C.c_double),
-                ("unc_tau_bsel", C.c_double), ("unc_eps_val", C.c_double)]
+                ("unc_eps_val", C.c_double)]
 
 
 class Stats(C.Structure):

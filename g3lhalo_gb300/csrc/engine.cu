@@ -198,15 +198,21 @@ __device__ void radix_select(const double *err, const unsigned long long *q, lon
     __syncthreads();
 }
 
+// pass 0 selects for every live integral; pass 1 (mixed precision) selects again, in
+// the same round, for the integrals pass 0 deferred, once the FP64 re-evaluation of
+// their ambiguous boundary regions has run.
 __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D,
                                                    IntState *__restrict__ S, Pool P, BatchHdr *H,
-                                                   double tau_sel, double tau_val)
+                                                   double tau_sel, double tau_val, int pass)
 {
     __shared__ SelShared sh;
     __shared__ int s_flag[4];  // fin, status, polish passes
     __shared__ double s_tot[2];
     const int n = H->n;
     for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        if (pass == 1 && !S[i].defer) continue;  // block-uniform
+        __syncthreads();
+        if (threadIdx.x == 0) S[i].defer = 0;
         if (S[i].done) {
             if (threadIdx.x == 0) S[i].K = 0;
             continue;
@@ -295,13 +301,13 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
                         const unsigned long long kb =
                             (unsigned long long)__double_as_longlong(P.key[base + j]);
                         if (kb >= pb && P.uval[base + j] > 0.f) {
-                            const int k = atomicAdd(&H->n_esc, 1);
-                            if (k < H->esc_cap) P.esc[k] = make_int2(i, j | (1 << 30));
+                            push_esc(H, P, d.kind * 3 + d.term - 1, i, j | (1 << 30));
                         }
                     }
                     if (threadIdx.x == 0) {
                         S[i].K = 0;
                         S[i].pad += 1;
+                        S[i].defer = 1;  // finish (or polish again) after the re-evaluation
                         atomicAdd(&H->polished, 1ull);
                     }
                 }
@@ -396,12 +402,12 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
                         const double e = P.err[base + j];
                         const float u = P.unc[base + j];
                         if (u > 0.f && e * (1.0 + u) >= blo && e * (1.0 - u) <= bhi) {
-                            const int k = atomicAdd(&H->n_esc, 1);
-                            if (k < H->esc_cap) P.esc[k] = make_int2(i, j | (1 << 30));
+                            push_esc(H, P, d.kind * 3 + d.term - 1, i, j | (1 << 30));
                         }
                     }
                     if (threadIdx.x == 0) {
                         S[i].K = 0;
+                        S[i].defer = 1;
                         atomicAdd(&H->deferred, 1ull);
                     }
                     __syncthreads();
@@ -435,9 +441,19 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
             run_tie += ntie;
             run_sel += nsel;
         }
+        // Mixed precision: selected parents whose split is flagged unsettled get it
+        // re-taken in FP64 before this round's cut.
+        if (H->mixed) {
+            __syncthreads();
+            for (int j = threadIdx.x; j < (int)K; j += SEL_BS) {
+                const int r = P.cand[base + j];
+                if (P.split[base + r] & 0x80) {
+                    push_esc(H, P, d.kind * 3 + d.term - 1, i, r);
+                }
+            }
+        }
         if (threadIdx.x == 0) {
             S[i].K = (int)K;
-            S[i].bsel = K == (unsigned long long)R ? 0.0 : __longlong_as_double((long long)bkey);
             S[i].neval = neval + twoNp * K;
             S[i].nR = R + (int)K;
             S[i].rounds += 1;
@@ -475,7 +491,9 @@ __global__ void __launch_bounds__(1024) k_scan(IntState *__restrict__ S, long lo
         woff[n] = tot;
         H->total_work = tot;
         // keep looping while there is work or a deferred FP64 re-evaluation
-        const int more = tot > 0 || H->n_esc > 0;
+        int pending = 0;
+        for (int g = 0; g < NGROUPS; ++g) pending |= H->n_esc[g];
+        const int more = tot > 0 || pending > 0;
         H->any_active = more;
         H->regions += 2ull * (unsigned long long)tot;
         if (more) H->rounds_done += 1;
@@ -506,7 +524,8 @@ __global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, 
         st.status = ST_OK;
         st.rounds = 0;
         st.pad = 0;
-        st.bsel = 0;
+        st.defer = 0;
+        st.pad2 = 0;
         S[i] = st;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -516,7 +535,7 @@ __global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, 
         H->rounds_done = 0;
         H->ties = 0;
         H->small_arg = 0;
-        H->n_esc = 0;
+        for (int g = 0; g < NGROUPS; ++g) H->n_esc[g] = 0;
         H->escalated = 0;
         H->deferred = 0;
         H->polished = 0;
@@ -526,9 +545,11 @@ __global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, 
 // end of a mixed-precision round: the FP64 re-evaluation queue has been consumed
 __global__ void k_round_end(BatchHdr *H)
 {
-    const int n = H->n_esc;
-    H->escalated += (unsigned long long)(n < H->esc_cap ? n : H->esc_cap);
-    H->n_esc = 0;
+    for (int g = 0; g < NGROUPS; ++g) {
+        const int n = H->n_esc[g];
+        H->escalated += (unsigned long long)(n < H->esc_cap[g] ? n : H->esc_cap[g]);
+        H->n_esc[g] = 0;
+    }
 }
 
 void *round_end_kernel() { return (void *)k_round_end; }

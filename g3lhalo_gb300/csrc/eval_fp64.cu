@@ -369,90 +369,232 @@ __global__ void __launch_bounds__(128) k_eval64(DevTables T, const IntDesc *__re
     }
 }
 
-// FP64 re-evaluation of the regions the mixed-precision pass escalated; each entry is
-// (integral, local slot | kind << 30): kind 0 = split decision only (the centre and
-// the 4 dim axis points enter the fourth differences, src/hcubature.cpp:527-575),
-// kind 1 = whole rule (value, error and split; for selection boundaries).  One
-// 256-thread block per region, one point per thread: few regions are escalated per
-// round, so latency rather than FP64 throughput decides the cost.
+static_assert(sizeof(Slot64) == reeval_slot_bytes, "re-evaluation scratch layout");
+
+// FP64 re-evaluation of the regions the mixed-precision pass queued for one group; each
+// entry is (integral, local slot | kind << 30): kind 0 = split decision only (the centre
+// and the 4 dim axis points enter the fourth differences, src/hcubature.cpp:527-575),
+// kind 1 = whole rule (value, error and split: ambiguous selection boundaries and the
+// final polish).  The FP64 pipe issues one warp instruction per 64 cycles per SM
+// sub-partition, so a round's re-evaluation time is set by the busiest sub-partition:
+// the work is spread evenly over the whole device in three passes over the first
+// P.rcap entries -- coordinate slots (one per thread), rule points (one per thread, each
+// entry's points padded to whole warps) and the sums (one thread per entry, in the
+// reference's order).  Entries beyond P.rcap take the batched kernel k_reeval64.
 template <int KIND, int TERM>
-__global__ void __launch_bounds__(256) k_reeval64(DevTables T, const IntDesc *__restrict__ D,
+struct Reeval {
+    static constexpr int DIM = TERM + 4;
+    static constexpr int NP = rule_points(DIM);
+    static constexpr int NAX = 1 + 4 * DIM;
+    static constexpr int NS = DIM * NVAR;
+    static constexpr int NPAD = (NP + 31) / 32 * 32;
+    static constexpr int G = KIND * 3 + TERM - 1;
+    __device__ static Slot64 *slots(const Pool &P)
+    {
+        return (Slot64 *)(P.rscr + (long long)G * P.rscr_group);
+    }
+    __device__ static double *vals(const Pool &P)
+    {
+        return (double *)(P.rscr + (long long)G * P.rscr_group +
+                          ((long long)P.rcap * MAX_DIM * NVAR * reeval_slot_bytes + 255) / 256 * 256);
+    }
+    __device__ static int count(const Pool &P, const BatchHdr *H)
+    {
+        const int cap = H->esc_cap[G];
+        const int n = H->n_esc[G] < cap ? H->n_esc[G] : cap;
+        return n < P.rcap ? n : P.rcap;
+    }
+};
+
+template <int KIND, int TERM>
+__global__ void __launch_bounds__(128) k_re_fill(DevTables T, const IntDesc *__restrict__ D,
+                                                 IntState *__restrict__ S, Pool P, BatchHdr *H,
+                                                 const long long *__restrict__ woff)
+{
+    using R = Reeval<KIND, TERM>;
+    const int m = R::count(P, H);
+    if (m == 0) return;
+    const int2 *Q = P.esc + H->esc_beg[R::G];
+    Slot64 *SL = R::slots(P);
+    const long long stride = P.stride;
+    const long long tot = (long long)m * R::NS;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t / R::NS), r = (int)(t - (long long)k * R::NS);
+        const int dim = r / NVAR, v = r - dim * NVAR;
+        const int2 ent = Q[k];
+        if (!(ent.y >> 30) && v >= 5) continue;  // split only: variants c, -+r2, -+r4
+        const IntDesc &d = D[ent.x];
+        const long long slot = d.base + (ent.y & 0x3FFFFFFF);
+        const double c = P.center[dim * stride + slot];
+        const double hw = ldexp(d.hw0[dim], -(int)P.level[dim * stride + slot]);
+        double x = c;
+        if (v > 0) {
+            double lam = (v <= 2) ? G3L_LAMBDA2 : (v <= 4 ? G3L_LAMBDA4 : G3L_LAMBDA5);
+            double rr = hw * lam;
+            x = (v & 1) ? c - rr : c + rr;
+        }
+        Model64<KIND, TERM>::fill(T, d, dim, x, SL[(long long)k * R::NS + r], &H->ties);
+    }
+}
+
+template <int KIND, int TERM>
+__global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *__restrict__ D,
+                                                   IntState *__restrict__ S, Pool P, BatchHdr *H,
+                                                   const long long *__restrict__ woff)
+{
+    using R = Reeval<KIND, TERM>;
+    constexpr int DIM = R::DIM;
+    __shared__ uint32_t sdesc[R::NP];
+    const int m = R::count(P, H);
+    if (m == 0) return;
+    for (int p = threadIdx.x; p < R::NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
+    __syncthreads();
+    const int2 *Q = P.esc + H->esc_beg[R::G];
+    const Slot64 *SL = R::slots(P);
+    double *VL = R::vals(P);
+    const long long tot = (long long)m * R::NPAD;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t / R::NPAD), p = (int)(t - (long long)k * R::NPAD);
+        const int2 ent = Q[k];
+        if (p >= ((ent.y >> 30) ? R::NP : R::NAX)) continue;
+        const IntDesc &d = D[ent.x];
+        const uint32_t vv = sdesc[p];
+        const Slot64 *base = SL + (long long)k * R::NS;
+        const Slot64 *sp[DIM];
+#pragma unroll
+        for (int dd = 0; dd < DIM; ++dd) sp[dd] = base + dd * NVAR + ((vv >> (3 * dd)) & 7);
+        VL[(long long)k * R::NPAD + p] = Model64<KIND, TERM>::point(T, d, sp);
+    }
+}
+
+// the sums of one re-evaluated region (vl: its rule-point values)
+template <int DIM>
+__device__ void reeval_finish(const IntDesc &d, const Pool &P, long long slot, bool full,
+                              const double *vl)
+{
+    const long long stride = P.stride;
+    if (full) {
+        int lsum = 0;
+        for (int q = 0; q < DIM; ++q) lsum += P.level[q * stride + slot];
+        double val, err;
+        int split;
+        combine64<DIM>(vl, ldexp(d.rootvol, -lsum), val, err, split);
+        P.val[slot] = val;
+        P.err[slot] = err;
+        P.split[slot] = (unsigned char)split;
+        P.unc[slot] = 0.f;
+        P.uval[slot] = 0.f;
+    } else {
+        const double ratio = (G3L_LAMBDA2 * G3L_LAMBDA2) / (G3L_LAMBDA4 * G3L_LAMBDA4);
+        const double val0 = vl[0];
+        double maxdiff = 0;
+        int dimDiffMax = 0;
+        for (int q = 0; q < DIM; ++q) {
+            double v0 = vl[1 + 4 * q], v1 = vl[2 + 4 * q];
+            double v2 = vl[3 + 4 * q], v3 = vl[4 + 4 * q];
+            double diff = 0;
+            diff += fabs(v0 + v1 - 2 * val0 - ratio * (v2 + v3 - 2 * val0));
+            if (diff > maxdiff) {
+                maxdiff = diff;
+                dimDiffMax = q;
+            }
+        }
+        P.split[slot] = (unsigned char)dimDiffMax;
+    }
+}
+
+template <int KIND, int TERM>
+__global__ void __launch_bounds__(128) k_re_combine(DevTables T, const IntDesc *__restrict__ D,
+                                                    IntState *__restrict__ S, Pool P, BatchHdr *H,
+                                                    const long long *__restrict__ woff)
+{
+    using R = Reeval<KIND, TERM>;
+    const int m = R::count(P, H);
+    const int2 *Q = P.esc + H->esc_beg[R::G];
+    const double *VL = R::vals(P);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+        const int2 ent = Q[k];
+        const IntDesc &d = D[ent.x];
+        reeval_finish<R::DIM>(d, P, d.base + (ent.y & 0x3FFFFFFF), (ent.y >> 30) != 0,
+                              VL + (long long)k * R::NPAD);
+    }
+}
+
+// Entries beyond P.rcap: a block takes a batch of RB entries and spreads their slots and
+// points over its threads (shared-memory staging, no scratch).
+template <int KIND, int TERM>
+__global__ void __launch_bounds__(128) k_reeval64(DevTables T, const IntDesc *__restrict__ D,
                                                   IntState *__restrict__ S, Pool P, BatchHdr *H,
                                                   const long long *__restrict__ woff)
 {
     constexpr int DIM = TERM + 4;
     constexpr int NP = rule_points(DIM);
     constexpr int NAX = 1 + 4 * DIM;
+    constexpr int RB = 4;  // entries per batch
+    constexpr int NS = DIM * NVAR;
     __shared__ uint32_t sdesc[NP];
-    __shared__ Slot64 slots[DIM * NVAR];
-    __shared__ double vals[NP];
-    const int n = H->n_esc;
-    if (n == 0) return;
-    for (int p = threadIdx.x; p < NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
-    __syncthreads();
+    __shared__ Slot64 slots[RB][NS];
+    __shared__ double vals[RB][NP];
+    __shared__ int2 sent[RB];
     const int g = KIND * 3 + TERM - 1;
-    const int nmax = n < H->esc_cap ? n : H->esc_cap;
+    const int cap = H->esc_cap[g];
+    const int n = H->n_esc[g] < cap ? H->n_esc[g] : cap;
+    const int first = P.rcap;
+    if (n <= first) return;
+    for (int p = threadIdx.x; p < NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
+    const int2 *Q = P.esc + H->esc_beg[g];
     const long long stride = P.stride;
-    for (int e = blockIdx.x; e < nmax; e += gridDim.x) {
-        const int2 ent = P.esc[e];
-        const IntDesc &d = D[ent.x];
-        if (d.kind * 3 + d.term - 1 != g) continue;
-        const long long slot = d.base + (ent.y & 0x3FFFFFFF);
-        const bool full = (ent.y >> 30) != 0;
-        const int nv = full ? NVAR : 5;  // split only: variants c, -+r2, -+r4
-        for (int t = threadIdx.x; t < DIM * nv; t += blockDim.x) {
-            const int dim = t / nv, v = t - dim * nv;
+    const int nb = (n - first + RB - 1) / RB;
+    for (int b = blockIdx.x; b < nb; b += gridDim.x) {
+        const int e0 = first + b * RB;
+        const int ne = n - e0 < RB ? n - e0 : RB;
+        __syncthreads();
+        if (threadIdx.x < ne) sent[threadIdx.x] = Q[e0 + threadIdx.x];
+        __syncthreads();
+        for (int t = threadIdx.x; t < ne * NS; t += blockDim.x) {
+            const int k = t / NS, r = t - k * NS;
+            const int dim = r / NVAR, v = r - dim * NVAR;
+            const int2 ent = sent[k];
+            if (!(ent.y >> 30) && v >= 5) continue;
+            const IntDesc &d = D[ent.x];
+            const long long slot = d.base + (ent.y & 0x3FFFFFFF);
             const double c = P.center[dim * stride + slot];
             const double hw = ldexp(d.hw0[dim], -(int)P.level[dim * stride + slot]);
             double x = c;
             if (v > 0) {
                 double lam = (v <= 2) ? G3L_LAMBDA2 : (v <= 4 ? G3L_LAMBDA4 : G3L_LAMBDA5);
-                double r = hw * lam;
-                x = (v & 1) ? c - r : c + r;
+                double rr = hw * lam;
+                x = (v & 1) ? c - rr : c + rr;
             }
-            Model64<KIND, TERM>::fill(T, d, dim, x, slots[dim * NVAR + v], &H->ties);
+            Model64<KIND, TERM>::fill(T, d, dim, x, slots[k][r], &H->ties);
         }
         __syncthreads();
-        const int np = full ? NP : NAX;
-        for (int p = threadIdx.x; p < np; p += blockDim.x) {
+        int pb[RB + 1];
+        pb[0] = 0;
+#pragma unroll
+        for (int k = 0; k < RB; ++k)
+            pb[k + 1] = pb[k] + (k < ne ? ((sent[k].y >> 30) ? NP : NAX) : 0);
+        for (int t = threadIdx.x; t < pb[RB]; t += blockDim.x) {
+            int k = 0;
+#pragma unroll
+            for (int q = 1; q < RB; ++q) k += t >= pb[q] ? 1 : 0;
+            const int p = t - pb[k];
+            const IntDesc &d = D[sent[k].x];
             const uint32_t vv = sdesc[p];
             const Slot64 *sp[DIM];
 #pragma unroll
-            for (int dd = 0; dd < DIM; ++dd) sp[dd] = &slots[dd * NVAR + ((vv >> (3 * dd)) & 7)];
-            vals[p] = Model64<KIND, TERM>::point(T, d, sp);
+            for (int dd = 0; dd < DIM; ++dd) sp[dd] = &slots[k][dd * NVAR + ((vv >> (3 * dd)) & 7)];
+            vals[k][p] = Model64<KIND, TERM>::point(T, d, sp);
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            if (full) {
-                int lsum = 0;
-                for (int k = 0; k < DIM; ++k) lsum += P.level[k * stride + slot];
-                double val, err;
-                int split;
-                combine64<DIM>(vals, ldexp(d.rootvol, -lsum), val, err, split);
-                P.val[slot] = val;
-                P.err[slot] = err;
-                P.split[slot] = (unsigned char)split;
-                P.unc[slot] = 0.f;
-                P.uval[slot] = 0.f;
-            } else {
-                const double ratio = (G3L_LAMBDA2 * G3L_LAMBDA2) / (G3L_LAMBDA4 * G3L_LAMBDA4);
-                const double val0 = vals[0];
-                double maxdiff = 0;
-                int dimDiffMax = 0;
-                for (int k = 0; k < DIM; ++k) {
-                    double v0 = vals[1 + 4 * k], v1 = vals[2 + 4 * k];
-                    double v2 = vals[3 + 4 * k], v3 = vals[4 + 4 * k];
-                    double diff = 0;
-                    diff += fabs(v0 + v1 - 2 * val0 - ratio * (v2 + v3 - 2 * val0));
-                    if (diff > maxdiff) {
-                        maxdiff = diff;
-                        dimDiffMax = k;
-                    }
-                }
-                P.split[slot] = (unsigned char)dimDiffMax;
-            }
+        if (threadIdx.x < ne) {
+            const int2 ent = sent[threadIdx.x];
+            const IntDesc &d = D[ent.x];
+            reeval_finish<DIM>(d, P, d.base + (ent.y & 0x3FFFFFFF), (ent.y >> 30) != 0,
+                               vals[threadIdx.x]);
         }
-        __syncthreads();
     }
 }
 
@@ -460,13 +602,31 @@ __global__ void __launch_bounds__(256) k_reeval64(DevTables T, const IntDesc *__
     template __global__ void k_eval64<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,      \
                                              BatchHdr *, const long long *);                     \
     template __global__ void k_reeval64<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,    \
-                                               BatchHdr *, const long long *);
+                                               BatchHdr *, const long long *);                   \
+    template __global__ void k_re_fill<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,     \
+                                              BatchHdr *, const long long *);                    \
+    template __global__ void k_re_points<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,   \
+                                                BatchHdr *, const long long *);                  \
+    template __global__ void k_re_combine<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,  \
+                                                 BatchHdr *, const long long *);
 G3L_INST64(0, 1)
 G3L_INST64(0, 2)
 G3L_INST64(0, 3)
 G3L_INST64(1, 1)
 G3L_INST64(1, 2)
 G3L_INST64(1, 3)
+
+// re-evaluation kernels of a group: 0 = fill, 1 = points, 2 = combine, 3 = batched tail
+void *reeval_phase_kernel(int kind, int term, int phase)
+{
+#define G3L_RE_ROW(K, Tm)                                                                       \
+    {(void *)k_re_fill<K, Tm>, (void *)k_re_points<K, Tm>, (void *)k_re_combine<K, Tm>,          \
+     (void *)k_reeval64<K, Tm>}
+    static void *tab[2][3][4] = {{G3L_RE_ROW(0, 1), G3L_RE_ROW(0, 2), G3L_RE_ROW(0, 3)},
+                                 {G3L_RE_ROW(1, 1), G3L_RE_ROW(1, 2), G3L_RE_ROW(1, 3)}};
+#undef G3L_RE_ROW
+    return tab[kind][term - 1][phase];
+}
 
 void *reeval64_kernel(int kind, int term)
 {

@@ -624,7 +624,7 @@ __device__ __forceinline__ df hw_sum(df a)
 // only if its region could move the integral by more than T.tau_impact of it.
 
 template <int KIND, int TERM>
-__device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, double Vcur, double Bcur,
+__device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, double Vcur,
                            const Pool &P, BatchHdr *H, long long pslot, long long qslot, bool cut,
                            SlotF *slots, float *vals, Child &C, const uint32_t *sdesc,
                            unsigned &ties, int &small)
@@ -635,7 +635,7 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
     using W = RuleW<DIM>;
     const int lane = threadIdx.x & 31;
     const long long stride = P.stride;
-    const int sdim = cut ? P.split[pslot] : 0;
+    const int sdim = cut ? (P.split[pslot] & 0x7F) : 0;
     const int nchild = cut ? 2 : 1;
     // parent geometry -> child centres (FP64: one add per child)
     double c_l = 0;
@@ -804,19 +804,14 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
         const long long slot = hh == 0 ? pslot : qslot;
         if (hl == 0) {
             P.val[slot] = out;
-            P.split[slot] = (unsigned char)sidx;
             P.uval[slot] = uvrel;
         } else {
             P.err[slot] = out;
             P.unc[slot] = urel;
-            // an uncertain split of a region that matters: re-evaluate in FP64.  A region
-            // matters if its error is a visible part of the integral, or if it can reach
-            // the selection boundary (Bcur = 0 while every region is still being cut).
-            if (!split_sure && (out > T.tau_impact * fabs(Vcur) ||
-                                (T.tau_bsel > 0.0 && out > T.tau_bsel * Bcur))) {
-                const int k = atomicAdd(&H->n_esc, 1);
-                if (k < H->esc_cap) P.esc[k] = make_int2(iint, (int)(slot - d.base));
-            }
+            // An unsettled split is flagged (bit 7); the selection kernel has it re-taken
+            // in FP64 only if the region is selected for cutting, so leaves never pay.
+            const bool flag = !split_sure && out > T.tau_impact * fabs(Vcur);
+            P.split[slot] = (unsigned char)(sidx | (flag ? 0x80 : 0));
         }
     }
     // child geometry
@@ -866,7 +861,7 @@ __global__ void __launch_bounds__(128) k_evalmx(DevTables T, const IntDesc *__re
         const bool cut = cj >= 0;
         const long long pslot = d.base + (cut ? cj : 0);
         const long long qslot = cut ? d.base + (S[i].nR - S[i].K) + j : -1;
-        warp_itemF<KIND, TERM>(T, d, i, S[i].val, S[i].bsel, P, H, pslot, qslot, cut, sslot[wib],
+        warp_itemF<KIND, TERM>(T, d, i, S[i].val, P, H, pslot, qslot, cut, sslot[wib],
                                svals[wib], schild[wib], sdesc, ties, small);
     }
     // warp-aggregated diagnostics

@@ -8,7 +8,8 @@
 //                              (compute_vol / cut_region, src/hcubature.cpp:134-141,
 //                              206-218: halving and products scale exactly by 2)
 //   val, err                   FP64 rule value and error of the region
-//   split                      dimension to bisect next (src/hcubature.cpp:565-575)
+//   split                      dimension to bisect next (src/hcubature.cpp:565-575); in the
+//                              mixed pass bit 7 flags a split the FP32 values did not settle
 // Integral i owns slots [base_i, base_i + cap_i); its live regions are the first nR_i.
 #pragma once
 #include <cstdint>
@@ -65,7 +66,6 @@ struct DevTables {
     float unc_eps, unc_abs;        // FP32 point-value error bound (decisions)
     float unc_val_ratio;           // value-noise bound / decision bound
     double tau_impact, tau_sel;    // escalation thresholds (fraction of the integral)
-    double tau_bsel;               // split escalation threshold (fraction of the last boundary)
     double tau_val;                // bound on the FP32 noise left in a finished integral
     const unsigned long long *tie_z_bits;
     const int *tie_z_round, *tie_z_trunc;
@@ -93,8 +93,8 @@ struct IntDesc {
 struct IntState {
     double val, err;
     unsigned long long neval;
-    int nR, K, done, status, rounds, pad;
-    double bsel;  // error at the last selection boundary (0 while every region is cut)
+    int nR, K, done, status, rounds, pad;  // pad: FP64 polish passes so far
+    int defer, pad2;                       // defer: selection deferred in this round's first pass
 };
 
 struct Pool {
@@ -109,7 +109,20 @@ struct Pool {
     double *key;            // selection scratch (polish keys |val| * uval)
     int2 *esc;              // regions queued for FP64 re-evaluation: (integral, local slot)
     long long stride;
+    // FP64 re-evaluation scratch: per group, coordinate slots and rule-point values of the
+    // first rcap queued entries of a round (later entries take the batched kernel)
+    unsigned char *rscr;
+    long long rscr_group;   // bytes per group
+    int rcap;
 };
+
+// Bytes of re-evaluation scratch per group for rcap entries (any term).
+constexpr long long reeval_slot_bytes = 56;  // sizeof(Slot64)
+__host__ __device__ constexpr long long reeval_scratch_group_bytes(int rcap)
+{
+    return ((long long)rcap * MAX_DIM * NVAR * reeval_slot_bytes + 255) / 256 * 256 +
+           (long long)rcap * 256 * 8;
+}
 
 // Per-call header kept in device memory so one instantiated graph serves any batch.
 struct BatchHdr {
@@ -125,12 +138,22 @@ struct BatchHdr {
     unsigned long long regions;
     int rounds_done;
     int mixed;                   // 1: mixed-precision pass (uncertainty bookkeeping on)
-    int n_esc, esc_cap;          // FP64 re-evaluation queue fill / capacity
+    int n_esc[NGROUPS];          // FP64 re-evaluation queue of each group: fill,
+    int esc_cap[NGROUPS];        //   capacity (the group's pool slots)
+    long long esc_beg[NGROUPS];  //   and first entry in Pool::esc
     unsigned long long escalated;// statistics: regions re-evaluated in FP64
     unsigned long long deferred; // statistics: selections deferred for re-evaluation
     unsigned long long polished; // statistics: finished integrals polished in FP64
     double *dbg;                 // debug: per-point integrand values of one work item
 };
+
+// Queue region `code` (local slot | whole-rule flag << 30) of integral i, group g, for
+// FP64 re-evaluation in this round.
+__device__ inline void push_esc(BatchHdr *H, const Pool &P, int g, int i, int code)
+{
+    const int k = atomicAdd(&H->n_esc[g], 1);
+    if (k < H->esc_cap[g]) P.esc[H->esc_beg[g] + k] = make_int2(i, code);
+}
 
 // Point p of a dim-dimensional Genz-Malik rule -> coordinate variant of dim d,
 // in the reference's generation order (src/hcubature.cpp:343-414, 476-503):

@@ -24,6 +24,7 @@
 namespace g3l {
 void *eval64_kernel(int kind, int term);
 void *reeval64_kernel(int kind, int term);
+void *reeval_phase_kernel(int kind, int term, int phase);
 void *round_end_kernel();
 void *evalmx_kernel(int kind, int term);
 void *select_kernel();
@@ -59,6 +60,10 @@ int dalloc(T **p, size_t n)
     }
     return G3L_OK;
 }
+
+// FP64 re-evaluation entries per group and round that take the device-wide passes
+// (scratch ~39 MB per group); further entries take the batched kernel.
+constexpr int kReevalCap = 8192;
 
 struct Workspace {
     size_t pool_cap = 0;
@@ -209,7 +214,6 @@ int prepare_mixed(g3l_ctx *c, const g3l_tables *t)
     T.tau_impact = c->opt.unc_tau_impact;
     T.tau_sel = c->opt.unc_tau_sel;
     T.tau_val = c->opt.unc_tau_val;
-    T.tau_bsel = c->opt.unc_tau_bsel;
     T.unc_val_ratio = (float)(c->opt.unc_eps_val / c->opt.unc_eps_rel);
     st |= dalloc(&c->d_fnbar, (size_t)MAX_HOD_SLOTS * Nz);
     st |= dalloc(&c->d_fhodp, (size_t)MAX_HOD_SLOTS * 8);
@@ -263,7 +267,7 @@ int ensure_workspace(g3l_ctx *c, int n, size_t pool)
     if (n > W.n_cap) ncap = std::max(ncap, (int)(n * 1.25) + 16);
     if (pool > W.pool_cap) pcap = std::max(pcap, (size_t)(pool * 1.25) + 1024);
     void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.q, W.P.cand,
-                    W.P.unc,    W.P.esc,   W.P.uval, W.P.key, W.D,  W.S,  W.woff, W.H};
+                    W.P.unc,    W.P.esc,   W.P.uval, W.P.key, W.P.rscr, W.D, W.S, W.woff, W.H};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     W = Workspace{W.pool_cap, W.n_cap, Pool{}, nullptr, nullptr, nullptr, nullptr, W.gen};
@@ -281,6 +285,9 @@ int ensure_workspace(g3l_ctx *c, int n, size_t pool)
     st |= dalloc(&W.P.uval, pcap);
     st |= dalloc(&W.P.key, pcap);
     st |= dalloc(&W.P.esc, pcap);
+    W.P.rcap = kReevalCap;
+    W.P.rscr_group = reeval_scratch_group_bytes(kReevalCap);
+    st |= dalloc(&W.P.rscr, (size_t)(NGROUPS * W.P.rscr_group));
     st |= dalloc(&W.D, (size_t)ncap);
     st |= dalloc(&W.S, (size_t)ncap);
     st |= dalloc(&W.woff, (size_t)ncap + 1);
@@ -312,10 +319,17 @@ int eval_grid(g3l_ctx *c, void *fn)
     return nb * c->nsm;
 }
 
+int grid128(g3l_ctx *c, void *fn)
+{
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, 0) != cudaSuccess || nb < 1) nb = 1;
+    return nb * c->nsm;
+}
+
 int reeval_grid(g3l_ctx *c, void *fn)
 {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 256, 0) != cudaSuccess || nb < 1) nb = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 128, 0) != cudaSuccess || nb < 1) nb = 1;
     return nb * c->nsm;
 }
 
@@ -330,6 +344,7 @@ struct KernelArgs {
     int use_cond;
     double tau_sel;
     double tau_val;
+    int pass0 = 0, pass1 = 1;
 };
 
 int add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *deps, size_t ndeps,
@@ -343,6 +358,20 @@ int add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *deps
     kp.kernelParams = args;
     G3L_CK(cudaGraphAddKernelNode(node, g, deps, ndeps, &kp));
     return G3L_OK;
+}
+
+// FP64 re-evaluation queues: group g gets as many entries as its integrals have pool
+// slots (a region is queued at most once per round), laid out group after group.
+void set_esc_queues(const IntDesc *D, int n, BatchHdr &H)
+{
+    long long cnt[NGROUPS] = {};
+    for (int r = 0; r < n; ++r) cnt[D[r].kind * 3 + D[r].term - 1] += D[r].cap;
+    long long beg = 0;
+    for (int g = 0; g < NGROUPS; ++g) {
+        H.esc_beg[g] = beg;
+        H.esc_cap[g] = (int)std::min<long long>(cnt[g], 0x7fffffff);
+        beg += cnt[g];
+    }
 }
 
 int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
@@ -367,17 +396,63 @@ int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
     G3L_CK(cudaGraphAddNode(&n_while, g, &n_init, nullptr, 1, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     cudaGraphNode_t n_sel, n_scan, prev;
+    // mixed: FP64 re-evaluations queued by a selection pass (unsettled splits of the
+    // parents about to be cut, ambiguous boundary regions, polish), then the round end
+    // (one branch per group, side by side: each group reads only its own queue)
+    auto add_reevals = [&](cudaGraphNode_t &dep) -> int {
+        cudaGraphNode_t br[2 * NGROUPS];
+        int nbr = 0;
+        for (int grp = 0; grp < NGROUPS; ++grp) {
+            if (!(gmask & (1 << grp))) continue;
+            void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
+            cudaGraphNode_t chain = dep;
+            for (int ph = 0; ph < 3; ++ph) {
+                void *fn = reeval_phase_kernel(grp / 3, grp % 3 + 1, ph);
+                cudaGraphNode_t nd;
+                int st = add_kernel(body, &nd, &chain, 1, fn, ph == 2 ? c->nsm : grid128(c, fn), 128,
+                                    args);
+                if (st) return st;
+                chain = nd;
+            }
+            br[nbr++] = chain;
+            void *fn = reeval_phase_kernel(grp / 3, grp % 3 + 1, 3);
+            int st = add_kernel(body, &br[nbr], &dep, 1, fn, reeval_grid(c, fn), 128, args);
+            if (st) return st;
+            ++nbr;
+        }
+        void *args[] = {&a.H};
+        cudaGraphNode_t n_end;
+        int st = add_kernel(body, &n_end, nbr ? br : &dep, nbr ? nbr : 1, round_end_kernel(), 1,
+                            1, args);
+        if (st) return st;
+        dep = n_end;
+        return G3L_OK;
+    };
     {
-        void *args[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val};
+        void *args[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val, &a.pass0};
         int st = add_kernel(body, &n_sel, nullptr, 0, select_kernel(), c->nsm * 8, 256, args);
         if (st) return st;
     }
+    prev = n_sel;
+    if (precision == G3L_MIXED) {
+        int st = add_reevals(prev);
+        if (st) return st;
+        void *args[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val, &a.pass1};
+        cudaGraphNode_t n_sel1;
+        st = add_kernel(body, &n_sel1, &prev, 1, select_kernel(), c->nsm * 8, 256, args);
+        if (st) return st;
+        prev = n_sel1;
+    }
     {
         void *args[] = {&a.S, &a.woff, &a.H, &a.handle, &a.use_cond};
-        int st = add_kernel(body, &n_scan, &n_sel, 1, scan_kernel(), 1, 1024, args);
+        int st = add_kernel(body, &n_scan, &prev, 1, scan_kernel(), 1, 1024, args);
         if (st) return st;
     }
     prev = n_scan;
+    if (precision == G3L_MIXED) {
+        int st = add_reevals(prev);
+        if (st) return st;
+    }
     for (int grp = 0; grp < NGROUPS; ++grp) {
         if (!(gmask & (1 << grp))) continue;
         void *fn = eval_fn(precision, grp);
@@ -386,21 +461,6 @@ int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
         int st = add_kernel(body, &n_ev, &prev, 1, fn, eval_grid(c, fn), 128, args);
         if (st) return st;
         prev = n_ev;
-    }
-    if (precision == G3L_MIXED) {
-        for (int grp = 0; grp < NGROUPS; ++grp) {
-            if (!(gmask & (1 << grp))) continue;
-            void *fn = reeval64_kernel(grp / 3, grp % 3 + 1);
-            void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
-            cudaGraphNode_t n_re;
-            int st = add_kernel(body, &n_re, &prev, 1, fn, reeval_grid(c, fn), 256, args);
-            if (st) return st;
-            prev = n_re;
-        }
-        void *args[] = {&a.H};
-        cudaGraphNode_t n_end;
-        int st = add_kernel(body, &n_end, &prev, 1, round_end_kernel(), 1, 1, args);
-        if (st) return st;
     }
     cudaGraphExec_t ex;
     G3L_CK(cudaGraphInstantiate(&ex, g, 0));
@@ -467,14 +527,58 @@ int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
     for (int g = 0; g < NGROUPS; ++g) c->stats.group_ms[g] = 0;
     c->stats.reeval_ms = 0;
     c->stats.select_ms = 0;
+    float ms;
+    auto reevals = [&]() -> int {
+        G3L_CK(cudaEventRecord(c->tev[12], s));
+        for (int grp = 0; grp < NGROUPS; ++grp) {
+            if (!(gmask & (1 << grp))) continue;
+            void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
+            for (int ph = 0; ph < 4; ++ph) {
+                void *fn = reeval_phase_kernel(grp / 3, grp % 3 + 1, ph);
+                const int grid = ph == 2 ? c->nsm : (ph == 3 ? reeval_grid(c, fn) : grid128(c, fn));
+                G3L_CK(cudaLaunchKernel(fn, dim3(grid), dim3(128), args, 0, s));
+                ++*launches;
+            }
+        }
+        G3L_CK(cudaEventRecord(c->tev[13], s));
+        void *eargs[] = {&a.H};
+        G3L_CK(cudaLaunchKernel(round_end_kernel(), dim3(1), dim3(1), eargs, 0, s));
+        ++*launches;
+        G3L_CK(cudaEventSynchronize(c->tev[13]));
+        cudaEventElapsedTime(&ms, c->tev[12], c->tev[13]);
+        c->stats.reeval_ms += ms;
+        return G3L_OK;
+    };
     for (int r = 0; r < c->opt.max_rounds + 4; ++r) {
-        void *sargs[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val};
+        void *sargs[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val, &a.pass0};
         G3L_CK(cudaEventRecord(c->tev[14], s));
         G3L_CK(cudaLaunchKernel(select_kernel(), dim3(c->nsm * 8), dim3(256), sargs, 0, s));
+        G3L_CK(cudaEventRecord(c->tev[15], s));
+        ++*launches;
+        G3L_CK(cudaEventSynchronize(c->tev[15]));
+        cudaEventElapsedTime(&ms, c->tev[14], c->tev[15]);
+        c->stats.select_ms += ms;
+        if (precision == G3L_MIXED) {
+            int st = reevals();
+            if (st) return st;
+            void *sargs1[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val, &a.pass1};
+            G3L_CK(cudaEventRecord(c->tev[14], s));
+            G3L_CK(cudaLaunchKernel(select_kernel(), dim3(c->nsm * 8), dim3(256), sargs1, 0, s));
+            ++*launches;
+        } else {
+            G3L_CK(cudaEventRecord(c->tev[14], s));
+        }
         void *cargs[] = {&a.S, &a.woff, &a.H, &a.handle, &a.use_cond};
         G3L_CK(cudaLaunchKernel(scan_kernel(), dim3(1), dim3(1024), cargs, 0, s));
         G3L_CK(cudaEventRecord(c->tev[15], s));
-        *launches += 2;
+        ++*launches;
+        G3L_CK(cudaEventSynchronize(c->tev[15]));
+        cudaEventElapsedTime(&ms, c->tev[14], c->tev[15]);
+        c->stats.select_ms += ms;
+        if (precision == G3L_MIXED) {
+            int st = reevals();
+            if (st) return st;
+        }
         for (int grp = 0; grp < NGROUPS; ++grp) {
             if (!(gmask & (1 << grp))) continue;
             void *fn = eval_fn(precision, grp);
@@ -484,35 +588,14 @@ int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
             G3L_CK(cudaEventRecord(c->tev[2 * grp + 1], s));
             ++*launches;
         }
-        if (precision == G3L_MIXED) {
-            G3L_CK(cudaEventRecord(c->tev[12], s));
-            for (int grp = 0; grp < NGROUPS; ++grp) {
-                if (!(gmask & (1 << grp))) continue;
-                void *fn = reeval64_kernel(grp / 3, grp % 3 + 1);
-                void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
-                G3L_CK(cudaLaunchKernel(fn, dim3(reeval_grid(c, fn)), dim3(256), args, 0, s));
-                ++*launches;
-            }
-            G3L_CK(cudaEventRecord(c->tev[13], s));
-            void *eargs[] = {&a.H};
-            G3L_CK(cudaLaunchKernel(round_end_kernel(), dim3(1), dim3(1), eargs, 0, s));
-            ++*launches;
-        }
         G3L_CK(cudaMemcpyAsync(c->h_pinned, &W.H->any_active, sizeof(int),
                                cudaMemcpyDeviceToHost, s));
         G3L_CK(cudaStreamSynchronize(s));
-        float ms;
         for (int grp = 0; grp < NGROUPS; ++grp)
             if (gmask & (1 << grp)) {
                 cudaEventElapsedTime(&ms, c->tev[2 * grp], c->tev[2 * grp + 1]);
                 c->stats.group_ms[grp] += ms;
             }
-        if (precision == G3L_MIXED) {
-            cudaEventElapsedTime(&ms, c->tev[12], c->tev[13]);
-            c->stats.reeval_ms += ms;
-        }
-        cudaEventElapsedTime(&ms, c->tev[14], c->tev[15]);
-        c->stats.select_ms += ms;
         if (*(int *)c->h_pinned == 0) break;
     }
     return G3L_OK;
@@ -607,7 +690,6 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
     c->opt.unc_tau_impact = 0.0;
     c->opt.unc_tau_sel = 1e-7;
     c->opt.unc_tau_val = 5e-5;
-    c->opt.unc_tau_bsel = 0.0;
     c->opt.unc_eps_val = 5e-6;
 
     DevTables &T = c->T;
@@ -681,7 +763,7 @@ void g3l_ctx_destroy(g3l_ctx *c)
     }
     Workspace &W = c->W;
     void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.q, W.P.cand,
-                    W.P.unc,    W.P.esc,   W.P.uval, W.P.key, W.D,  W.S,  W.woff, W.H};
+                    W.P.unc,    W.P.esc,   W.P.uval, W.P.key, W.P.rscr, W.D, W.S, W.woff, W.H};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (void *p : c->allocs) cudaFree(p);
@@ -789,7 +871,6 @@ int g3l_set_options(g3l_ctx *c, const g3l_options *o)
     c->T.tau_impact = o->unc_tau_impact;
     c->T.tau_sel = o->unc_tau_sel;
     c->T.tau_val = o->unc_tau_val;
-    c->T.tau_bsel = o->unc_tau_bsel;
     c->T.unc_val_ratio = (float)(o->unc_eps_val / o->unc_eps_rel);
     for (auto &g : c->graphs) {
         cudaGraphExecDestroy(g.exec);
@@ -866,7 +947,7 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
     int st = ensure_workspace(c, n, (size_t)base);
     if (st) return st;
     Workspace &W = c->W;
-    H.esc_cap = (int)std::min<size_t>(W.pool_cap, 0x7fffffff);
+    set_esc_queues(D.data(), n, H);
     H.dbg = nullptr;
     // stage through pinned host memory: descriptors + header in, states + header out
     const size_t in_bytes = sizeof(IntDesc) * n + sizeof(BatchHdr);
@@ -936,7 +1017,9 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
     sx.kernel_launches = launches >= 0 ? (uint64_t)launches
                                        : (uint64_t)(1 + (Hout.rounds_done + 1) *
                                                            (2 + ngroups +
-                                                            (precision == G3L_MIXED ? ngroups + 1 : 0)));
+                                                            (precision == G3L_MIXED
+                                                                 ? 2 * (ngroups + 1) + 1
+                                                                 : 0)));
     sx.regions_evaluated = Hout.regions;
     sx.tie_fallbacks = Hout.ties;
     sx.small_arg_fp64 = Hout.small_arg;
@@ -1005,7 +1088,7 @@ int g3l_debug_pool(g3l_ctx *c, int index, int max_regions, double *centers, int 
     G3L_CK(cudaMemcpy(err, W.P.err + d.base, nR * sizeof(double), cudaMemcpyDeviceToHost));
     G3L_CK(cudaMemcpy(b.data(), W.P.split + d.base, nR, cudaMemcpyDeviceToHost));
     for (int j = 0; j < nR; ++j) {
-        split[j] = b[j];
+        split[j] = b[j] & 0x7F;
         val[j] *= d.scale;
         err[j] *= d.scale;
     }
@@ -1046,7 +1129,7 @@ int g3l_debug_region(g3l_ctx *c, const g3l_integral *item, const double *center,
     for (int g = 0; g <= NGROUPS; ++g) H.gbeg[g] = g <= grp ? 0 : 1;
     H.max_rounds = 1;
     H.mixed = precision == G3L_MIXED;
-    H.esc_cap = 2;
+    H.esc_cap[grp] = 2;
     H.dbg = dbg;
     IntState S{};
     S.nR = 1;
@@ -1093,7 +1176,7 @@ int g3l_debug_region(g3l_ctx *c, const g3l_integral *item, const double *center,
         }
         out[0] = vv[0];
         out[1] = vv[1];
-        out[2] = sp;
+        out[2] = sp & 0x7F;
     } while (0);
     if (rc) host::set_error(std::string("g3l_debug_region: ") + cudaGetErrorString(cudaGetLastError()));
     cudaFree(dbg);
@@ -1153,6 +1236,7 @@ namespace {
 constexpr size_t kStaticScratchBytes = 64ull << 20;  // 64 MiB per device
 constexpr int kStaticMaxItems = 1024;
 constexpr int kStaticMaxDevices = 64;
+constexpr int kStaticReevalCap = 512;  // re-evaluation entries per group and round (device-wide passes)
 
 static __device__ __align__(256) unsigned char g3l_static_scratch[kStaticScratchBytes];
 
@@ -1169,7 +1253,7 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // Bytes of scratch a call with n integrals and `pool` region slots needs, and the
 // offsets of its arrays (same arrays as the context workspace).
 struct StaticLayout {
-    size_t H, D, S, woff, center, level, val, err, split, q, cand, unc, uval, key, esc, end;
+    size_t H, D, S, woff, center, level, val, err, split, q, cand, unc, uval, key, esc, rscr, end;
 };
 
 StaticLayout static_layout(int n, size_t pool)
@@ -1191,6 +1275,7 @@ StaticLayout static_layout(int n, size_t pool)
     L.uval = o;   o = align256(o + sizeof(float) * pool);
     L.key = o;    o = align256(o + sizeof(double) * pool);
     L.esc = o;    o = align256(o + sizeof(int2) * pool);
+    L.rscr = o;   o = align256(o + (size_t)(NGROUPS * reeval_scratch_group_bytes(kStaticReevalCap)));
     L.end = o;
     return L;
 }
@@ -1287,7 +1372,7 @@ extern "C" int g3l_eval_static(g3l_ctx *c, const g3l_integral *items, int n, int
     H.gbeg[NGROUPS] = n;
     H.max_rounds = c->opt.max_rounds;
     H.mixed = precision == G3L_MIXED ? 1 : 0;
-    H.esc_cap = (int)std::min<size_t>(pool, 0x7fffffff);
+    set_esc_queues(g_st_desc, n, H);
     H.dbg = nullptr;
 
     G3L_CK(cudaSetDevice(c->device));
@@ -1311,6 +1396,9 @@ extern "C" int g3l_eval_static(g3l_ctx *c, const g3l_integral *items, int n, int
     a.P.uval = (float *)(base + L.uval);
     a.P.key = (double *)(base + L.key);
     a.P.esc = (int2 *)(base + L.esc);
+    a.P.rscr = base + L.rscr;
+    a.P.rcap = kStaticReevalCap;
+    a.P.rscr_group = reeval_scratch_group_bytes(kStaticReevalCap);
     a.P.stride = (long long)pool;
     a.handle = 0;
     a.use_cond = 0;
@@ -1328,29 +1416,42 @@ extern "C" int g3l_eval_static(g3l_ctx *c, const g3l_integral *items, int n, int
         ++launches;
     }
     int active = 1;
+    auto reevals = [&]() -> int {
+        for (int g = 0; g < NGROUPS; ++g) {
+            if (!(gmask & (1 << g))) continue;
+            void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
+            for (int ph = 0; ph < 4; ++ph) {
+                void *fn = reeval_phase_kernel(g / 3, g % 3 + 1, ph);
+                const int grid = ph == 2 ? c->nsm : (ph == 3 ? reeval_grid(c, fn) : grid128(c, fn));
+                G3L_CK(cudaLaunchKernel(fn, dim3(grid), dim3(128), args, 0, s));
+                ++launches;
+            }
+        }
+        void *eargs[] = {&a.H};
+        G3L_CK(cudaLaunchKernel(round_end_kernel(), dim3(1), dim3(1), eargs, 0, s));
+        ++launches;
+        return G3L_OK;
+    };
     for (int r = 0; r < c->opt.max_rounds + 4 && active; ++r) {
-        void *sargs[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val};
+        void *sargs[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val, &a.pass0};
         G3L_CK(cudaLaunchKernel(select_kernel(), dim3(c->nsm * 8), dim3(256), sargs, 0, s));
+        ++launches;
+        if (precision == G3L_MIXED) {
+            if ((st = reevals())) return st;
+            void *sargs1[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val, &a.pass1};
+            G3L_CK(cudaLaunchKernel(select_kernel(), dim3(c->nsm * 8), dim3(256), sargs1, 0, s));
+            ++launches;
+        }
         void *cargs[] = {&a.S, &a.woff, &a.H, &a.handle, &a.use_cond};
         G3L_CK(cudaLaunchKernel(scan_kernel(), dim3(1), dim3(1024), cargs, 0, s));
-        launches += 2;
+        ++launches;
+        if (precision == G3L_MIXED)
+            if ((st = reevals())) return st;
         for (int g = 0; g < NGROUPS; ++g) {
             if (!(gmask & (1 << g))) continue;
             void *fn = eval_fn(precision, g);
             void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
             G3L_CK(cudaLaunchKernel(fn, dim3(eval_grid(c, fn)), dim3(128), args, 0, s));
-            ++launches;
-        }
-        if (precision == G3L_MIXED) {
-            for (int g = 0; g < NGROUPS; ++g) {
-                if (!(gmask & (1 << g))) continue;
-                void *fn = reeval64_kernel(g / 3, g % 3 + 1);
-                void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
-                G3L_CK(cudaLaunchKernel(fn, dim3(reeval_grid(c, fn)), dim3(256), args, 0, s));
-                ++launches;
-            }
-            void *eargs[] = {&a.H};
-            G3L_CK(cudaLaunchKernel(round_end_kernel(), dim3(1), dim3(1), eargs, 0, s));
             ++launches;
         }
         G3L_CK(cudaMemcpyAsync(&active, &a.H->any_active, sizeof(int), cudaMemcpyDeviceToHost, s));

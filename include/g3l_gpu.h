@@ -145,10 +145,6 @@ typedef struct g3l_options {
      * unc_tau_val |value| has its largest-bound regions re-evaluated in FP64, at
      * most twice (default 5e-5; 0 = off). */
     double unc_tau_val;
-    /* An unsettled split is also re-evaluated when the region's error exceeds
-     * unc_tau_bsel times the error at the integral's last selection boundary, or
-     * in any round that cuts every region (default 0 = off). */
-    double unc_tau_bsel;
     /* Relative bound on the FP32 error of one point value used for the value-noise
      * estimate of unc_tau_val (decisions use unc_eps_rel; default 5e-6). */
     double unc_eps_val;
@@ -196,10 +192,10 @@ int g3l_debug_region(g3l_ctx *ctx, const g3l_integral *item, const double *cente
  * allocator, or a loop that cannot take an allocation's implicit synchronisation.
  *  - Scratch: one fixed 64 MiB device array per device, built into the library.  A
  *    call may hold at most 1024 integrals and as many region slots as fit beside them
- *    (about 116 bytes per slot; each integral takes 3 + (max_eval + P) / (2 P) slots
- *    for its P-point rule, so ~550k slots, e.g. 260 seven-dimensional integrals at
- *    max_eval = 1e6).  Larger calls fail with G3L_ERR_INVALID and a message stating
- *    the bytes needed; nothing is evaluated.
+ *    and the 15 MB of re-evaluation scratch (about 116 bytes per slot; each integral
+ *    takes 3 + (max_eval + P) / (2 P) slots for its P-point rule, so ~420k slots, e.g.
+ *    200 seven-dimensional integrals at max_eval = 1e6).  Larger calls fail with
+ *    G3L_ERR_INVALID and a message stating the bytes needed; nothing is evaluated.
  *  - Set-up: the first call on a device looks up the scratch's device address (with
  *    that device current); make that first call before capturing any stream.
  *  - The scratch is shared by every context on a device: calls must not overlap
