@@ -39,10 +39,12 @@ sys.path.insert(0, ROOT)
 METRIC = "NNMap evals/s (220 triplets,1h+2h+3h,rtol 1e-4) mixed vs FP64; p50/p99 ms"
 MAX_EVAL = 1_000_000
 RTOL = 1e-4
-# FP32 operations per integrand point of the NNMap 2-halo rule kernel, from the ncu
-# instruction counts (fadd + fmul + 2 ffma, thread-level) of one launch divided by
-# the points it evaluated; see profiles/k_evalmx_nnmap2h.md.
-FLOPS_PER_POINT = {"nnmap_2h": None}
+# FP32 operations per integrand point of the NNMap 2-halo rule kernel k_evalmx<0,2>:
+# ncu thread-level instruction counts (fadd + fmul + 2 ffma) over every launch of one
+# benchmark evaluation (3.434e11) divided by the points those launches evaluated
+# (2.2005e8).  DRAM traffic per launch from the same capture (read + write).
+FLOPS_PER_POINT = {"nnmap_2h": 1561.0}
+DRAM_BYTES_PER_LAUNCH = {"nnmap_2h": 4.03e6}
 
 
 def parse():
@@ -300,10 +302,12 @@ def main():
         if fpp:
             ach = pts_g * fpp / (ms_g * 1e-3) / 1e12
             out["roofline"] = {"bound": "fp32", "achieved": ach, "peak": p32, "unit": "TFLOP/s",
-                               "frac": ach / p32, "traffic": None,
+                               "frac": ach / p32, "traffic": DRAM_BYTES_PER_LAUNCH["nnmap_2h"],
+                               "traffic_unit": "bytes per launch (ncu dram read+write)",
+                               "flops_per_point": fpp,
                                "peak_source": "measured FP32 FMA rate of this device "
-                                              "(g3l_measure_peaks); MEASURED_PEAKS.json holds "
-                                              "only HBM and bf16 figures", **kern}
+                                              "(g3l_measure_peaks, CUDA events); the measured-peaks "
+                                              "file holds only HBM and bf16 figures", **kern}
         else:
             out["roofline"] = {"bound": "fp32", "achieved": None, "peak": p32, "unit": "TFLOP/s",
                                "frac": None, "traffic": None, **kern}

@@ -70,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 print(l)
     objs = [os.path.join(OUT, s + ".o") for s in list(UNITS) + HOST_UNITS]
     tmp = LIB + ".tmp%d" % os.getpid()
-    _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"])
+    _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

@@ -5,6 +5,9 @@
 // n_bar and the integration bounds equal the reference's bit for bit on the
 // same libm.
 #include <algorithm>
+#include <atomic>
+#include <thread>
+#include <vector>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -89,13 +92,27 @@ int n_bar(const Binning &B, const double *hmf, const double hod[6], double *out)
     const double lo[1] = {std::log10(B.mmin)};
     const double hi[1] = {std::log10(B.mmax_integral())};
     const double ln10 = std::log(10.0);
-    for (int i = 0; i < B.Nz; ++i) {
-        NbarCtx C{&B, hmf, hod, B.zmin + i * (B.zmax - B.zmin) / B.Nz};
-        double val, err;
-        if (cubature(1, nbar_integrand, &C, lo, hi, 0, 0, 1e-4, &val, &err, nullptr)) return 1;
-        out[i] = ln10 * val;
-    }
-    return 0;
+    // the Nz integrals are independent: spread them over the host cores (each one is
+    // the same sequential computation as in a single thread)
+    std::atomic<int> next{0}, failed{0};
+    auto work = [&]() {
+        for (int i; (i = next.fetch_add(1)) < B.Nz;) {
+            NbarCtx C{&B, hmf, hod, B.zmin + i * (B.zmax - B.zmin) / B.Nz};
+            double val, err;
+            if (cubature(1, nbar_integrand, &C, lo, hi, 0, 0, 1e-4, &val, &err, nullptr)) {
+                failed = 1;
+                continue;
+            }
+            out[i] = ln10 * val;
+        }
+    };
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nt = (int)std::min<unsigned>(hw, (unsigned)std::max(1, B.Nz / 2));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+    work();
+    for (auto &th : pool) th.join();
+    return failed.load() ? 1 : 0;
 }
 
 double apply_prefactor(int kind, int term, double H0, double Om, double raw)
