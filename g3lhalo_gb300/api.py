@@ -52,6 +52,12 @@ class Result(C.Structure):
                 ("neval", C.c_uint64), ("status", C.c_int32), ("rounds", C.c_int32)]
 
 
+class ServerStats(C.Structure):
+    _fields_ = [("launches", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
+                ("queued", C.c_int32), ("running_integrals", C.c_int32),
+                ("free_regions", C.c_uint64)]
+
+
 class Options(C.Structure):
     _fields_ = [("eval_blocks_per_sm", C.c_int), ("eval_warps_per_block", C.c_int),
                 ("use_graph", C.c_int), ("max_rounds", C.c_int), ("unlimited_pool", C.c_uint64),
@@ -100,6 +106,15 @@ def lib():
                                      C.POINTER(C.c_int64)]
             L.g3l_poll.argtypes = [C.c_void_p, C.c_int64, C.POINTER(Result), C.c_int]
             L.g3l_cancel.argtypes = [C.c_void_p, C.c_int64]
+            L.g3l_server_create.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_int,
+                                            C.POINTER(C.c_void_p)]
+            L.g3l_server_destroy.argtypes = [C.c_void_p]
+            L.g3l_server_destroy.restype = None
+            L.g3l_server_submit.argtypes = [C.c_void_p, C.POINTER(Integral), C.c_int,
+                                            C.POINTER(C.c_int64)]
+            L.g3l_server_poll.argtypes = [C.c_void_p, C.c_int64, C.POINTER(Result), C.c_int, _dp]
+            L.g3l_server_cancel.argtypes = [C.c_void_p, C.c_int64]
+            L.g3l_server_info.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
             L.g3l_get_options.argtypes = [C.c_void_p, C.POINTER(Options)]
             L.g3l_set_options.argtypes = [C.c_void_p, C.POINTER(Options)]
             L.g3l_get_stats.argtypes = [C.c_void_p, C.POINTER(Stats)]
@@ -298,6 +313,61 @@ def results_to_numpy(out, n):
         o = out[i]
         r[i] = (o.val, o.err, o.result, o.neval, o.status, o.rounds)
     return r
+
+
+class Server:
+    """Continuous-batching server on a context (g3l_server_*): submit requests from any
+    thread, poll for results; requests that arrive while others run are admitted as
+    slots and pool space free up and integrate concurrently with them."""
+
+    def __init__(self, ctx, precision=MIXED, max_items_per_term=1024, pool_regions=1 << 22,
+                 rounds_per_launch=4):
+        self.ctx = ctx  # keeps the context alive
+        h = C.c_void_p()
+        _check(lib().g3l_server_create(ctx.h, precision, max_items_per_term, pool_regions,
+                                       rounds_per_launch, C.byref(h)))
+        self.h = h
+        self._n = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().g3l_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, specs):
+        """specs as for Context.eval; returns a ticket."""
+        items, n = Context.make_items(specs)
+        t = C.c_int64()
+        _check(lib().g3l_server_submit(self.h, items, n, C.byref(t)))
+        self._n[t.value] = n
+        return t.value
+
+    def poll(self, ticket, wait_ms=-1, check=True):
+        """Results (structured array) and latency in ms, or None while running."""
+        n = self._n[ticket]
+        out = (Result * n)()
+        lat = C.c_double()
+        st = lib().g3l_server_poll(self.h, ticket, out, wait_ms, C.byref(lat))
+        if st == 9:  # G3L_ERR_BUSY
+            return None
+        del self._n[ticket]
+        if check and st != 0 and st not in (4, 5, 6, 7):
+            _check(st)
+        return results_to_numpy(out, n), lat.value
+
+    def cancel(self, ticket):
+        _check(lib().g3l_server_cancel(self.h, ticket))
+
+    def info(self):
+        s = ServerStats()
+        _check(lib().g3l_server_info(self.h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in ServerStats._fields_}
 
 
 class NNMapModel:

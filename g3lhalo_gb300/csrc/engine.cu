@@ -497,7 +497,11 @@ __global__ void __launch_bounds__(1024) k_scan(IntState *__restrict__ S, long lo
         H->any_active = more;
         H->regions += 2ull * (unsigned long long)tot;
         if (more) H->rounds_done += 1;
-        if (use_cond) cudaGraphSetConditional(handle, more ? 1u : 0u);
+        // a serving launch ends after chunk_rounds rounds; this round's body still runs,
+        // so the states are consistent for the host between launches
+        int go = more;
+        if (more && H->chunk_rounds > 0 && ++H->chunk_count >= H->chunk_rounds) go = 0;
+        if (use_cond) cudaGraphSetConditional(handle, go ? 1u : 0u);
     }
 }
 
@@ -533,6 +537,7 @@ __global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, 
         H->total_work = 0;
         H->regions = (unsigned long long)n;
         H->rounds_done = 0;
+        H->chunk_count = 0;
         H->ties = 0;
         H->small_arg = 0;
         for (int g = 0; g < NGROUPS; ++g) H->n_esc[g] = 0;
@@ -552,6 +557,36 @@ __global__ void k_round_end(BatchHdr *H)
     }
 }
 
+// Serving: place m integrals (packed descriptors Dn) into table slots idx[] and start
+// each one at its root region.
+__global__ void k_admit(const IntDesc *__restrict__ Dn, const int *__restrict__ idx, int m,
+                        IntDesc *__restrict__ D, IntState *__restrict__ S, Pool P)
+{
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < m; j += gridDim.x * blockDim.x) {
+        const IntDesc d = Dn[j];
+        const int i = idx[j];
+        D[i] = d;
+        for (int k = 0; k < d.dim; ++k) {
+            P.center[k * P.stride + d.base] = d.c0[k];
+            P.level[k * P.stride + d.base] = 0;
+        }
+        IntState st;
+        st.val = 0;
+        st.err = 0;
+        st.neval = 0;
+        st.nR = 0;
+        st.K = 0;
+        st.done = 0;
+        st.status = ST_OK;
+        st.rounds = 0;
+        st.pad = 0;
+        st.defer = 0;
+        st.pad2 = 0;
+        S[i] = st;
+    }
+}
+
+void *admit_kernel() { return (void *)k_admit; }
 void *round_end_kernel() { return (void *)k_round_end; }
 void *select_kernel() { return (void *)k_select; }
 void *scan_kernel() { return (void *)k_scan; }

@@ -137,6 +137,8 @@ struct BatchHdr {
     unsigned long long small_arg;
     unsigned long long regions;
     int rounds_done;
+    int chunk_rounds;            // > 0: stop the device loop after this many rounds (serving)
+    int chunk_count;             //   rounds run in the current launch
     int mixed;                   // 1: mixed-precision pass (uncertainty bookkeeping on)
     int n_esc[NGROUPS];          // FP64 re-evaluation queue of each group: fill,
     int esc_cap[NGROUPS];        //   capacity (the group's pool slots)

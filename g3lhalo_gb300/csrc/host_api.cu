@@ -9,12 +9,16 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "g3l_device.cuh"
@@ -30,6 +34,7 @@ void *evalmx_kernel(int kind, int term);
 void *select_kernel();
 void *scan_kernel();
 void *init_kernel();
+void *admit_kernel();
 namespace host {
 const char *last_error_cstr();
 }
@@ -111,8 +116,8 @@ struct g3l_ctx {
     size_t stage_bytes = 0;
     long long *h_pinned = nullptr;
     size_t last_h2d = 0, last_d2h = 0;
-    int64_t next_ticket = 1;
-    std::map<int64_t, std::pair<int, std::vector<g3l_result>>> tickets;
+    g3l_server *srv[2] = {nullptr, nullptr};  // serving loops behind g3l_submit, per precision
+    std::mutex srv_mu;
     // last g3l_eval: descriptor, live region count and pool position of each item
     std::vector<IntDesc> last_D;
     std::vector<int> last_nR, last_pos;
@@ -257,22 +262,21 @@ bool finite_all(const double *a, size_t n)
     return true;
 }
 
-int ensure_workspace(g3l_ctx *c, int n, size_t pool)
+void free_workspace(Workspace &W)
 {
-    Workspace &W = c->W;
-    if (n <= W.n_cap && pool <= W.pool_cap) return G3L_OK;
-    cudaStreamSynchronize(c->stream);
-    int ncap = std::max(n, W.n_cap);
-    size_t pcap = std::max(pool, W.pool_cap);
-    if (n > W.n_cap) ncap = std::max(ncap, (int)(n * 1.25) + 16);
-    if (pool > W.pool_cap) pcap = std::max(pcap, (size_t)(pool * 1.25) + 1024);
     void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.q, W.P.cand,
                     W.P.unc,    W.P.esc,   W.P.uval, W.P.key, W.P.rscr, W.D, W.S, W.woff, W.H};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    W = Workspace{W.pool_cap, W.n_cap, Pool{}, nullptr, nullptr, nullptr, nullptr, W.gen};
-    W.pool_cap = 0;
-    W.n_cap = 0;
+    const int gen = W.gen;
+    W = Workspace{};
+    W.gen = gen;
+}
+
+// Region pools for `pcap` slots and per-integral arrays for `ncap` integrals.
+int alloc_workspace(Workspace &W, int ncap, size_t pcap)
+{
+    free_workspace(W);
     int st = 0;
     st |= dalloc(&W.P.center, pcap * MAX_DIM);
     st |= dalloc(&W.P.level, pcap * MAX_DIM);
@@ -292,17 +296,32 @@ int ensure_workspace(g3l_ctx *c, int n, size_t pool)
     st |= dalloc(&W.S, (size_t)ncap);
     st |= dalloc(&W.woff, (size_t)ncap + 1);
     st |= dalloc(&W.H, 1);
-    if (st) return G3L_ERR_NOMEM;
+    if (st) {
+        free_workspace(W);
+        return G3L_ERR_NOMEM;
+    }
     W.P.stride = (long long)pcap;
     W.pool_cap = pcap;
     W.n_cap = ncap;
     W.gen += 1;
+    return G3L_OK;
+}
+
+int ensure_workspace(g3l_ctx *c, int n, size_t pool)
+{
+    Workspace &W = c->W;
+    if (n <= W.n_cap && pool <= W.pool_cap) return G3L_OK;
+    cudaStreamSynchronize(c->stream);
+    int ncap = std::max(n, W.n_cap);
+    size_t pcap = std::max(pool, W.pool_cap);
+    if (n > W.n_cap) ncap = std::max(ncap, (int)(n * 1.25) + 16);
+    if (pool > W.pool_cap) pcap = std::max(pcap, (size_t)(pool * 1.25) + 1024);
     for (auto &g : c->graphs) {
         cudaGraphExecDestroy(g.exec);
         cudaGraphDestroy(g.graph);
     }
     c->graphs.clear();
-    return G3L_OK;
+    return alloc_workspace(W, ncap, pcap);
 }
 
 void *eval_fn(int precision, int group)
@@ -374,14 +393,17 @@ void set_esc_queues(const IntDesc *D, int n, BatchHdr &H)
     }
 }
 
-int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
+// The device loop as one graph: init, then WHILE (conditional node) { select, [mixed:
+// FP64 re-evaluations, second selection pass], scan, [mixed: re-evaluations], rule
+// evaluation per group }.  `init` = false leaves the states as they are (serving).
+int build_graph_ws(g3l_ctx *c, Workspace &W, int precision, int gmask, bool init,
+                   GraphEntry &out)
 {
-    Workspace &W = c->W;
     KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 1, c->T.tau_sel, c->T.tau_val};
     cudaGraph_t g;
     G3L_CK(cudaGraphCreate(&g, 0));
     cudaGraphNode_t n_init;
-    {
+    if (init) {
         void *args[] = {&a.D, &a.S, &a.P, &a.H};
         int st = add_kernel(g, &n_init, nullptr, 0, init_kernel(), c->nsm * 4, 256, args);
         if (st) return st;
@@ -393,7 +415,7 @@ int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
     cp.conditional.type = cudaGraphCondTypeWhile;
     cp.conditional.size = 1;
     cudaGraphNode_t n_while;
-    G3L_CK(cudaGraphAddNode(&n_while, g, &n_init, nullptr, 1, &cp));
+    G3L_CK(cudaGraphAddNode(&n_while, g, init ? &n_init : nullptr, nullptr, init ? 1 : 0, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     cudaGraphNode_t n_sel, n_scan, prev;
     // mixed: FP64 re-evaluations queued by a selection pass (unsettled splits of the
@@ -466,6 +488,11 @@ int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
     G3L_CK(cudaGraphInstantiate(&ex, g, 0));
     out = GraphEntry{W.gen, precision, gmask, g, ex};
     return G3L_OK;
+}
+
+int build_graph(g3l_ctx *c, int precision, int gmask, GraphEntry &out)
+{
+    return build_graph_ws(c, c->W, precision, gmask, true, out);
 }
 
 // descriptor of one integral: bounds and root geometry as the reference computes them
@@ -599,6 +626,451 @@ int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
         if (*(int *)c->h_pinned == 0) break;
     }
     return G3L_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ serving
+//
+// A server keeps a table of integral slots (one segment per kind x term group, so the
+// rule kernels see each group contiguously) and a region pool on the device, and runs
+// the same device loop as g3l_eval in launches of a few rounds.  Between launches its
+// driver thread collects finished integrals, completes their requests, returns their
+// slots and pool ranges, and admits waiting requests (first come, first served) as
+// slots and pool space allow.  The trajectory of every integral depends only on its
+// own regions, so a result is the same alone and in any mix.
+namespace {
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+struct SrvReq {
+    std::vector<IntDesc> desc;  // per item; base filled at admission
+    std::vector<int> slot;      // table slot per item (-1 before admission)
+    std::vector<g3l_result> res;
+    int remaining = 0;
+    bool admitted = false, done = false, cancel = false;
+    double t_submit = 0, t_done = 0;
+};
+
+// First-fit allocator of pool slot ranges.
+struct RangeAlloc {
+    std::map<long long, long long> free_;  // start -> length
+    long long total_free = 0;
+    void init(long long n)
+    {
+        free_.clear();
+        free_[0] = n;
+        total_free = n;
+    }
+    long long take(long long n)
+    {
+        for (auto it = free_.begin(); it != free_.end(); ++it)
+            if (it->second >= n) {
+                const long long b = it->first, len = it->second;
+                free_.erase(it);
+                if (len > n) free_[b + n] = len - n;
+                total_free -= n;
+                return b;
+            }
+        return -1;
+    }
+    void give(long long b, long long n)
+    {
+        total_free += n;
+        auto it = free_.emplace(b, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+};
+
+}  // namespace
+
+struct g3l_server {
+    g3l_ctx *c = nullptr;
+    int precision = G3L_MIXED;
+    int per_group = 0, n = 0, chunk = 4;
+    size_t pool = 0;
+    cudaStream_t s = nullptr;
+    Workspace W;
+    GraphEntry G{};
+    bool graph_ok = false;
+    std::vector<IntState> Sh;       // host copy of the states after each launch
+    std::vector<int64_t> slot_req;  // slot -> ticket (0 = free)
+    std::vector<int> slot_item;
+    std::vector<std::vector<int>> free_slots;  // per group
+    RangeAlloc ra;
+    std::map<int64_t, SrvReq> reqs;
+    std::deque<int64_t> pending;
+    int64_t next_ticket = 1;
+    int active = 0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::thread th;
+    bool stop = false;
+    int fatal = G3L_OK;
+    std::string fatal_msg;
+    IntDesc *d_new = nullptr;  // admission staging (device)
+    int *d_idx = nullptr;
+    uint64_t launches = 0, admitted_total = 0, completed_total = 0;
+};
+
+namespace {
+
+// Admit waiting requests in order while their items fit (caller holds the lock).
+void srv_admit(g3l_server *v, std::vector<IntDesc> &nd, std::vector<int> &ni)
+{
+    while (!v->pending.empty()) {
+        const int64_t t = v->pending.front();
+        SrvReq &q = v->reqs[t];
+        if (q.cancel) {
+            v->pending.pop_front();
+            for (auto &r : q.res) r.status = G3L_ERR_CANCELLED;
+            q.done = true;
+            q.t_done = now_s();
+            continue;
+        }
+        const int m = (int)q.desc.size();
+        int need[NGROUPS] = {};
+        for (const IntDesc &d : q.desc) ++need[d.kind * 3 + d.term - 1];
+        bool ok = true;
+        for (int g = 0; g < NGROUPS; ++g) ok &= (int)v->free_slots[g].size() >= need[g];
+        if (!ok) break;
+        std::vector<long long> bases(m, -1);
+        for (int k = 0; k < m && ok; ++k) {
+            bases[k] = v->ra.take(q.desc[k].cap);
+            if (bases[k] < 0) ok = false;
+        }
+        if (!ok) {
+            for (int k = 0; k < m; ++k)
+                if (bases[k] >= 0) v->ra.give(bases[k], q.desc[k].cap);
+            break;
+        }
+        v->pending.pop_front();
+        for (int k = 0; k < m; ++k) {
+            IntDesc &d = q.desc[k];
+            auto &fs = v->free_slots[d.kind * 3 + d.term - 1];
+            const int sl = fs.back();
+            fs.pop_back();
+            d.base = bases[k];
+            q.slot[k] = sl;
+            v->slot_req[sl] = t;
+            v->slot_item[sl] = k;
+            v->Sh[sl] = IntState{};
+            nd.push_back(d);
+            ni.push_back(sl);
+        }
+        q.admitted = true;
+        v->active += m;
+        v->admitted_total += 1;
+    }
+}
+
+void srv_fail_all(g3l_server *v, int st, const std::string &msg)
+{
+    std::lock_guard<std::mutex> lk(v->mu);
+    v->fatal = st;
+    v->fatal_msg = msg;
+    for (auto &kv : v->reqs)
+        if (!kv.second.done) {
+            for (auto &r : kv.second.res) r.status = st;
+            kv.second.done = true;
+            kv.second.t_done = now_s();
+        }
+    v->pending.clear();
+    v->cv_done.notify_all();
+}
+
+#define SRV_CK(x)                                                                   \
+    do {                                                                            \
+        cudaError_t e_ = (x);                                                       \
+        if (e_ != cudaSuccess) {                                                    \
+            srv_fail_all(v, G3L_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+            return;                                                                 \
+        }                                                                           \
+    } while (0)
+
+void srv_loop(g3l_server *v)
+{
+    cudaSetDevice(v->c->device);
+    std::vector<IntDesc> nd;
+    std::vector<int> ni;
+    std::vector<int> cancel_slots;
+    BatchHdr H{};
+    for (;;) {
+        nd.clear();
+        ni.clear();
+        cancel_slots.clear();
+        long long cnt[NGROUPS] = {};
+        {
+            std::unique_lock<std::mutex> lk(v->mu);
+            v->cv_work.wait(lk, [&] { return v->stop || !v->pending.empty() || v->active > 0; });
+            if (v->stop) return;
+            srv_admit(v, nd, ni);
+            v->cv_done.notify_all();  // requests cancelled while queued
+            for (int i = 0; i < v->n; ++i) {
+                const int64_t t = v->slot_req[i];
+                if (!t) continue;
+                const SrvReq &q = v->reqs[t];
+                if (q.cancel && !v->Sh[i].done) cancel_slots.push_back(i);
+                const IntDesc &d = q.desc[v->slot_item[i]];
+                cnt[d.kind * 3 + d.term - 1] += d.cap;
+            }
+            if (v->active == 0) continue;
+        }
+        cudaStream_t s = v->s;
+        if (!nd.empty()) {
+            const int m = (int)nd.size();
+            SRV_CK(cudaMemcpyAsync(v->d_new, nd.data(), sizeof(IntDesc) * m, cudaMemcpyHostToDevice, s));
+            SRV_CK(cudaMemcpyAsync(v->d_idx, ni.data(), sizeof(int) * m, cudaMemcpyHostToDevice, s));
+            void *args[] = {&v->d_new, &v->d_idx, (void *)&m, &v->W.D, &v->W.S, &v->W.P};
+            SRV_CK(cudaLaunchKernel(admit_kernel(), dim3((m + 127) / 128), dim3(128), args, 0, s));
+            SRV_CK(cudaStreamSynchronize(s));  // m and the staging must outlive the launch
+        }
+        for (int i : cancel_slots) {
+            IntState st{};
+            st.done = 1;
+            st.status = G3L_ERR_CANCELLED;
+            SRV_CK(cudaMemcpyAsync(v->W.S + i, &st, sizeof st, cudaMemcpyHostToDevice, s));
+        }
+        // header: fixed table layout, this launch's re-evaluation queues and round budget
+        H = BatchHdr{};
+        H.n = v->n;
+        for (int g = 0; g <= NGROUPS; ++g) H.gbeg[g] = g * v->per_group;
+        H.max_rounds = v->c->opt.max_rounds;
+        H.mixed = v->precision == G3L_MIXED ? 1 : 0;
+        H.chunk_rounds = v->chunk;
+        long long beg = 0;
+        for (int g = 0; g < NGROUPS; ++g) {
+            H.esc_beg[g] = beg;
+            H.esc_cap[g] = (int)std::min<long long>(cnt[g], 0x7fffffff);
+            beg += cnt[g];
+        }
+        SRV_CK(cudaMemcpyAsync(v->W.H, &H, sizeof H, cudaMemcpyHostToDevice, s));
+        SRV_CK(cudaGraphLaunch(v->G.exec, s));
+        SRV_CK(cudaMemcpyAsync(v->Sh.data(), v->W.S, sizeof(IntState) * v->n, cudaMemcpyDeviceToHost, s));
+        SRV_CK(cudaStreamSynchronize(s));
+        SRV_CK(cudaGetLastError());
+        {
+            std::lock_guard<std::mutex> lk(v->mu);
+            v->launches += 1;
+            const double t = now_s();
+            for (int i = 0; i < v->n; ++i) {
+                const int64_t tk = v->slot_req[i];
+                if (!tk || !v->Sh[i].done) continue;
+                SrvReq &q = v->reqs[tk];
+                const int k = v->slot_item[i];
+                const IntDesc &d = q.desc[k];
+                const IntState &sr = v->Sh[i];
+                g3l_result &o = q.res[k];
+                o.val = sr.val * d.scale;
+                o.err = sr.err * d.scale;
+                o.neval = sr.neval;
+                o.status = sr.status;
+                o.rounds = sr.rounds;
+                o.result = host::apply_prefactor(d.kind, d.term, v->c->H0, v->c->Om, o.val);
+                v->slot_req[i] = 0;
+                v->free_slots[d.kind * 3 + d.term - 1].push_back(i);
+                v->ra.give(d.base, d.cap);
+                v->active -= 1;
+                if (--q.remaining == 0) {
+                    q.done = true;
+                    q.t_done = t;
+                    v->completed_total += 1;
+                }
+            }
+            v->cv_done.notify_all();
+        }
+    }
+}
+
+void srv_destroy(g3l_server *v)
+{
+    if (!v) return;
+    {
+        std::lock_guard<std::mutex> lk(v->mu);
+        v->stop = true;
+    }
+    v->cv_work.notify_all();
+    if (v->th.joinable()) v->th.join();
+    cudaSetDevice(v->c->device);
+    if (v->s) cudaStreamSynchronize(v->s);
+    if (v->graph_ok) {
+        cudaGraphExecDestroy(v->G.exec);
+        cudaGraphDestroy(v->G.graph);
+    }
+    free_workspace(v->W);
+    if (v->d_new) cudaFree(v->d_new);
+    if (v->d_idx) cudaFree(v->d_idx);
+    if (v->s) cudaStreamDestroy(v->s);
+    delete v;
+}
+
+int srv_create(g3l_ctx *c, int precision, int per_group, uint64_t pool_regions, int chunk,
+               g3l_server **out)
+{
+    if (!c || !out || (precision != G3L_FP64 && precision != G3L_MIXED) || per_group < 1 ||
+        per_group > (1 << 20) || pool_regions < 64 || pool_regions > (1ull << 31) || chunk < 1) {
+        host::set_error("g3l_server_create: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    if (precision == G3L_MIXED && !evalmx_kernel(0, 1)) {
+        host::set_error("g3l_server_create: mixed-precision kernels not built");
+        return G3L_ERR_INVALID;
+    }
+    G3L_CK(cudaSetDevice(c->device));
+    auto *v = new g3l_server;
+    v->c = c;
+    v->precision = precision;
+    v->per_group = per_group;
+    v->n = NGROUPS * per_group;
+    v->pool = (size_t)pool_regions;
+    v->chunk = chunk;
+    int st = G3L_OK;
+    if (cudaStreamCreateWithFlags(&v->s, cudaStreamNonBlocking) != cudaSuccess) st = G3L_ERR_CUDA;
+    if (!st) st = alloc_workspace(v->W, v->n, v->pool);
+    if (!st) st = dalloc(&v->d_new, (size_t)v->n) | dalloc(&v->d_idx, (size_t)v->n);
+    if (!st) st = build_graph_ws(c, v->W, precision, (1 << NGROUPS) - 1, false, v->G);
+    if (!st) v->graph_ok = true;
+    if (!st) {
+        // every slot starts free: a finished state, never selected
+        v->Sh.assign(v->n, IntState{});
+        for (auto &x : v->Sh) x.done = 1;
+        if (cudaMemcpy(v->W.S, v->Sh.data(), sizeof(IntState) * v->n, cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+            st = G3L_ERR_CUDA;
+    }
+    if (st) {
+        if (st == G3L_ERR_NOMEM) host::set_error("g3l_server_create: device allocation failed");
+        srv_destroy(v);
+        return st;
+    }
+    v->slot_req.assign(v->n, 0);
+    v->slot_item.assign(v->n, 0);
+    v->free_slots.assign(NGROUPS, {});
+    for (int g = 0; g < NGROUPS; ++g)
+        for (int k = per_group - 1; k >= 0; --k) v->free_slots[g].push_back(g * per_group + k);
+    v->ra.init((long long)v->pool);
+    v->th = std::thread(srv_loop, v);
+    *out = v;
+    return G3L_OK;
+}
+
+int srv_submit(g3l_server *v, const g3l_integral *items, int n, int64_t *ticket)
+{
+    if (!v || !ticket || n < 1 || !items) {
+        host::set_error("g3l_server_submit: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    SrvReq q;
+    q.desc.resize(n);
+    q.slot.assign(n, -1);
+    q.res.assign(n, g3l_result{});
+    q.remaining = n;
+    int need[NGROUPS] = {};
+    for (int i = 0; i < n; ++i) {
+        if (!item_ok(v->c, items[i])) {
+            host::set_error("g3l_server_submit: invalid integral " + std::to_string(i));
+            return G3L_ERR_INVALID;
+        }
+        IntDesc &d = q.desc[i];
+        fill_desc(v->c, items[i], v->precision, d);
+        unsigned long long cap = items[i].max_eval
+                                     ? 3 + (items[i].max_eval + d.npts) / (2ull * d.npts)
+                                     : v->c->opt.unlimited_pool;
+        if (cap > v->pool) {
+            host::set_error("g3l_server_submit: integral " + std::to_string(i) +
+                            " needs more region slots than the server's pool");
+            return G3L_ERR_INVALID;
+        }
+        d.cap = (int)cap;
+        ++need[d.kind * 3 + d.term - 1];
+    }
+    for (int g = 0; g < NGROUPS; ++g)
+        if (need[g] > v->per_group) {
+            host::set_error("g3l_server_submit: more integrals of one kind and term than the "
+                            "server's slots for it");
+            return G3L_ERR_INVALID;
+        }
+    std::lock_guard<std::mutex> lk(v->mu);
+    if (v->fatal) {
+        host::set_error("g3l_server_submit: server stopped: " + v->fatal_msg);
+        return v->fatal;
+    }
+    q.t_submit = now_s();
+    const int64_t t = v->next_ticket++;
+    v->reqs.emplace(t, std::move(q));
+    v->pending.push_back(t);
+    *ticket = t;
+    v->cv_work.notify_all();
+    return G3L_OK;
+}
+
+int srv_poll(g3l_server *v, int64_t ticket, g3l_result *out, int wait_ms, double *latency_ms)
+{
+    if (!v) return G3L_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(v->mu);
+    auto it = v->reqs.find(ticket);
+    if (it == v->reqs.end()) {
+        host::set_error("g3l_server_poll: unknown ticket");
+        return G3L_ERR_INVALID;
+    }
+    if (!it->second.done && wait_ms != 0) {
+        auto pred = [&] { return v->reqs.at(ticket).done; };
+        if (wait_ms < 0) v->cv_done.wait(lk, pred);
+        else v->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), pred);
+    }
+    it = v->reqs.find(ticket);
+    if (!it->second.done) return G3L_ERR_BUSY;
+    SrvReq &q = it->second;
+    int first_bad = G3L_OK;
+    for (auto &r : q.res)
+        if (r.status && !first_bad) first_bad = r.status;
+    if (out) std::copy(q.res.begin(), q.res.end(), out);
+    if (latency_ms) *latency_ms = 1e3 * (q.t_done - q.t_submit);
+    v->reqs.erase(it);
+    if (first_bad) host::set_error("g3l_server_poll: an integral ended with status " + std::to_string(first_bad));
+    return first_bad;
+}
+
+int srv_cancel(g3l_server *v, int64_t ticket)
+{
+    if (!v) return G3L_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(v->mu);
+    auto it = v->reqs.find(ticket);
+    if (it == v->reqs.end() || it->second.done) return G3L_ERR_INVALID;
+    SrvReq &q = it->second;
+    q.cancel = true;
+    if (!q.admitted) {  // still queued: finish it now
+        v->pending.erase(std::find(v->pending.begin(), v->pending.end(), ticket));
+        for (auto &r : q.res) r.status = G3L_ERR_CANCELLED;
+        q.done = true;
+        q.t_done = now_s();
+        v->cv_done.notify_all();
+    }
+    v->cv_work.notify_all();
+    return G3L_OK;
+}
+
+g3l_server *ctx_server(g3l_ctx *c, int precision, int *st)
+{
+    std::lock_guard<std::mutex> lk(c->srv_mu);
+    g3l_server *&v = c->srv[precision == G3L_MIXED ? 1 : 0];
+    if (!v) *st = srv_create(c, precision, 1024, 1ull << 22, 4, &v);
+    return v;
 }
 
 }  // namespace
@@ -755,6 +1227,8 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
 void g3l_ctx_destroy(g3l_ctx *c)
 {
     if (!c) return;
+    srv_destroy(c->srv[0]);
+    srv_destroy(c->srv[1]);
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto &g : c->graphs) {
@@ -1193,30 +1667,68 @@ int g3l_measure_peaks(g3l_ctx *c, double *fp32_tflops, double *fp64_tflops)
 
 int g3l_submit(g3l_ctx *c, const g3l_integral *items, int n, int precision, int64_t *ticket)
 {
-    if (!c || !ticket) return G3L_ERR_INVALID;
-    std::vector<g3l_result> res(n > 0 ? n : 0);
-    int st = g3l_eval(c, items, n, precision, res.data());
-    *ticket = c->next_ticket++;
-    c->tickets[*ticket] = {st, std::move(res)};
-    return G3L_OK;
+    if (!c || !ticket || (precision != G3L_FP64 && precision != G3L_MIXED)) {
+        host::set_error("g3l_submit: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    int st = G3L_OK;
+    g3l_server *v = ctx_server(c, precision, &st);
+    if (!v) return st ? st : G3L_ERR_INVALID;
+    int64_t t = 0;
+    st = srv_submit(v, items, n, &t);
+    if (!st) *ticket = 2 * t + (precision == G3L_MIXED ? 1 : 0);
+    return st;
 }
 
 int g3l_poll(g3l_ctx *c, int64_t ticket, g3l_result *out, int wait)
 {
-    (void)wait;
-    if (!c) return G3L_ERR_INVALID;
-    auto it = c->tickets.find(ticket);
-    if (it == c->tickets.end()) return G3L_ERR_INVALID;
-    if (out) std::copy(it->second.second.begin(), it->second.second.end(), out);
-    int st = it->second.first;
-    c->tickets.erase(it);
-    return st;
+    if (!c || ticket < 2) return G3L_ERR_INVALID;
+    g3l_server *v = c->srv[ticket & 1];
+    if (!v) return G3L_ERR_INVALID;
+    return srv_poll(v, ticket >> 1, out, wait ? -1 : 0, nullptr);
 }
 
 int g3l_cancel(g3l_ctx *c, int64_t ticket)
 {
-    if (!c) return G3L_ERR_INVALID;
-    return c->tickets.count(ticket) ? G3L_OK : G3L_ERR_INVALID;
+    if (!c || ticket < 2) return G3L_ERR_INVALID;
+    g3l_server *v = c->srv[ticket & 1];
+    if (!v) return G3L_ERR_INVALID;
+    return srv_cancel(v, ticket >> 1);
+}
+
+int g3l_server_create(g3l_ctx *ctx, int precision, int max_items_per_term, uint64_t pool_regions,
+                      int rounds_per_launch, g3l_server **out)
+{
+    return srv_create(ctx, precision, max_items_per_term, pool_regions, rounds_per_launch, out);
+}
+
+void g3l_server_destroy(g3l_server *srv) { srv_destroy(srv); }
+
+int g3l_server_submit(g3l_server *srv, const g3l_integral *items, int n, int64_t *ticket)
+{
+    return srv_submit(srv, items, n, ticket);
+}
+
+int g3l_server_poll(g3l_server *srv, int64_t ticket, g3l_result *out, int wait_ms,
+                    double *latency_ms)
+{
+    return srv_poll(srv, ticket, out, wait_ms, latency_ms);
+}
+
+int g3l_server_cancel(g3l_server *srv, int64_t ticket) { return srv_cancel(srv, ticket); }
+
+int g3l_server_info(g3l_server *srv, g3l_server_stats *st)
+{
+    if (!srv || !st) return G3L_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    *st = g3l_server_stats{};
+    st->launches = srv->launches;
+    st->admitted = srv->admitted_total;
+    st->completed = srv->completed_total;
+    st->queued = (int)srv->pending.size();
+    st->running_integrals = srv->active;
+    st->free_regions = (uint64_t)srv->ra.total_free;
+    return G3L_OK;
 }
 
 }  // extern "C"

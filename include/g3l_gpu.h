@@ -116,9 +116,51 @@ int g3l_get_densities(g3l_ctx *ctx, int slot, double *rho_bar, double *n_bar);
 int g3l_eval(g3l_ctx *ctx, const g3l_integral *items, int n, int precision,
              g3l_result *out);
 
-/* Asynchronous form for serving: enqueue on the context's stream and return a
- * ticket; g3l_poll returns G3L_OK with results when done, G3L_ERR_BUSY while
- * running.  g3l_cancel stops the refinement loop of a running ticket. */
+/* Serving with continuous batching.  A server owns a table of integral slots
+ * (max_items_per_term for each kind x term) and a pool of pool_regions region slots
+ * on the device, and a driver thread that runs the device loop of g3l_eval in
+ * launches of rounds_per_launch refinement rounds.  Between launches it completes
+ * the integrals that finished, frees their slots and pool ranges, and admits waiting
+ * requests first come, first served, as slots and pool space allow (an integral with
+ * max_eval M and a P-point rule takes 3 + (M + P) / (2P) pool slots).  Requests that
+ * arrive while others run are therefore integrated concurrently with them, and every
+ * integral's result is the same as from g3l_eval alone (its trajectory depends only
+ * on its own regions).  The server reads the context's tables, HOD slots and options
+ * as they are at creation; a HOD slot used by a queued or running request must not
+ * be changed until that request completes.  Submit, poll and cancel may be called
+ * from any thread.  The reference evaluates one term per blocking call
+ * (src/NNMap_Model.cu:299-373); this replaces its calculateAll loop for callers that
+ * issue many model evaluations (src/NNMap_Model.cu:382-415). */
+typedef struct g3l_server g3l_server;
+typedef struct g3l_server_stats {
+    uint64_t launches;        /* device-loop launches so far */
+    uint64_t admitted;        /* requests admitted */
+    uint64_t completed;       /* requests whose integrals all finished */
+    int32_t queued;           /* requests waiting for slots or pool space */
+    int32_t running_integrals;/* integrals on the device now */
+    uint64_t free_regions;    /* unallocated pool slots */
+} g3l_server_stats;
+int g3l_server_create(g3l_ctx *ctx, int precision, int max_items_per_term, uint64_t pool_regions,
+                      int rounds_per_launch, g3l_server **out);
+void g3l_server_destroy(g3l_server *srv); /* waits for the running launch, drops the rest */
+/* Queue n integrals as one request.  Fails (G3L_ERR_INVALID) if the request could
+ * never fit the server's slots or pool. */
+int g3l_server_submit(g3l_server *srv, const g3l_integral *items, int n, int64_t *ticket);
+/* G3L_ERR_BUSY while the request runs (after waiting up to wait_ms; -1 = until done,
+ * 0 = do not wait).  Once done: copies the n results to out, releases the ticket and
+ * returns the first non-OK integral status, or OK; latency_ms (optional) receives the
+ * time from submit to completion. */
+int g3l_server_poll(g3l_server *srv, int64_t ticket, g3l_result *out, int wait_ms,
+                    double *latency_ms);
+/* A queued request finishes at once; a running one at the next launch boundary.  Its
+ * integrals report G3L_ERR_CANCELLED unless they had already finished. */
+int g3l_server_cancel(g3l_server *srv, int64_t ticket);
+int g3l_server_info(g3l_server *srv, g3l_server_stats *st);
+
+/* The same on a context: g3l_submit starts (on first use) one server per precision
+ * with 1024 slots per kind x term, 4M pool slots and 4 rounds per launch.  g3l_poll
+ * with wait != 0 blocks until the request is done; otherwise it returns G3L_ERR_BUSY
+ * while it runs.  g3l_ctx_destroy stops these servers. */
 int g3l_submit(g3l_ctx *ctx, const g3l_integral *items, int n, int precision,
                int64_t *ticket);
 int g3l_poll(g3l_ctx *ctx, int64_t ticket, g3l_result *out, int wait);
