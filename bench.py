@@ -59,6 +59,7 @@ def parse():
     # smaller cases for profiler captures: N evenly spaced triplets, host-driven rounds
     ap.add_argument("--triplets", type=int, default=0)
     ap.add_argument("--host-loop", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     return ap.parse_args()
 
 
@@ -179,6 +180,47 @@ def run_reference(args, rank, world):
             "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def serving_leg(G, ctx, trip, hods, args, n_req=48, rate=12.0, seed=7):
+    """Continuous batching: a seeded Poisson stream of model evaluations (triplet
+    count log-uniform in 1..220, NNMap or NMapMap, one of 8 HOD vectors) submitted to
+    a server while earlier ones run; latency = submit to completion."""
+    rng = np.random.default_rng(seed)
+    for k in range(8):
+        ctx.set_hod(8 + k, hods[(40 + k) % len(hods)])
+    srv = G.Server(ctx, G.MIXED, max_items_per_term=2048, pool_regions=1 << 24,
+                   rounds_per_launch=4)
+    reqs = []
+    for _ in range(n_req):
+        nt = int(np.clip(np.round(np.exp(rng.uniform(0, np.log(220)))), 1, 220))
+        idx = np.sort(rng.choice(len(trip), nt, replace=False))
+        kind = int(rng.integers(0, 2))
+        slot = 8 + int(rng.integers(0, 8))
+        reqs.append([(kind, t, slot, slot, tuple(trip[i]), RTOL, args.max_eval)
+                     for i in idx for t in (1, 2, 3)])
+    gaps = rng.exponential(1.0 / rate, n_req)
+    tickets, lat = [], []
+    t0 = time.perf_counter()
+    for q, gap in zip(reqs, gaps):
+        time.sleep(gap)
+        tickets.append(srv.submit(q))
+    for t in tickets:
+        r, ms = srv.poll(t)
+        lat.append(ms)
+    wall = time.perf_counter() - t0
+    info = srv.info()
+    srv.close()
+    pts_integrals = sum(len(q) for q in reqs)
+    return {"requests": n_req, "arrival_rate_per_s": rate, "integrals": pts_integrals,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(np.mean(lat)), "wall_s": wall,
+            "requests_per_s": n_req / wall,
+            "model_evals_per_s": pts_integrals / 660.0 / wall,
+            "launches": info["launches"],
+            "workload": "Poisson arrivals (seeded), triplets per request log-uniform 1..220, "
+                        "NNMap or NMapMap 1h+2h+3h, rtol 1e-4, maxEval %d, 8 HOD vectors; "
+                        "model_evals_per_s counts 660 integrals as one evaluation" % args.max_eval}
 
 
 def main():
@@ -312,6 +354,8 @@ def main():
             out["roofline"] = {"bound": "fp32", "achieved": None, "peak": p32, "unit": "TFLOP/s",
                                "frac": None, "traffic": None, **kern}
         out["peaks_measured"] = {"fp32_tflops": p32, "fp64_tflops": p64}
+        if not args.no_serving:
+            out["serving"] = serving_leg(G, ctx, trip, hods, args)
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_sample(T, trip, hods[last_hod], args.max_eval, 4)
         out["config"] = config(len(trip), args.max_eval)
