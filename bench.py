@@ -182,6 +182,17 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(dev_s, wall_s, dist=None):
+    """Device and wall time of the timed steps, the maximum over the replicas (one
+    rank per GPU; the replicas share no data, so this is the only collective)."""
+    if dist is None:
+        return dev_s, wall_s
+    import torch
+    tt = torch.tensor([dev_s, wall_s], dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt[0]), float(tt[1])
+
+
 def serving_leg(G, ctx, trip, hods, args, n_req=48, rate=12.0, seed=7):
     """Continuous batching: a seeded Poisson stream of model evaluations (triplet
     count log-uniform in 1..220, NNMap or NMapMap, one of 8 HOD vectors) submitted to
@@ -276,12 +287,8 @@ def main():
         results.append(r)
     total = time.perf_counter() - t0
     if dist:
-        import torch
-        tt = torch.tensor([sum(dev_ms), total], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dev_total, total = float(tt[0]) / 1e3, float(tt[1])
-    else:
-        dev_total = sum(dev_ms) / 1e3
+        dist.barrier()
+    dev_total, total = max_over_ranks(sum(dev_ms) / 1e3, total, dist)
     clk = clocks.stop()
     st_last = ctx.stats()
     value = world * args.steps / dev_total
