@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--triplets", type=int, default=0)
     ap.add_argument("--host-loop", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    # batched fit sweep: this many HOD vectors in one launch (0 = skip)
+    ap.add_argument("--sweep", type=int, default=16)
     return ap.parse_args()
 
 
@@ -191,6 +193,30 @@ def max_over_ranks(dev_s, wall_s, dist=None):
     tt = torch.tensor([dev_s, wall_s], dtype=torch.float64)
     dist.all_reduce(tt, op=dist.ReduceOp.MAX)
     return float(tt[0]), float(tt[1])
+
+
+def sweep_leg(G, ctx, trip, hods, n_hod, max_eval):
+    """Batched fit sweep: n_hod HOD vectors x 220 triplets x 3 terms in one launch."""
+    from g3lhalo_gb300 import workloads as W
+    hs = hods[:n_hod] if n_hod <= len(hods) else W.hod_sweep(n_hod, seed=12345)
+    t0 = time.perf_counter()
+    for k, h in enumerate(hs):
+        ctx.set_hod(16 + k, h)
+    t_hod = time.perf_counter() - t0
+    specs = [(G.NNMAP, t, 16 + k, 16 + k, tuple(th), RTOL, max_eval)
+             for k in range(n_hod) for th in trip for t in (1, 2, 3)]
+    ctx.eval(specs[:3 * len(trip)], G.MIXED)  # warm the graph shapes
+    t0 = time.perf_counter()
+    r = ctx.eval(specs, G.MIXED)
+    wall = time.perf_counter() - t0
+    st = ctx.stats()
+    return {"hod_vectors": n_hod, "integrals": len(specs),
+            "model_evals_per_s": n_hod / (st["device_ms"] * 1e-3),
+            "device_ms": st["device_ms"], "wall_s": wall, "hod_update_s": t_hod,
+            "points_per_s": st["points_evaluated"] / (st["device_ms"] * 1e-3),
+            "rounds": st["rounds"], "status_ok": bool((r["status"] == 0).all()),
+            "workload": "%d seeded HOD vectors (the fit-sweep box) x 220 triplets x 1h+2h+3h, "
+                        "rtol 1e-4, maxEval %d, one g3l_eval call" % (n_hod, max_eval)}
 
 
 def serving_leg(G, ctx, trip, hods, args, n_req=48, rate=12.0, seed=7):
@@ -363,6 +389,8 @@ def main():
         out["peaks_measured"] = {"fp32_tflops": p32, "fp64_tflops": p64}
         if not args.no_serving:
             out["serving"] = serving_leg(G, ctx, trip, hods, args)
+        if args.sweep:
+            out["sweep"] = sweep_leg(G, ctx, trip, hods, args.sweep, args.max_eval)
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_sample(T, trip, hods[last_hod], args.max_eval, 4)
         out["config"] = config(len(trip), args.max_eval)

@@ -64,7 +64,7 @@ class Options(C.Structure):
                 ("small_arg", C.c_double), ("unc_eps_rel", C.c_double),
                 ("unc_tau_abs", C.c_double), ("unc_tau_impact", C.c_double),
                 ("unc_tau_sel", C.c_double), ("unc_tau_val", C.c_double),
-                ("unc_eps_val", C.c_double)]
+                ("unc_eps_val", C.c_double), ("unc_eps_sel", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -75,7 +75,8 @@ class Stats(C.Structure):
                 ("escalated", C.c_uint64), ("deferred", C.c_uint64), ("polished", C.c_uint64),
                 ("group_ms", C.c_double * 6), ("group_points", C.c_uint64 * 6),
                 ("reeval_ms", C.c_double), ("select_ms", C.c_double),
-                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64)]
+                ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+                ("escalated_full", C.c_uint64)]
 
 
 INTEGRAND_V = C.CFUNCTYPE(C.c_int, C.c_uint, C.c_size_t, _dp, C.c_void_p, C.c_uint, _dp)

@@ -544,6 +544,7 @@ __global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, 
         H->escalated = 0;
         H->deferred = 0;
         H->polished = 0;
+        H->esc_full = 0;
     }
 }
 

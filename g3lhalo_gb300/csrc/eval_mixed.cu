@@ -788,7 +788,8 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
     const float ue = fabsf((float)(W::w1 - W::wE1)) * u0 + fabsf((float)(W::w2 - W::wE2)) * u2 +
                      fabsf((float)(W::w3 - W::wE3)) * u3 + fabsf((float)(W::w4 - W::wE4)) * u4 +
                      fabsf((float)W::w5) * u5;
-    const float urel = e.hi > 0.f ? fminf(ue / e.hi, 1e30f) : (ue > 0.f ? 1e30f : 0.f);
+    const float urel =
+        e.hi > 0.f ? fminf(T.unc_sel_ratio * ue / e.hi, 1e30f) : (ue > 0.f ? 1e30f : 0.f);
     // and of the value (weights of res7)
     const float uv = fabsf((float)W::w1) * u0 + fabsf((float)W::w2) * u2 +
                      fabsf((float)W::w3) * u3 + fabsf((float)W::w4) * u4 +

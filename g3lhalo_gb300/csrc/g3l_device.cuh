@@ -65,6 +65,7 @@ struct DevTables {
     float fA, feps, small_arg;
     float unc_eps, unc_abs;        // FP32 point-value error bound (decisions)
     float unc_val_ratio;           // value-noise bound / decision bound
+    float unc_sel_ratio;           // error-estimate bound (selection) / decision bound
     double tau_impact, tau_sel;    // escalation thresholds (fraction of the integral)
     double tau_val;                // bound on the FP32 noise left in a finished integral
     const unsigned long long *tie_z_bits;
@@ -146,6 +147,7 @@ struct BatchHdr {
     unsigned long long escalated;// statistics: regions re-evaluated in FP64
     unsigned long long deferred; // statistics: selections deferred for re-evaluation
     unsigned long long polished; // statistics: finished integrals polished in FP64
+    unsigned long long esc_full; // statistics: whole-rule FP64 re-evaluations queued
     double *dbg;                 // debug: per-point integrand values of one work item
 };
 
@@ -155,6 +157,7 @@ __device__ inline void push_esc(BatchHdr *H, const Pool &P, int g, int i, int co
 {
     const int k = atomicAdd(&H->n_esc[g], 1);
     if (k < H->esc_cap[g]) P.esc[H->esc_beg[g] + k] = make_int2(i, code);
+    if (code >> 30) atomicAdd(&H->esc_full, 1ull);
 }
 
 // Point p of a dim-dimensional Genz-Malik rule -> coordinate variant of dim d,

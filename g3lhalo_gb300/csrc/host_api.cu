@@ -67,8 +67,12 @@ int dalloc(T **p, size_t n)
 }
 
 // FP64 re-evaluation entries per group and round that take the device-wide passes
-// (scratch ~39 MB per group); further entries take the batched kernel.
-constexpr int kReevalCap = 8192;
+// (4.8 kB of scratch each): 4 per integral, between 8192 (39 MB per group) and 524288
+// (2.5 GB per group); further entries take the batched kernel.
+int reeval_cap(int n_integrals)
+{
+    return (int)std::min<long long>(std::max<long long>(4ll * n_integrals, 8192), 524288);
+}
 
 struct Workspace {
     size_t pool_cap = 0;
@@ -220,6 +224,7 @@ int prepare_mixed(g3l_ctx *c, const g3l_tables *t)
     T.tau_sel = c->opt.unc_tau_sel;
     T.tau_val = c->opt.unc_tau_val;
     T.unc_val_ratio = (float)(c->opt.unc_eps_val / c->opt.unc_eps_rel);
+    T.unc_sel_ratio = (float)(c->opt.unc_eps_sel / c->opt.unc_eps_rel);
     st |= dalloc(&c->d_fnbar, (size_t)MAX_HOD_SLOTS * Nz);
     st |= dalloc(&c->d_fhodp, (size_t)MAX_HOD_SLOTS * 8);
     if (st) return st;
@@ -289,8 +294,8 @@ int alloc_workspace(Workspace &W, int ncap, size_t pcap)
     st |= dalloc(&W.P.uval, pcap);
     st |= dalloc(&W.P.key, pcap);
     st |= dalloc(&W.P.esc, pcap);
-    W.P.rcap = kReevalCap;
-    W.P.rscr_group = reeval_scratch_group_bytes(kReevalCap);
+    W.P.rcap = reeval_cap(ncap);
+    W.P.rscr_group = reeval_scratch_group_bytes(W.P.rcap);
     st |= dalloc(&W.P.rscr, (size_t)(NGROUPS * W.P.rscr_group));
     st |= dalloc(&W.D, (size_t)ncap);
     st |= dalloc(&W.S, (size_t)ncap);
@@ -1163,6 +1168,7 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
     c->opt.unc_tau_sel = 1e-7;
     c->opt.unc_tau_val = 5e-5;
     c->opt.unc_eps_val = 5e-6;
+    c->opt.unc_eps_sel = 5e-5;
 
     DevTables &T = c->T;
     T.Nz = t->Nz;
@@ -1334,7 +1340,7 @@ int g3l_get_options(g3l_ctx *c, g3l_options *o)
 int g3l_set_options(g3l_ctx *c, const g3l_options *o)
 {
     if (!c || !o || o->max_rounds < 1 || o->unlimited_pool < 16 || !(o->small_arg >= 0) ||
-        !(o->unc_eps_rel > 0) || !(o->unc_eps_val >= 0)) {
+        !(o->unc_eps_rel > 0) || !(o->unc_eps_val >= 0) || !(o->unc_eps_sel >= 0)) {
         host::set_error("g3l_set_options: invalid option value");
         return G3L_ERR_INVALID;
     }
@@ -1346,6 +1352,7 @@ int g3l_set_options(g3l_ctx *c, const g3l_options *o)
     c->T.tau_sel = o->unc_tau_sel;
     c->T.tau_val = o->unc_tau_val;
     c->T.unc_val_ratio = (float)(o->unc_eps_val / o->unc_eps_rel);
+    c->T.unc_sel_ratio = (float)(o->unc_eps_sel / o->unc_eps_rel);
     for (auto &g : c->graphs) {
         cudaGraphExecDestroy(g.exec);
         cudaGraphDestroy(g.graph);
@@ -1502,6 +1509,7 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
     sx.d2h_bytes = c->last_d2h;
     sx.deferred = Hout.deferred;
     sx.polished = Hout.polished;
+    sx.escalated_full = Hout.esc_full;
     sx.device_ms = ms;
     int first_bad = G3L_OK;
     uint64_t pts = 0;

@@ -190,6 +190,10 @@ typedef struct g3l_options {
     /* Relative bound on the FP32 error of one point value used for the value-noise
      * estimate of unc_tau_val (decisions use unc_eps_rel; default 5e-6). */
     double unc_eps_val;
+    /* Relative bound on the FP32 error of one point value used for the bound on a
+     * region's error estimate, which decides whether a selection boundary is settled
+     * (split decisions use unc_eps_rel). */
+    double unc_eps_sel;
 } g3l_options;
 int g3l_get_options(g3l_ctx *ctx, g3l_options *opt);
 int g3l_set_options(g3l_ctx *ctx, const g3l_options *opt);
@@ -215,6 +219,7 @@ typedef struct g3l_stats {
     double reeval_ms;         /* FP64 re-evaluation kernels */
     double select_ms;         /* selection + scan kernels */
     uint64_t h2d_bytes, d2h_bytes; /* bytes copied in / out by the call */
+    uint64_t escalated_full;  /* of escalated: whole-rule re-evaluations (selection, polish) */
 } g3l_stats;
 int g3l_get_stats(g3l_ctx *ctx, g3l_stats *st);
 
