@@ -64,7 +64,8 @@ class Options(C.Structure):
                 ("small_arg", C.c_double), ("unc_eps_rel", C.c_double),
                 ("unc_tau_abs", C.c_double), ("unc_tau_impact", C.c_double),
                 ("unc_tau_sel", C.c_double), ("unc_tau_val", C.c_double),
-                ("unc_eps_val", C.c_double), ("unc_eps_sel", C.c_double)]
+                ("unc_eps_val", C.c_double), ("unc_eps_sel", C.c_double),
+                ("evalmx_variant", C.c_int * 6)]
 
 
 class Stats(C.Structure):
@@ -125,6 +126,8 @@ def lib():
                                            C.POINTER(C.c_int), C.c_int, _dp, _dp]
             L.g3l_eval_static.argtypes = [C.c_void_p, C.POINTER(Integral), C.c_int, C.c_int,
                                           C.POINTER(Result)]
+            L.g3l_autotune.argtypes = [C.c_void_p, C.POINTER(Integral), C.c_int,
+                                       C.POINTER(C.c_int), _dp]
             L.g3l_debug_pool.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp,
                                          C.POINTER(C.c_int), _dp, _dp, C.POINTER(C.c_int),
                                          C.POINTER(C.c_float), C.POINTER(C.c_int)]
@@ -283,6 +286,15 @@ class Context:
                                     C.byref(n)))
         return {"n": nr, "centers": cen, "levels": lev, "val": val[:nr], "err": err[:nr],
                 "split": spl[:nr], "unc": unc[:nr], "uval": unc[nr:2 * nr]}
+
+    def autotune(self, specs):
+        """Pick the rule-kernel register budget per kind x term on this batch; returns
+        (variant per group, ms[6][3])."""
+        items, n = self.make_items(specs)
+        v = (C.c_int * 6)()
+        ms = np.zeros(18)
+        _check(lib().g3l_autotune(self.h, items, n, v, _ptr(ms)))
+        return list(v), ms.reshape(6, 3)
 
     @staticmethod
     def make_items(specs):

@@ -25,7 +25,8 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-I" + CSRC, "-I" + INCLUDE,
 UNITS = {
     "engine.cu": ["-fmad=false"],
     "eval_fp64.cu": ["-fmad=false"],
-    "eval_mixed.cu": ["-fmad=true"],
+    "evalmx_k0.cu": ["-fmad=true"],
+    "evalmx_k1.cu": ["-fmad=true"],
     "host_api.cu": ["-fmad=false"],
     "probe.cu": ["-fmad=true"],
 }

@@ -1,3 +1,4 @@
+#pragma once
 // eval_mixed.cu -- mixed-precision rule evaluation: FP32 integrand, wide accumulation.
 //
 // Same work decomposition as eval_fp64.cu (one warp cuts one parent region and
@@ -825,8 +826,10 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
     __syncwarp();
 }
 
-template <int KIND, int TERM>
-__global__ void __launch_bounds__(128) k_evalmx(DevTables T, const IntDesc *__restrict__ D,
+// MINB: the blocks per SM the register budget is cut for (4: 128 registers per thread,
+// 6: 80, 8: 64); the autotuner picks it per kind x term.
+template <int KIND, int TERM, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_evalmx(DevTables T, const IntDesc *__restrict__ D,
                                                 IntState *__restrict__ S, Pool P, BatchHdr *H,
                                                 const long long *__restrict__ woff)
 {
@@ -872,24 +875,6 @@ __global__ void __launch_bounds__(128) k_evalmx(DevTables T, const IntDesc *__re
         if (tw) atomicAdd(&H->ties, (unsigned long long)tw);
         if (sw) atomicAdd(&H->small_arg, (unsigned long long)sw);
     }
-}
-
-#define G3L_INSTMX(K, Tm)                                                                        \
-    template __global__ void k_evalmx<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,      \
-                                             BatchHdr *, const long long *);
-G3L_INSTMX(0, 1)
-G3L_INSTMX(0, 2)
-G3L_INSTMX(0, 3)
-G3L_INSTMX(1, 1)
-G3L_INSTMX(1, 2)
-G3L_INSTMX(1, 3)
-
-void *evalmx_kernel(int kind, int term)
-{
-    static void *tab[2][3] = {
-        {(void *)k_evalmx<0, 1>, (void *)k_evalmx<0, 2>, (void *)k_evalmx<0, 3>},
-        {(void *)k_evalmx<1, 1>, (void *)k_evalmx<1, 2>, (void *)k_evalmx<1, 3>}};
-    return tab[kind][term - 1];
 }
 
 }  // namespace g3l

@@ -30,7 +30,12 @@ void *eval64_kernel(int kind, int term);
 void *reeval64_kernel(int kind, int term);
 void *reeval_phase_kernel(int kind, int term, int phase);
 void *round_end_kernel();
-void *evalmx_kernel(int kind, int term);
+void *evalmx_kernel_k0(int term, int variant);
+void *evalmx_kernel_k1(int term, int variant);
+inline void *evalmx_kernel(int kind, int term, int variant = 0)
+{
+    return kind == 0 ? evalmx_kernel_k0(term, variant) : evalmx_kernel_k1(term, variant);
+}
 void *select_kernel();
 void *scan_kernel();
 void *init_kernel();
@@ -329,10 +334,11 @@ int ensure_workspace(g3l_ctx *c, int n, size_t pool)
     return alloc_workspace(W, ncap, pcap);
 }
 
-void *eval_fn(int precision, int group)
+void *eval_fn(const g3l_ctx *c, int precision, int group)
 {
     int kind = group / 3, term = group % 3 + 1;
-    return precision == G3L_FP64 ? eval64_kernel(kind, term) : evalmx_kernel(kind, term);
+    return precision == G3L_FP64 ? eval64_kernel(kind, term)
+                                 : evalmx_kernel(kind, term, c->opt.evalmx_variant[group]);
 }
 
 int eval_grid(g3l_ctx *c, void *fn)
@@ -482,7 +488,7 @@ int build_graph_ws(g3l_ctx *c, Workspace &W, int precision, int gmask, bool init
     }
     for (int grp = 0; grp < NGROUPS; ++grp) {
         if (!(gmask & (1 << grp))) continue;
-        void *fn = eval_fn(precision, grp);
+        void *fn = eval_fn(c, precision, grp);
         void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
         cudaGraphNode_t n_ev;
         int st = add_kernel(body, &n_ev, &prev, 1, fn, eval_grid(c, fn), 128, args);
@@ -613,7 +619,7 @@ int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
         }
         for (int grp = 0; grp < NGROUPS; ++grp) {
             if (!(gmask & (1 << grp))) continue;
-            void *fn = eval_fn(precision, grp);
+            void *fn = eval_fn(c, precision, grp);
             void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
             G3L_CK(cudaEventRecord(c->tev[2 * grp], s));
             G3L_CK(cudaLaunchKernel(fn, dim3(eval_grid(c, fn)), dim3(128), args, 0, s));
@@ -1169,6 +1175,9 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
     c->opt.unc_tau_val = 5e-5;
     c->opt.unc_eps_val = 5e-6;
     c->opt.unc_eps_sel = 5e-5;
+    // register-budget variant of the rule kernels per kind x term (autotuned default:
+    // 6 blocks per SM for 1h and 2h, 8 for 3h)
+    for (int g = 0; g < NGROUPS; ++g) c->opt.evalmx_variant[g] = (g % 3 == 2) ? 2 : 1;
 
     DevTables &T = c->T;
     T.Nz = t->Nz;
@@ -1340,7 +1349,9 @@ int g3l_get_options(g3l_ctx *c, g3l_options *o)
 int g3l_set_options(g3l_ctx *c, const g3l_options *o)
 {
     if (!c || !o || o->max_rounds < 1 || o->unlimited_pool < 16 || !(o->small_arg >= 0) ||
-        !(o->unc_eps_rel > 0) || !(o->unc_eps_val >= 0) || !(o->unc_eps_sel >= 0)) {
+        !(o->unc_eps_rel > 0) || !(o->unc_eps_val >= 0) || !(o->unc_eps_sel >= 0) ||
+        std::any_of(o->evalmx_variant, o->evalmx_variant + NGROUPS,
+                    [](int v) { return v < 0 || v > 2; })) {
         host::set_error("g3l_set_options: invalid option value");
         return G3L_ERR_INVALID;
     }
@@ -1359,6 +1370,48 @@ int g3l_set_options(g3l_ctx *c, const g3l_options *o)
     }
     c->graphs.clear();
     return G3L_OK;
+}
+
+int g3l_autotune(g3l_ctx *c, const g3l_integral *items, int n, int variant_out[6],
+                 double *ms_out)
+{
+    if (!c || !items || n < 1 || !variant_out) {
+        host::set_error("g3l_autotune: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    const g3l_options keep = c->opt;
+    double ms[NGROUPS][3] = {};
+    uint64_t pts[NGROUPS] = {};
+    std::vector<g3l_result> res(n);
+    int st = G3L_OK;
+    for (int v = 0; v < 3 && !st; ++v) {
+        g3l_options o = keep;
+        o.use_graph = 0;
+        for (int g = 0; g < NGROUPS; ++g) o.evalmx_variant[g] = v;
+        st = g3l_set_options(c, &o);
+        for (int rep = 0; rep < 2 && !st; ++rep) {  // the first pass warms the kernels
+            st = g3l_eval(c, items, n, G3L_MIXED, res.data());
+            if (st == G3L_ERR_POOL || st == G3L_ERR_ROUNDS || st == G3L_ERR_NONFINITE) st = G3L_OK;
+        }
+        for (int g = 0; g < NGROUPS; ++g) {
+            ms[g][v] = c->stats.group_ms[g];
+            pts[g] = c->stats.group_points[g];
+        }
+    }
+    g3l_options best = keep;
+    for (int g = 0; g < NGROUPS; ++g) {
+        if (!st && pts[g]) {
+            int b = 0;
+            for (int v = 1; v < 3; ++v)
+                if (ms[g][v] < ms[g][b]) b = v;
+            best.evalmx_variant[g] = b;
+        }
+        variant_out[g] = best.evalmx_variant[g];
+        if (ms_out)
+            for (int v = 0; v < 3; ++v) ms_out[g * 3 + v] = ms[g][v];
+    }
+    const int st2 = g3l_set_options(c, &best);
+    return st ? st : st2;
 }
 
 int g3l_get_stats(g3l_ctx *c, g3l_stats *s)
@@ -1642,7 +1695,7 @@ int g3l_debug_region(g3l_ctx *c, const g3l_integral *item, const double *center,
         if (rc) break;
         KernelArgs a{c->T, W.D, W.S, W.P, W.H, W.woff, 0, 0, 0.0, 0.0};
         void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
-        if (cudaLaunchKernel(eval_fn(precision, grp), dim3(1), dim3(128), args, 0, s)) {
+        if (cudaLaunchKernel(eval_fn(c, precision, grp), dim3(1), dim3(128), args, 0, s)) {
             rc = G3L_ERR_CUDA;
             break;
         }
@@ -1969,7 +2022,7 @@ extern "C" int g3l_eval_static(g3l_ctx *c, const g3l_integral *items, int n, int
             if ((st = reevals())) return st;
         for (int g = 0; g < NGROUPS; ++g) {
             if (!(gmask & (1 << g))) continue;
-            void *fn = eval_fn(precision, g);
+            void *fn = eval_fn(c, precision, g);
             void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
             G3L_CK(cudaLaunchKernel(fn, dim3(eval_grid(c, fn)), dim3(128), args, 0, s));
             ++launches;

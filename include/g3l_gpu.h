@@ -194,9 +194,23 @@ typedef struct g3l_options {
      * region's error estimate, which decides whether a selection boundary is settled
      * (split decisions use unc_eps_rel). */
     double unc_eps_sel;
+    /* Register budget of the mixed-precision rule kernel per kind x term
+     * (kind * 3 + term - 1): 0, 1, 2 = 4, 6, 8 blocks per SM (128, 80, 64 registers
+     * per thread).  Set by g3l_autotune; default 1, 1, 2 for the 1-, 2-, 3-halo terms. */
+    int evalmx_variant[6];
 } g3l_options;
 int g3l_get_options(g3l_ctx *ctx, g3l_options *opt);
 int g3l_set_options(g3l_ctx *ctx, const g3l_options *opt);
+
+/* Autotuner: runs the batch once per register-budget variant of the mixed-precision
+ * rule kernels (after one warm-up pass each; host-driven rounds with CUDA events around
+ * every launch), and keeps for each kind x term present the variant with the least
+ * rule-kernel time in the context's options (evalmx_variant).  variant_out[6] receives
+ * the choice; ms_out (optional, [6][3]) the rule-kernel milliseconds per group and
+ * variant.  The number of regions refined per round is not tuned: it is fixed by the
+ * reference's algorithm (src/hcubature.cpp:904-1021), which the results must follow. */
+int g3l_autotune(g3l_ctx *ctx, const g3l_integral *items, int n, int variant_out[6],
+                 double *ms_out);
 
 /* Per-call diagnostics of the last g3l_eval: kernel launches, rounds, regions,
  * device time, and counters of the exact-index fallbacks. */

@@ -150,3 +150,21 @@ def test_mixed_statistics(rect):
     assert st["points_evaluated"] > 0 and st["regions_evaluated"] > 0
     assert st["escalated"] > 0   # FP64 re-evaluations happen on these integrals
     assert st["device_ms"] > 0
+
+
+def test_autotune_picks_a_variant_per_term_and_keeps_parity(rect):
+    """g3l_autotune times the three register-budget variants of the rule kernels on a
+    batch and keeps the fastest per kind x term; the results stay within the contract."""
+    T, _ = rect
+    c = G.Context(T, clamp_k=True)
+    c.set_hod(0, W.hod_default())
+    specs = _bench_specs(G.NNMAP, step=22, max_eval=200_000)
+    variants, ms = c.autotune(specs)
+    assert all(v in (0, 1, 2) for v in variants)
+    assert np.all(ms[:3] > 0)                      # NNMap groups timed for every variant
+    assert list(c.options().evalmx_variant) == variants
+    assert c.options().use_graph == 1              # the tuner restores the graph path
+    a = c.eval(specs, G.FP64)
+    b = c.eval(specs, G.MIXED)
+    assert np.array_equal(a["neval"], b["neval"])
+    assert _rel(b["val"], a["val"]).max() < TERM_RTOL
