@@ -293,6 +293,11 @@ __device__ __forceinline__ df ln_df(float v)
     return df_add_f(el, logf(m));
 }
 
+// Distinct (l, m, z) variant combinations among the points of one Genz-Malik rule:
+// the centre, 4 axis variants of each of the 3 dimensions, 4 (+-l4, +-l4) pairs of each
+// of the 3 dimension pairs, and the 8 corners.
+constexpr int UC_MAX = 1 + 12 + 12 + 8;
+
 // ------------------------------------------------------------------ per-term models
 struct Child {
     double c64[MAX_DIM + 1];  // FP64 centres: dims of child 0, then child 1's split dim
@@ -449,9 +454,43 @@ struct ModelF {
         return kix_exact64(T, q);
     }
 
+    // u_NFW calls that depend on one l, one mass and z only: evaluated once per distinct
+    // (l, m, z) variant combination of a work item (ucached) and passed to point() in uc[].
+    // {l dim, m dim, concentration factor: 0 = 1, 1 = f of hod1, 2 = f of hod2}
+    static constexpr int NF = TERM == 2 ? 4 : 2;
+    // the 3-halo kernels evaluate their u_NFW per point: measured faster there
+    static constexpr bool UC = TERM != 3;
+    __host__ __device__ static constexpr int ufun(int f, int k)
+    {
+        return KIND == 0 ? (TERM == 1 ? (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1) : (k == 0 ? 1 : k == 1 ? 3 : 2))
+                            : TERM == 2 ? (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1)
+                                           : f == 1 ? (k == 0 ? 1 : k == 1 ? 3 : 2)
+                                           : f == 2 ? (k == 0 ? 0 : k == 1 ? 4 : 1)
+                                                    : (k == 0 ? 1 : k == 1 ? 4 : 2))
+                                        : (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1) : (k == 0 ? 1 : k == 1 ? 4 : 2)))
+                         : (TERM == 1 ? (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1) : (k == 0 ? 1 : k == 1 ? 3 : 0))
+                            : TERM == 2 ? (f == 0 ? (k == 0 ? 1 : k == 1 ? 3 : 0)
+                                           : f == 1 ? (k == 0 ? 0 : k == 1 ? 4 : 1)
+                                           : f == 2 ? (k == 0 ? 1 : k == 1 ? 4 : 0)
+                                                    : (k == 0 ? 0 : k == 1 ? 3 : 1))
+                                        : (f == 0 ? (k == 0 ? 1 : k == 1 ? 3 : 0) : (k == 0 ? 0 : k == 1 ? 4 : 1)));
+    }
+
+    // the cached u_NFW f at slots L (l), M (mass), Z (z), with the expressions of point()
+    __device__ static float ucached(const DevTables &T, const IntDesc &d, int f, const SlotF &L,
+                                    const SlotF &M, const SlotF &Z, int &small)
+    {
+        const float kx = L.f[0] * Z.f[1];
+        const float r = cbrtf(M.f[0] * Z.f[2]);
+        const float cc = __ldg(T.f_conc + Z.i1 * T.Nm + M.i1);
+        const int fs = ufun(f, 2);
+        const float fac = fs == 0 ? cc : (fs == 1 ? T.f_hodp[8 * d.hod1] : T.f_hodp[8 * d.hod2]) * cc;
+        return u_nfw32(kx * r, fac, T.small_arg, small);
+    }
+
     __device__ static float point(const DevTables &T, const IntDesc &d, const SlotF *const *s,
                                   const Child &C, int ch, int sdim, uint32_t vv, unsigned &ties,
-                                  int &small)
+                                  int &small, const float *uc)
     {
         const SlotF &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
         const float l1 = L1.f[0], l2 = L2.f[0], cphi = PH.f[0];
@@ -470,8 +509,8 @@ struct ModelF {
                 const float r2 = cbrtf(M.f[0] * k200);
                 const float cc = __ldg(T.f_conc + zt * Nm + M.i1);
                 const float u3 = u_nfw32(k3 * r2, cc, sa, small);
-                const float u1 = u_nfw32(k1 * r2, f1 * cc, sa, small);
-                const float u2 = u_nfw32(k2 * r2, f2 * cc, sa, small);
+                const float u1 = uc[0];
+                const float u2 = uc[1];
                 const float H = __ldg(T.f_hmf + zr * Nm + M.i0);
                 const float Ggg = M.f[1] * M.f[4] * u2 + M.f[3] * M.f[2] * u1 + M.f[5] * u1 * u2;
                 return A12 * U3 * Z.f[0] * (H * M.f[0] * M.f[0]) * u3 * Ggg;
@@ -487,10 +526,10 @@ struct ModelF {
                 const float cb = __ldg(T.f_conc + zt * Nm + M2.i1);
                 const float u3_1 = u_nfw32(k3 * ra, ca, sa, small);
                 const float u3_2 = u_nfw32(k3 * rb, cb, sa, small);
-                const float u1_1 = u_nfw32(k1 * ra, f1 * ca, sa, small);
-                const float u2_1 = u_nfw32(k2 * ra, f2 * ca, sa, small);
-                const float u1_2 = u_nfw32(k1 * rb, f1 * cb, sa, small);
-                const float u2_2 = u_nfw32(k2 * rb, f2 * cb, sa, small);
+                const float u1_1 = uc[0];
+                const float u2_1 = uc[1];
+                const float u1_2 = uc[2];
+                const float u2_2 = uc[3];
                 const float Ggg = M2.f[1] * M2.f[4] * u2_2 + M2.f[3] * M2.f[2] * u1_2 +
                                   M2.f[5] * u1_2 * u2_2;
                 const float G11 = M1.f[1] + M1.f[2] * u1_1, G22 = M2.f[3] + M2.f[4] * u2_2;
@@ -523,8 +562,8 @@ struct ModelF {
                 const float r2 = cbrtf(M.f[0] * k200);
                 const float cc = __ldg(T.f_conc + zt * Nm + M.i1);
                 const float m = M.f[0];
-                const float G = M.f[1] + M.f[2] * u_nfw32(k1 * r2, f * cc, sa, small);
-                const float u2 = u_nfw32(k2 * r2, cc, sa, small);
+                const float G = M.f[1] + M.f[2] * uc[0];
+                const float u2 = uc[1];
                 const float u3 = u_nfw32(k3 * r2, cc, sa, small);
                 return A12 * U3 * Z.f[0] * (__ldg(T.f_hmf + zr * Nm + M.i0) * m * m * m) * G * u2 * u3;
             } else if (TERM == 2) {
@@ -537,12 +576,12 @@ struct ModelF {
                 const float ra = cbrtf(M1.f[0] * k200), rb = cbrtf(M2.f[0] * k200);
                 const float ca = __ldg(T.f_conc + zt * Nm + M1.i1);
                 const float cb = __ldg(T.f_conc + zt * Nm + M2.i1);
-                const float u2_1 = u_nfw32(k2 * ra, ca, sa, small);
+                const float u2_1 = uc[0];
                 const float u3_2 = u_nfw32(k3 * rb, cb, sa, small);
-                const float u1_2f = u_nfw32(k1 * rb, f * cb, sa, small);
+                const float u1_2f = uc[1];
                 const float u3_1 = u_nfw32(k3 * ra, ca, sa, small);
-                const float u2_2 = u_nfw32(k2 * rb, cb, sa, small);
-                const float u1_1f = u_nfw32(k1 * ra, f * ca, sa, small);
+                const float u2_2 = uc[2];
+                const float u1_1f = uc[3];
                 const float G2 = M2.f[1] + M2.f[2] * u1_2f, G1 = M1.f[1] + M1.f[2] * u1_1f;
                 const float m1 = M1.f[0], m2 = M2.f[0];
                 const float HB = (__ldg(T.f_hmf + zr * Nm + M1.i0) * m1) *
@@ -628,7 +667,8 @@ template <int KIND, int TERM>
 __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, double Vcur,
                            const Pool &P, BatchHdr *H, long long pslot, long long qslot, bool cut,
                            SlotF *slots, float *vals, Child &C, const uint32_t *sdesc,
-                           unsigned &ties, int &small)
+                           unsigned &ties, int &small, const uint8_t *ucidx,
+                           const uint16_t *ucl, const int *ucn, float *ucache)
 {
     constexpr int DIM = TERM + 4;
     constexpr int NP = rule_points(DIM);
@@ -678,6 +718,22 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
         ModelF<KIND, TERM>::fill(T, d, C, sd, dim, v, x, slots[t], ties);
     }
     __syncwarp();
+    // u_NFW of the (l, m, z) variant combinations the points share, per child
+    constexpr int NF = ModelF<KIND, TERM>::NF;
+    for (int t = lane; ModelF<KIND, TERM>::UC && t < nchild * NF * UC_MAX; t += 32) {
+        const int ch = t / (NF * UC_MAX), r = t - ch * NF * UC_MAX;
+        const int f = r / UC_MAX, j = r - f * UC_MAX;
+        if (j >= ucn[f]) continue;
+        const uint32_t key = ucl[f * UC_MAX + j];
+        const int dl = ModelF<KIND, TERM>::ufun(f, 0), dm = ModelF<KIND, TERM>::ufun(f, 1);
+        const int vl = key & 7, vm = (key >> 3) & 7, vz = (key >> 6) & 7;
+        auto sl = [&](int dim, int v) -> const SlotF & {
+            return (ch && dim == sdim) ? slots[DIM * NVAR + v] : slots[dim * NVAR + v];
+        };
+        ucache[(ch * NF + f) * UC_MAX + j] =
+            ModelF<KIND, TERM>::ucached(T, d, f, sl(dl, vl), sl(dm, vm), sl(DIM - 1, vz), small);
+    }
+    __syncwarp();
     // points
     for (int p = lane; p < nchild * NP; p += 32) {
         const int ch = p >= NP ? 1 : 0;
@@ -689,7 +745,12 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
             const int v = (vv >> (3 * dd)) & 7;
             sp[dd] = (ch && dd == sdim) ? &slots[DIM * NVAR + v] : &slots[dd * NVAR + v];
         }
-        vals[p] = ModelF<KIND, TERM>::point(T, d, sp, C, ch, sdim, vv, ties, small);
+        float uc[NF] = {};
+        if (ModelF<KIND, TERM>::UC) {
+#pragma unroll
+            for (int f = 0; f < NF; ++f) uc[f] = ucache[(ch * NF + f) * UC_MAX + ucidx[f * NP + pp]];
+        }
+        vals[p] = ModelF<KIND, TERM>::point(T, d, sp, C, ch, sdim, vv, ties, small, uc);
         if (H->dbg) H->dbg[p] = (double)vals[p];
     }
     __syncwarp();
@@ -841,6 +902,26 @@ __global__ void __launch_bounds__(128, MINB) k_evalmx(DevTables T, const IntDesc
     __shared__ SlotF sslot[WPB][NSLOT];
     __shared__ float svals[WPB][2 * NP];
     __shared__ Child schild[WPB];
+    constexpr int NF = ModelF<KIND, TERM>::NF;
+    __shared__ uint8_t ucidx[NF * NP];           // combination of each point, per function
+    __shared__ uint16_t ucl[NF * UC_MAX];        // variants (l | m << 3 | z << 6) of each
+    __shared__ int ucn[NF];
+    __shared__ float ucache[WPB][2 * NF * UC_MAX];
+    if (ModelF<KIND, TERM>::UC && threadIdx.x < NF) {  // the distinct (l, m, z) combinations
+        const int f = threadIdx.x;
+        const int dl = ModelF<KIND, TERM>::ufun(f, 0), dm = ModelF<KIND, TERM>::ufun(f, 1);
+        int n = 0;
+        for (int p = 0; p < NP; ++p) {
+            const uint32_t vv = point_variants(DIM, p);
+            const uint32_t key = ((vv >> (3 * dl)) & 7) | (((vv >> (3 * dm)) & 7) << 3) |
+                                 (((vv >> (3 * (DIM - 1))) & 7) << 6);
+            int j = 0;
+            while (j < n && ucl[f * UC_MAX + j] != key) ++j;
+            if (j == n && n < UC_MAX) ucl[f * UC_MAX + n++] = (uint16_t)key;
+            ucidx[f * NP + p] = (uint8_t)(j < UC_MAX ? j : UC_MAX - 1);
+        }
+        ucn[f] = n;
+    }
     const int g = KIND * 3 + TERM - 1;
     for (int p = threadIdx.x; p < NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
     __syncthreads();
@@ -866,7 +947,8 @@ __global__ void __launch_bounds__(128, MINB) k_evalmx(DevTables T, const IntDesc
         const long long pslot = d.base + (cut ? cj : 0);
         const long long qslot = cut ? d.base + (S[i].nR - S[i].K) + j : -1;
         warp_itemF<KIND, TERM>(T, d, i, S[i].val, P, H, pslot, qslot, cut, sslot[wib],
-                               svals[wib], schild[wib], sdesc, ties, small);
+                               svals[wib], schild[wib], sdesc, ties, small, ucidx, ucl, ucn,
+                               ucache[wib]);
     }
     // warp-aggregated diagnostics
     unsigned tw = __reduce_add_sync(0xffffffffu, ties);
