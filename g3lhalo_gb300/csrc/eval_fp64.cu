@@ -55,7 +55,21 @@ struct Model64 {
     }
 
     // Integrand at one point from its variant slots (kernel_function_* of the reference).
-    __device__ static double point(const DevTables &T, const IntDesc &d, const Slot64 *const *s)
+    // cached u_NFW f (ucache_fun) at slots L (l), M (mass), Z (z): the expressions of point()
+    __device__ static double ucached(const DevTables &T, const IntDesc &d, int f, const Slot64 &L,
+                                     const Slot64 &M, const Slot64 &Z)
+    {
+        const double w_ = __ldg(T.w + Z.i0);
+        const double k = L.a[0] / w_;
+        const double r = r200_64(M.a[0], __ldg(T.rho_bar + Z.i1));
+        const double c = __ldg(T.conc + Z.i1 * T.Nm + M.i1);
+        const int fs = ucache_fun(KIND, TERM, f, 2);
+        return u_nfw64(k, r, c, fs == 0 ? 1.0 : (fs == 1 ? T.hod[6 * d.hod1] : T.hod[6 * d.hod2]));
+    }
+
+    // uc: the cached u_NFW values of this point (ucache_fun order), or null
+    __device__ static double point(const DevTables &T, const IntDesc &d, const Slot64 *const *s,
+                                   const double *uc = nullptr)
     {
         const Slot64 &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
         const double l1 = L1.a[0], l2 = L2.a[0], cphi = PH.a[0], z = Z.a[0];
@@ -80,8 +94,8 @@ struct Model64 {
                 const double r2 = r200_64(m, rhot);
                 const double cc = __ldg(T.conc + z_it * Nm + M.i1);
                 const double u3 = u_nfw64(k3, r2, cc, 1);
-                const double u2 = u_nfw64(k2, r2, cc, f2);
-                const double u1 = u_nfw64(k1, r2, cc, f1);
+                const double u2 = uc ? uc[1] : u_nfw64(k2, r2, cc, f2);
+                const double u1 = uc ? uc[0] : u_nfw64(k1, r2, cc, f1);
                 double Bggd = 1. / nbar1 / nbar2 / rho * __ldg(T.hmf + z_ix * Nm + M.i0) * m * u3;
                 Bggd *= M.a[1] * M.a[4] * u2 + M.a[3] * M.a[2] * u1 + M.a[5] * u1 * u2;
                 double bggk = Bggd / __ldg(T.dwdz + z_ix) * __ldg(T.g + z_ix) *
@@ -99,10 +113,10 @@ struct Model64 {
                 const double cb = __ldg(T.conc + z_it * Nm + M2.i1);
                 const double u3_1 = u_nfw64(k3, ra, ca, 1);
                 const double u3_2 = u_nfw64(k3, rb, cb, 1);
-                const double u1_1 = u_nfw64(k1, ra, ca, f1);
-                const double u2_1 = u_nfw64(k2, ra, ca, f2);
-                const double u1_2 = u_nfw64(k1, rb, cb, f1);
-                const double u2_2 = u_nfw64(k2, rb, cb, f2);
+                const double u1_1 = uc ? uc[0] : u_nfw64(k1, ra, ca, f1);
+                const double u2_1 = uc ? uc[1] : u_nfw64(k2, ra, ca, f2);
+                const double u1_2 = uc ? uc[2] : u_nfw64(k1, rb, cb, f1);
+                const double u2_2 = uc ? uc[3] : u_nfw64(k2, rb, cb, f2);
                 // G_gg(k1, k2, m2)
                 const double Ggg = M2.a[1] * M2.a[4] * u2_2 + M2.a[3] * M2.a[2] * u1_2 +
                                    M2.a[5] * u1_2 * u2_2;
@@ -123,8 +137,8 @@ struct Model64 {
                 const Slot64 &M1 = *s[3], &M2 = *s[4], &M3 = *s[5];
                 const double m1 = M1.a[0], m2 = M2.a[0], m3 = M3.a[0];
                 const double u3 = u_nfw64(k3, r200_64(m3, rhot), __ldg(T.conc + z_it * Nm + M3.i1), 1);
-                const double u1 = u_nfw64(k1, r200_64(m1, rhot), __ldg(T.conc + z_it * Nm + M1.i1), f1);
-                const double u2 = u_nfw64(k2, r200_64(m2, rhot), __ldg(T.conc + z_it * Nm + M2.i1), f2);
+                const double u1 = uc ? uc[0] : u_nfw64(k1, r200_64(m1, rhot), __ldg(T.conc + z_it * Nm + M1.i1), f1);
+                const double u2 = uc ? uc[1] : u_nfw64(k2, r200_64(m2, rhot), __ldg(T.conc + z_it * Nm + M2.i1), f2);
                 const double Gg1 = M1.a[1] + M1.a[2] * u1;  // hod1 at m1
                 const double Gg2 = M2.a[3] + M2.a[4] * u2;  // hod2 at m2
                 double Bggd = 1. / nbar1 / nbar2 / rho * __ldg(T.hmf + z_ix * Nm + M1.i0) *
@@ -147,8 +161,8 @@ struct Model64 {
                 const double r2 = r200_64(m, rhot);
                 const double cc = __ldg(T.conc + z_it * Nm + M.i1);
                 double Bgdd = 1. / nbar / rho / rho * __ldg(T.hmf + z_ix * Nm + M.i0) * m * m *
-                              (M.a[1] + M.a[2] * u_nfw64(k1, r2, cc, f)) * u_nfw64(k2, r2, cc, 1) *
-                              u_nfw64(k3, r2, cc, 1);
+                              (M.a[1] + M.a[2] * (uc ? uc[0] : u_nfw64(k1, r2, cc, f))) *
+                              (uc ? uc[1] : u_nfw64(k2, r2, cc, 1)) * u_nfw64(k3, r2, cc, 1);
                 double bgkk = Bgdd / __ldg(T.dwdz + z_ix) * gz * gz * __ldg(T.p1 + z_ix) / w_ / w_ *
                               (1. + z) * (1. + z);
                 return l1 * l2 * m * l1 * l2 * L1.a[1] * L2.a[1] * U3 * bgkk / nbar;
@@ -162,12 +176,12 @@ struct Model64 {
                 const double ra = r200_64(m1, rhot), rb = r200_64(m2, rhot);
                 const double ca = __ldg(T.conc + z_it * Nm + M1.i1);
                 const double cb = __ldg(T.conc + z_it * Nm + M2.i1);
-                const double u2_1 = u_nfw64(k2, ra, ca, 1);
+                const double u2_1 = uc ? uc[0] : u_nfw64(k2, ra, ca, 1);
                 const double u3_2 = u_nfw64(k3, rb, cb, 1);
-                const double u1_2f = u_nfw64(k1, rb, cb, f);
+                const double u1_2f = uc ? uc[1] : u_nfw64(k1, rb, cb, f);
                 const double u3_1 = u_nfw64(k3, ra, ca, 1);
-                const double u2_2 = u_nfw64(k2, rb, cb, 1);
-                const double u1_1f = u_nfw64(k1, ra, ca, f);
+                const double u2_2 = uc ? uc[2] : u_nfw64(k2, rb, cb, 1);
+                const double u1_1f = uc ? uc[3] : u_nfw64(k1, ra, ca, f);
                 double Bgdd = 1. / nbar / rho / rho * __ldg(T.hmf + z_ix * Nm + M1.i0) *
                               __ldg(T.hmf + z_ix * Nm + M2.i0) * __ldg(T.b_h + z_ix * Nm + M1.i0) *
                               __ldg(T.b_h + z_ix * Nm + M2.i0) *
@@ -187,8 +201,9 @@ struct Model64 {
                 double Bgdd = 1. / nbar / rho / rho * __ldg(T.hmf + z_ix * Nm + M1.i0) *
                               __ldg(T.hmf + z_ix * Nm + M2.i0) * __ldg(T.hmf + z_ix * Nm + M3.i0) *
                               __ldg(T.b_h + z_ix * Nm + M1.i0) * __ldg(T.b_h + z_ix * Nm + M2.i0) *
-                              __ldg(T.b_h + z_ix * Nm + M3.i0) * m1 * m2 * u_nfw64(k2, ra, ca, 1) *
-                              u_nfw64(k3, rb, cb, 1) * (M3.a[1] + M3.a[2] * u_nfw64(k1, rb, cb, f)) *
+                              __ldg(T.b_h + z_ix * Nm + M3.i0) * m1 * m2 *
+                              (uc ? uc[0] : u_nfw64(k2, ra, ca, 1)) * u_nfw64(k3, rb, cb, 1) *
+                              (M3.a[1] + M3.a[2] * (uc ? uc[1] : u_nfw64(k1, rb, cb, f))) *
                               bi_lin64(T, k1, k2, cphi, z_ix);
                 double bgkk = Bgdd / __ldg(T.dwdz + z_ix) * gz * gz * __ldg(T.p1 + z_ix) / w_ / w_ *
                               (1. + z) * (1. + z);
@@ -398,6 +413,10 @@ struct Reeval {
         return (double *)(P.rscr + (long long)G * P.rscr_group +
                           ((long long)P.rcap * MAX_DIM * NVAR * reeval_slot_bytes + 255) / 256 * 256);
     }
+    __device__ static double *ucv(const Pool &P)  // [rcap][UC_NF_MAX][UC_MAX]
+    {
+        return vals(P) + (long long)P.rcap * 256;
+    }
     __device__ static int count(const Pool &P, const BatchHdr *H)
     {
         const int cap = H->esc_cap[G];
@@ -438,6 +457,42 @@ __global__ void __launch_bounds__(128) k_re_fill(DevTables T, const IntDesc *__r
     }
 }
 
+// cached u_NFW of each entry's (l, m, z) combinations (whole rules: all of them; split
+// only: those without corner variants, whose slots are not filled)
+template <int KIND, int TERM>
+__global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *__restrict__ D,
+                                                   IntState *__restrict__ S, Pool P, BatchHdr *H,
+                                                   const long long *__restrict__ woff)
+{
+    using R = Reeval<KIND, TERM>;
+    constexpr int NF = ucache_nf(TERM);
+    __shared__ uint8_t ucidx[NF * R::NP];
+    __shared__ uint16_t ucl[NF * UC_MAX];
+    __shared__ int ucn[NF];
+    const int m = R::count(P, H);
+    if (m == 0) return;
+    ucache_tables<KIND, TERM>(ucidx, ucl, ucn);
+    __syncthreads();
+    const int2 *Q = P.esc + H->esc_beg[R::G];
+    const Slot64 *SL = R::slots(P);
+    double *UC = R::ucv(P);
+    const long long tot = (long long)m * NF * UC_MAX;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(t / (NF * UC_MAX)), r = (int)(t - (long long)k * NF * UC_MAX);
+        const int f = r / UC_MAX, j = r - f * UC_MAX;
+        if (j >= ucn[f]) continue;
+        const int2 ent = Q[k];
+        const uint32_t key = ucl[f * UC_MAX + j];
+        const int vl = key & 7, vm = (key >> 3) & 7, vz = (key >> 6) & 7;
+        if (!(ent.y >> 30) && (vl >= 5 || vm >= 5 || vz >= 5)) continue;
+        const Slot64 *base = SL + (long long)k * R::NS;
+        const int dl = ucache_fun(KIND, TERM, f, 0), dm = ucache_fun(KIND, TERM, f, 1);
+        UC[((long long)k * UC_NF_MAX + f) * UC_MAX + j] = Model64<KIND, TERM>::ucached(
+            T, D[ent.x], f, base[dl * NVAR + vl], base[dm * NVAR + vm], base[(R::DIM - 1) * NVAR + vz]);
+    }
+}
+
 template <int KIND, int TERM>
 __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *__restrict__ D,
                                                    IntState *__restrict__ S, Pool P, BatchHdr *H,
@@ -445,14 +500,20 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
 {
     using R = Reeval<KIND, TERM>;
     constexpr int DIM = R::DIM;
+    constexpr int NF = ucache_nf(TERM);
     __shared__ uint32_t sdesc[R::NP];
+    __shared__ uint8_t ucidx[NF * R::NP];
+    __shared__ uint16_t ucl[NF * UC_MAX];
+    __shared__ int ucn[NF];
     const int m = R::count(P, H);
     if (m == 0) return;
     for (int p = threadIdx.x; p < R::NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
+    ucache_tables<KIND, TERM>(ucidx, ucl, ucn);
     __syncthreads();
     const int2 *Q = P.esc + H->esc_beg[R::G];
     const Slot64 *SL = R::slots(P);
     double *VL = R::vals(P);
+    const double *UC = R::ucv(P);
     const long long tot = (long long)m * R::NPAD;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
          t += (long long)gridDim.x * blockDim.x) {
@@ -465,7 +526,11 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
         const Slot64 *sp[DIM];
 #pragma unroll
         for (int dd = 0; dd < DIM; ++dd) sp[dd] = base + dd * NVAR + ((vv >> (3 * dd)) & 7);
-        VL[(long long)k * R::NPAD + p] = Model64<KIND, TERM>::point(T, d, sp);
+        double uc[NF];
+#pragma unroll
+        for (int f = 0; f < NF; ++f)
+            uc[f] = UC[((long long)k * UC_NF_MAX + f) * UC_MAX + ucidx[f * R::NP + p]];
+        VL[(long long)k * R::NPAD + p] = Model64<KIND, TERM>::point(T, d, sp, uc);
     }
 }
 
@@ -605,6 +670,8 @@ __global__ void __launch_bounds__(128) k_reeval64(DevTables T, const IntDesc *__
                                                BatchHdr *, const long long *);                   \
     template __global__ void k_re_fill<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,     \
                                               BatchHdr *, const long long *);                    \
+    template __global__ void k_re_ucache<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,   \
+                                                BatchHdr *, const long long *);                  \
     template __global__ void k_re_points<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,   \
                                                 BatchHdr *, const long long *);                  \
     template __global__ void k_re_combine<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,  \
@@ -616,13 +683,14 @@ G3L_INST64(1, 1)
 G3L_INST64(1, 2)
 G3L_INST64(1, 3)
 
-// re-evaluation kernels of a group: 0 = fill, 1 = points, 2 = combine, 3 = batched tail
+// re-evaluation kernels of a group: 0 = fill, 1 = cached u_NFW, 2 = points, 3 = combine,
+// 4 = batched tail
 void *reeval_phase_kernel(int kind, int term, int phase)
 {
 #define G3L_RE_ROW(K, Tm)                                                                       \
-    {(void *)k_re_fill<K, Tm>, (void *)k_re_points<K, Tm>, (void *)k_re_combine<K, Tm>,          \
-     (void *)k_reeval64<K, Tm>}
-    static void *tab[2][3][4] = {{G3L_RE_ROW(0, 1), G3L_RE_ROW(0, 2), G3L_RE_ROW(0, 3)},
+    {(void *)k_re_fill<K, Tm>, (void *)k_re_ucache<K, Tm>, (void *)k_re_points<K, Tm>,           \
+     (void *)k_re_combine<K, Tm>, (void *)k_reeval64<K, Tm>}
+    static void *tab[2][3][5] = {{G3L_RE_ROW(0, 1), G3L_RE_ROW(0, 2), G3L_RE_ROW(0, 3)},
                                  {G3L_RE_ROW(1, 1), G3L_RE_ROW(1, 2), G3L_RE_ROW(1, 3)}};
 #undef G3L_RE_ROW
     return tab[kind][term - 1][phase];

@@ -293,11 +293,6 @@ __device__ __forceinline__ df ln_df(float v)
     return df_add_f(el, logf(m));
 }
 
-// Distinct (l, m, z) variant combinations among the points of one Genz-Malik rule:
-// the centre, 4 axis variants of each of the 3 dimensions, 4 (+-l4, +-l4) pairs of each
-// of the 3 dimension pairs, and the 8 corners.
-constexpr int UC_MAX = 1 + 12 + 12 + 8;
-
 // ------------------------------------------------------------------ per-term models
 struct Child {
     double c64[MAX_DIM + 1];  // FP64 centres: dims of child 0, then child 1's split dim
@@ -457,23 +452,12 @@ struct ModelF {
     // u_NFW calls that depend on one l, one mass and z only: evaluated once per distinct
     // (l, m, z) variant combination of a work item (ucached) and passed to point() in uc[].
     // {l dim, m dim, concentration factor: 0 = 1, 1 = f of hod1, 2 = f of hod2}
-    static constexpr int NF = TERM == 2 ? 4 : 2;
+    static constexpr int NF = ucache_nf(TERM);
     // the 3-halo kernels evaluate their u_NFW per point: measured faster there
     static constexpr bool UC = TERM != 3;
     __host__ __device__ static constexpr int ufun(int f, int k)
     {
-        return KIND == 0 ? (TERM == 1 ? (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1) : (k == 0 ? 1 : k == 1 ? 3 : 2))
-                            : TERM == 2 ? (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1)
-                                           : f == 1 ? (k == 0 ? 1 : k == 1 ? 3 : 2)
-                                           : f == 2 ? (k == 0 ? 0 : k == 1 ? 4 : 1)
-                                                    : (k == 0 ? 1 : k == 1 ? 4 : 2))
-                                        : (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1) : (k == 0 ? 1 : k == 1 ? 4 : 2)))
-                         : (TERM == 1 ? (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1) : (k == 0 ? 1 : k == 1 ? 3 : 0))
-                            : TERM == 2 ? (f == 0 ? (k == 0 ? 1 : k == 1 ? 3 : 0)
-                                           : f == 1 ? (k == 0 ? 0 : k == 1 ? 4 : 1)
-                                           : f == 2 ? (k == 0 ? 1 : k == 1 ? 4 : 0)
-                                                    : (k == 0 ? 0 : k == 1 ? 3 : 1))
-                                        : (f == 0 ? (k == 0 ? 1 : k == 1 ? 3 : 0) : (k == 0 ? 0 : k == 1 ? 4 : 1)));
+        return ucache_fun(KIND, TERM, f, k);
     }
 
     // the cached u_NFW f at slots L (l), M (mass), Z (z), with the expressions of point()
@@ -907,21 +891,7 @@ __global__ void __launch_bounds__(128, MINB) k_evalmx(DevTables T, const IntDesc
     __shared__ uint16_t ucl[NF * UC_MAX];        // variants (l | m << 3 | z << 6) of each
     __shared__ int ucn[NF];
     __shared__ float ucache[WPB][2 * NF * UC_MAX];
-    if (ModelF<KIND, TERM>::UC && threadIdx.x < NF) {  // the distinct (l, m, z) combinations
-        const int f = threadIdx.x;
-        const int dl = ModelF<KIND, TERM>::ufun(f, 0), dm = ModelF<KIND, TERM>::ufun(f, 1);
-        int n = 0;
-        for (int p = 0; p < NP; ++p) {
-            const uint32_t vv = point_variants(DIM, p);
-            const uint32_t key = ((vv >> (3 * dl)) & 7) | (((vv >> (3 * dm)) & 7) << 3) |
-                                 (((vv >> (3 * (DIM - 1))) & 7) << 6);
-            int j = 0;
-            while (j < n && ucl[f * UC_MAX + j] != key) ++j;
-            if (j == n && n < UC_MAX) ucl[f * UC_MAX + n++] = (uint16_t)key;
-            ucidx[f * NP + p] = (uint8_t)(j < UC_MAX ? j : UC_MAX - 1);
-        }
-        ucn[f] = n;
-    }
+    if (ModelF<KIND, TERM>::UC) ucache_tables<KIND, TERM>(ucidx, ucl, ucn);
     const int g = KIND * 3 + TERM - 1;
     for (int p = threadIdx.x; p < NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
     __syncthreads();

@@ -20,6 +20,8 @@ constexpr int MAX_DIM = 7;
 constexpr int NVAR = 7;  // coordinate variants per dimension: c, c-+r2, c-+r4, c-+r5
 constexpr int MAX_HOD_SLOTS = 1024;
 constexpr int NGROUPS = 6;  // kind * 3 + (term - 1)
+constexpr int UC_MAX = 1 + 12 + 12 + 8;  // (l, m, z) variant combinations of one rule
+constexpr int UC_NF_MAX = 4;             // cached u_NFW functions per integrand at most
 
 // status codes (mirror g3l_status)
 enum : int {
@@ -122,7 +124,7 @@ constexpr long long reeval_slot_bytes = 56;  // sizeof(Slot64)
 __host__ __device__ constexpr long long reeval_scratch_group_bytes(int rcap)
 {
     return ((long long)rcap * MAX_DIM * NVAR * reeval_slot_bytes + 255) / 256 * 256 +
-           (long long)rcap * 256 * 8;
+           (long long)rcap * 256 * 8 + (long long)rcap * UC_NF_MAX * UC_MAX * 8;
 }
 
 // Per-call header kept in device memory so one instantiated graph serves any batch.
@@ -150,6 +152,31 @@ struct BatchHdr {
     unsigned long long esc_full; // statistics: whole-rule FP64 re-evaluations queued
     double *dbg;                 // debug: per-point integrand values of one work item
 };
+
+// u_NFW calls of the integrands that depend on one l, one mass and z only.  The points
+// of one Genz-Malik rule take at most UC_MAX distinct (l, m, z) variant combinations
+// (the centre, 4 axis variants of each of the 3 dimensions, 4 (+-l4, +-l4) pairs of each
+// of the 3 dimension pairs, the 8 corners), so these are evaluated once per
+// combination.  ucache_fun(kind, term, f, k): function f's l dimension (k = 0), mass
+// dimension (k = 1) and concentration factor (k = 2: 0 = 1, 1 = f of hod1, 2 = f of hod2).
+__host__ __device__ constexpr int ucache_nf(int term) { return term == 2 ? 4 : 2; }
+__host__ __device__ constexpr int ucache_fun(int kind, int term, int f, int k)
+{
+    // rows {l, m, factor}
+    return kind == 0
+               ? (term == 1 ? (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1) : (k == 0 ? 1 : k == 1 ? 3 : 2))
+                  : term == 2 ? (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1)
+                                 : f == 1 ? (k == 0 ? 1 : k == 1 ? 3 : 2)
+                                 : f == 2 ? (k == 0 ? 0 : k == 1 ? 4 : 1)
+                                          : (k == 0 ? 1 : k == 1 ? 4 : 2))
+                              : (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1) : (k == 0 ? 1 : k == 1 ? 4 : 2)))
+               : (term == 1 ? (f == 0 ? (k == 0 ? 0 : k == 1 ? 3 : 1) : (k == 0 ? 1 : k == 1 ? 3 : 0))
+                  : term == 2 ? (f == 0 ? (k == 0 ? 1 : k == 1 ? 3 : 0)
+                                 : f == 1 ? (k == 0 ? 0 : k == 1 ? 4 : 1)
+                                 : f == 2 ? (k == 0 ? 1 : k == 1 ? 4 : 0)
+                                          : (k == 0 ? 0 : k == 1 ? 3 : 1))
+                              : (f == 0 ? (k == 0 ? 1 : k == 1 ? 3 : 0) : (k == 0 ? 0 : k == 1 ? 4 : 1)));
+}
 
 // Queue region `code` (local slot | whole-rule flag << 30) of integral i, group g, for
 // FP64 re-evaluation in this round.
@@ -192,6 +219,30 @@ __host__ __device__ inline uint32_t point_variants(int dim, int p)
     uint32_t out = 0;
     for (int d = 0; d < dim; ++d) out |= (((gray >> d) & 1u) ? 5u : 6u) << (3 * d);
     return out;
+}
+
+// Combination tables of one rule: ucl[f][j] = variants (l | m << 3 | z << 6) of
+// combination j of function f, ucn[f] their count, ucidx[f][p] the combination of
+// point p.  Built by threads 0..nf-1 of a block.
+template <int KIND, int TERM>
+__device__ inline void ucache_tables(uint8_t *ucidx, uint16_t *ucl, int *ucn)
+{
+    constexpr int DIM = TERM + 4;
+    constexpr int NP = rule_points(DIM);
+    const int f = threadIdx.x;
+    if (f >= ucache_nf(TERM)) return;
+    const int dl = ucache_fun(KIND, TERM, f, 0), dm = ucache_fun(KIND, TERM, f, 1);
+    int n = 0;
+    for (int p = 0; p < NP; ++p) {
+        const uint32_t vv = point_variants(DIM, p);
+        const uint32_t key = ((vv >> (3 * dl)) & 7) | (((vv >> (3 * dm)) & 7) << 3) |
+                             (((vv >> (3 * (DIM - 1))) & 7) << 6);
+        int j = 0;
+        while (j < n && ucl[f * UC_MAX + j] != key) ++j;
+        if (j == n && n < UC_MAX) ucl[f * UC_MAX + n++] = (uint16_t)key;
+        ucidx[f * NP + p] = (uint8_t)(j < UC_MAX ? j : UC_MAX - 1);
+    }
+    ucn[f] = n;
 }
 
 }  // namespace g3l

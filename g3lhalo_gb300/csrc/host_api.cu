@@ -439,16 +439,16 @@ int build_graph_ws(g3l_ctx *c, Workspace &W, int precision, int gmask, bool init
             if (!(gmask & (1 << grp))) continue;
             void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
             cudaGraphNode_t chain = dep;
-            for (int ph = 0; ph < 3; ++ph) {
+            for (int ph = 0; ph < 4; ++ph) {
                 void *fn = reeval_phase_kernel(grp / 3, grp % 3 + 1, ph);
                 cudaGraphNode_t nd;
-                int st = add_kernel(body, &nd, &chain, 1, fn, ph == 2 ? c->nsm : grid128(c, fn), 128,
+                int st = add_kernel(body, &nd, &chain, 1, fn, ph == 3 ? c->nsm : grid128(c, fn), 128,
                                     args);
                 if (st) return st;
                 chain = nd;
             }
             br[nbr++] = chain;
-            void *fn = reeval_phase_kernel(grp / 3, grp % 3 + 1, 3);
+            void *fn = reeval_phase_kernel(grp / 3, grp % 3 + 1, 4);
             int st = add_kernel(body, &br[nbr], &dep, 1, fn, reeval_grid(c, fn), 128, args);
             if (st) return st;
             ++nbr;
@@ -571,9 +571,9 @@ int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
         for (int grp = 0; grp < NGROUPS; ++grp) {
             if (!(gmask & (1 << grp))) continue;
             void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
-            for (int ph = 0; ph < 4; ++ph) {
+            for (int ph = 0; ph < 5; ++ph) {
                 void *fn = reeval_phase_kernel(grp / 3, grp % 3 + 1, ph);
-                const int grid = ph == 2 ? c->nsm : (ph == 3 ? reeval_grid(c, fn) : grid128(c, fn));
+                const int grid = ph == 3 ? c->nsm : (ph == 4 ? reeval_grid(c, fn) : grid128(c, fn));
                 G3L_CK(cudaLaunchKernel(fn, dim3(grid), dim3(128), args, 0, s));
                 ++*launches;
             }
@@ -1993,9 +1993,9 @@ extern "C" int g3l_eval_static(g3l_ctx *c, const g3l_integral *items, int n, int
         for (int g = 0; g < NGROUPS; ++g) {
             if (!(gmask & (1 << g))) continue;
             void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
-            for (int ph = 0; ph < 4; ++ph) {
+            for (int ph = 0; ph < 5; ++ph) {
                 void *fn = reeval_phase_kernel(g / 3, g % 3 + 1, ph);
-                const int grid = ph == 2 ? c->nsm : (ph == 3 ? reeval_grid(c, fn) : grid128(c, fn));
+                const int grid = ph == 3 ? c->nsm : (ph == 4 ? reeval_grid(c, fn) : grid128(c, fn));
                 G3L_CK(cudaLaunchKernel(fn, dim3(grid), dim3(128), args, 0, s));
                 ++launches;
             }
