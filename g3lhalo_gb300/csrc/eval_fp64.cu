@@ -404,6 +404,9 @@ struct Reeval {
     static constexpr int NS = DIM * NVAR;
     static constexpr int NPAD = (NP + 31) / 32 * 32;
     static constexpr int G = KIND * 3 + TERM - 1;
+    // the cached-u_NFW pass pays off for the 2-halo rules (4 of 6 u_NFW per point
+    // cached); for 1h and 3h its extra per-round latency costs more than it saves
+    static constexpr bool UCACHE = TERM == 2;
     __device__ static Slot64 *slots(const Pool &P)
     {
         return (Slot64 *)(P.rscr + (long long)G * P.rscr_group);
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *_
     __shared__ uint16_t ucl[NF * UC_MAX];
     __shared__ int ucn[NF];
     const int m = R::count(P, H);
-    if (m == 0) return;
+    if (m == 0 || !R::UCACHE) return;
     ucache_tables<KIND, TERM>(ucidx, ucl, ucn);
     __syncthreads();
     const int2 *Q = P.esc + H->esc_beg[R::G];
@@ -508,7 +511,7 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
     const int m = R::count(P, H);
     if (m == 0) return;
     for (int p = threadIdx.x; p < R::NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
-    ucache_tables<KIND, TERM>(ucidx, ucl, ucn);
+    if (R::UCACHE) ucache_tables<KIND, TERM>(ucidx, ucl, ucn);
     __syncthreads();
     const int2 *Q = P.esc + H->esc_beg[R::G];
     const Slot64 *SL = R::slots(P);
@@ -527,10 +530,12 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
 #pragma unroll
         for (int dd = 0; dd < DIM; ++dd) sp[dd] = base + dd * NVAR + ((vv >> (3 * dd)) & 7);
         double uc[NF];
+        if (R::UCACHE) {
 #pragma unroll
-        for (int f = 0; f < NF; ++f)
-            uc[f] = UC[((long long)k * UC_NF_MAX + f) * UC_MAX + ucidx[f * R::NP + p]];
-        VL[(long long)k * R::NPAD + p] = Model64<KIND, TERM>::point(T, d, sp, uc);
+            for (int f = 0; f < NF; ++f)
+                uc[f] = UC[((long long)k * UC_NF_MAX + f) * UC_MAX + ucidx[f * R::NP + p]];
+        }
+        VL[(long long)k * R::NPAD + p] = Model64<KIND, TERM>::point(T, d, sp, R::UCACHE ? uc : nullptr);
     }
 }
 
