@@ -39,12 +39,17 @@ sys.path.insert(0, ROOT)
 METRIC = "NNMap evals/s (220 triplets,1h+2h+3h,rtol 1e-4) mixed vs FP64; p50/p99 ms"
 MAX_EVAL = 1_000_000
 RTOL = 1e-4
-# FP32 operations per integrand point of the NNMap 2-halo rule kernel k_evalmx<0,2>:
-# ncu thread-level instruction counts (fadd + fmul + 2 ffma) over every launch of one
-# benchmark evaluation (3.434e11) divided by the points those launches evaluated
-# (2.2005e8).  DRAM traffic per launch from the same capture (read + write).
+# FP32 operations per integrand point of the NNMap 2-halo rule, counted by ncu
+# (thread-level fadd + fmul + 2 ffma over every launch of an evaluation, divided by its
+# points).  Algorithmic count: the integrand with its u_NFW calls de-duplicated within
+# a point, as the kernel evaluated it before sharing u_NFW across the points of a rule
+# (3.434e11 over 2.2005e8 points of the benchmark).  Executed count of the current
+# kernel, which evaluates the (l, m, z) u_NFW once per rule: 8.728e9 over 2 x 4,802,568
+# points of a 24-triplet, maxEval 2e5 case.  DRAM traffic per launch (read + write): the
+# mean over all 58 launches of two evaluations of the benchmark (one-pass capture).
 FLOPS_PER_POINT = {"nnmap_2h": 1561.0}
-DRAM_BYTES_PER_LAUNCH = {"nnmap_2h": 4.03e6}
+EXECUTED_FLOPS_PER_POINT = {"nnmap_2h": 909.0}
+DRAM_BYTES_PER_LAUNCH = {"nnmap_2h": 5.03e6}
 
 
 def parse():
@@ -380,6 +385,9 @@ def main():
                                "frac": ach / p32, "traffic": DRAM_BYTES_PER_LAUNCH["nnmap_2h"],
                                "traffic_unit": "bytes per launch (ncu dram read+write)",
                                "flops_per_point": fpp,
+                               "executed_flops_per_point": EXECUTED_FLOPS_PER_POINT["nnmap_2h"],
+                               "executed_tflops": pts_g * EXECUTED_FLOPS_PER_POINT["nnmap_2h"] /
+                                                  (ms_g * 1e-3) / 1e12,
                                "peak_source": "measured FP32 FMA rate of this device "
                                               "(g3l_measure_peaks, CUDA events); the measured-peaks "
                                               "file holds only HBM and bf16 figures", **kern}

@@ -472,10 +472,10 @@ __global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *_
     __shared__ uint8_t ucidx[NF * R::NP];
     __shared__ uint16_t ucl[NF * UC_MAX];
     __shared__ int ucn[NF];
+    __shared__ uint8_t ucmap[NF * 343];
     const int m = R::count(P, H);
     if (m == 0 || !R::UCACHE) return;
-    ucache_tables<KIND, TERM>(ucidx, ucl, ucn);
-    __syncthreads();
+    ucache_tables<KIND, TERM>(ucidx, ucl, ucn, ucmap);
     const int2 *Q = P.esc + H->esc_beg[R::G];
     const Slot64 *SL = R::slots(P);
     double *UC = R::ucv(P);
@@ -508,10 +508,11 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
     __shared__ uint8_t ucidx[NF * R::NP];
     __shared__ uint16_t ucl[NF * UC_MAX];
     __shared__ int ucn[NF];
+    __shared__ uint8_t ucmap[NF * 343];
     const int m = R::count(P, H);
     if (m == 0) return;
     for (int p = threadIdx.x; p < R::NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
-    if (R::UCACHE) ucache_tables<KIND, TERM>(ucidx, ucl, ucn);
+    if (R::UCACHE) ucache_tables<KIND, TERM>(ucidx, ucl, ucn, ucmap);
     __syncthreads();
     const int2 *Q = P.esc + H->esc_beg[R::G];
     const Slot64 *SL = R::slots(P);

@@ -891,7 +891,8 @@ __global__ void __launch_bounds__(128, MINB) k_evalmx(DevTables T, const IntDesc
     __shared__ uint16_t ucl[NF * UC_MAX];        // variants (l | m << 3 | z << 6) of each
     __shared__ int ucn[NF];
     __shared__ float ucache[WPB][2 * NF * UC_MAX];
-    if (ModelF<KIND, TERM>::UC) ucache_tables<KIND, TERM>(ucidx, ucl, ucn);
+    __shared__ uint8_t ucmap[NF * 343];
+    if (ModelF<KIND, TERM>::UC) ucache_tables<KIND, TERM>(ucidx, ucl, ucn, ucmap);
     const int g = KIND * 3 + TERM - 1;
     for (int p = threadIdx.x; p < NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
     __syncthreads();

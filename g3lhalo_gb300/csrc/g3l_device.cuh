@@ -222,27 +222,55 @@ __host__ __device__ inline uint32_t point_variants(int dim, int p)
 }
 
 // Combination tables of one rule: ucl[f][j] = variants (l | m << 3 | z << 6) of
-// combination j of function f, ucn[f] their count, ucidx[f][p] the combination of
-// point p.  Built by threads 0..nf-1 of a block.
+// combination j of function f (in key order), ucn[f] their count, ucidx[f][p] the
+// combination of point p.  Block-cooperative (every thread of the block calls it; it
+// synchronises); map is NF * 343 bytes of shared scratch.
 template <int KIND, int TERM>
-__device__ inline void ucache_tables(uint8_t *ucidx, uint16_t *ucl, int *ucn)
+__device__ inline void ucache_tables(uint8_t *ucidx, uint16_t *ucl, int *ucn, uint8_t *map)
 {
     constexpr int DIM = TERM + 4;
     constexpr int NP = rule_points(DIM);
-    const int f = threadIdx.x;
-    if (f >= ucache_nf(TERM)) return;
-    const int dl = ucache_fun(KIND, TERM, f, 0), dm = ucache_fun(KIND, TERM, f, 1);
-    int n = 0;
-    for (int p = 0; p < NP; ++p) {
+    constexpr int NF = ucache_nf(TERM);
+    auto key_of = [](int f, int p) -> uint32_t {
+        const int dl = ucache_fun(KIND, TERM, f, 0), dm = ucache_fun(KIND, TERM, f, 1);
         const uint32_t vv = point_variants(DIM, p);
-        const uint32_t key = ((vv >> (3 * dl)) & 7) | (((vv >> (3 * dm)) & 7) << 3) |
-                             (((vv >> (3 * (DIM - 1))) & 7) << 6);
-        int j = 0;
-        while (j < n && ucl[f * UC_MAX + j] != key) ++j;
-        if (j == n && n < UC_MAX) ucl[f * UC_MAX + n++] = (uint16_t)key;
-        ucidx[f * NP + p] = (uint8_t)(j < UC_MAX ? j : UC_MAX - 1);
+        return ((vv >> (3 * dl)) & 7) | (((vv >> (3 * dm)) & 7) << 3) |
+               (((vv >> (3 * (DIM - 1))) & 7) << 6);
+    };
+    for (int i = threadIdx.x; i < NF * 343; i += blockDim.x) map[i] = 0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < NF * NP; t += blockDim.x) {
+        const int f = t / NP, p = t - f * NP;
+        const uint32_t k = key_of(f, p);
+        map[f * 343 + (k & 7) + 7 * (((k >> 3) & 7) + 7 * (k >> 6))] = 1;
     }
-    ucn[f] = n;
+    __syncthreads();
+    if (threadIdx.x < 32) {  // number the present keys in key order
+        const int lane = threadIdx.x;
+        for (int f = 0; f < NF; ++f) {
+            int base = 0;
+            for (int c = 0; c < 343; c += 32) {
+                const int q = c + lane;
+                const bool on = q < 343 && map[f * 343 + q];
+                const unsigned b = __ballot_sync(0xffffffffu, on);
+                const int idx = base + __popc(b & ((1u << lane) - 1u));
+                if (on && idx < UC_MAX) {
+                    map[f * 343 + q] = (uint8_t)idx;
+                    const int vl = q % 7, vm = (q / 7) % 7, vz = q / 49;
+                    ucl[f * UC_MAX + idx] = (uint16_t)(vl | (vm << 3) | (vz << 6));
+                }
+                base += __popc(b);
+            }
+            if (lane == 0) ucn[f] = base < UC_MAX ? base : UC_MAX;
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < NF * NP; t += blockDim.x) {
+        const int f = t / NP, p = t - f * NP;
+        const uint32_t k = key_of(f, p);
+        ucidx[t] = map[f * 343 + (k & 7) + 7 * (((k >> 3) & 7) + 7 * (k >> 6))];
+    }
+    __syncthreads();
 }
 
 }  // namespace g3l
