@@ -453,8 +453,8 @@ struct ModelF {
     // (l, m, z) variant combination of a work item (ucached) and passed to point() in uc[].
     // {l dim, m dim, concentration factor: 0 = 1, 1 = f of hod1, 2 = f of hod2}
     static constexpr int NF = ucache_nf(TERM);
-    // the 3-halo kernels evaluate their u_NFW per point: measured faster there
-    static constexpr bool UC = TERM != 3;
+    // cache the (l, m, z) u_NFW for every term (measured faster for all six)
+    static constexpr bool UC = true;
     __host__ __device__ static constexpr int ufun(int f, int k)
     {
         return ucache_fun(KIND, TERM, f, k);
@@ -528,8 +528,8 @@ struct ModelF {
                 const SlotF &M1 = *s[3], &M2 = *s[4], &M3 = *s[5];
                 const float m1 = M1.f[0], m2 = M2.f[0], m3 = M3.f[0];
                 const float u3 = u_nfw32(k3 * cbrtf(m3 * k200), __ldg(T.f_conc + zt * Nm + M3.i1), sa, small);
-                const float u1 = u_nfw32(k1 * cbrtf(m1 * k200), f1 * __ldg(T.f_conc + zt * Nm + M1.i1), sa, small);
-                const float u2 = u_nfw32(k2 * cbrtf(m2 * k200), f2 * __ldg(T.f_conc + zt * Nm + M2.i1), sa, small);
+                const float u1 = UC ? uc[0] : u_nfw32(k1 * cbrtf(m1 * k200), f1 * __ldg(T.f_conc + zt * Nm + M1.i1), sa, small);
+                const float u2 = UC ? uc[1] : u_nfw32(k2 * cbrtf(m2 * k200), f2 * __ldg(T.f_conc + zt * Nm + M2.i1), sa, small);
                 const float G1 = M1.f[1] + M1.f[2] * u1, G2 = M2.f[3] + M2.f[4] * u2;
                 const float Bi = bi32(T, d, C, ch, sdim, vv, zr, k1, k2, k3, cphi, L1, L2, ties);
                 const float HB = (__ldg(T.f_hmf + zr * Nm + M1.i0) * m1) *
@@ -580,9 +580,9 @@ struct ModelF {
                 const float ra = cbrtf(m1 * k200), rb = cbrtf(m2 * k200);
                 const float ca = __ldg(T.f_conc + zt * Nm + M1.i1);
                 const float cb = __ldg(T.f_conc + zt * Nm + M2.i1);
-                const float u2_1 = u_nfw32(k2 * ra, ca, sa, small);
+                const float u2_1 = UC ? uc[0] : u_nfw32(k2 * ra, ca, sa, small);
                 const float u3_2 = u_nfw32(k3 * rb, cb, sa, small);
-                const float G = M3.f[1] + M3.f[2] * u_nfw32(k1 * rb, f * cb, sa, small);
+                const float G = M3.f[1] + M3.f[2] * (UC ? uc[1] : u_nfw32(k1 * rb, f * cb, sa, small));
                 const float Bi = bi32(T, d, C, ch, sdim, vv, zr, k1, k2, k3, cphi, L1, L2, ties);
                 const float HB = (__ldg(T.f_hmf + zr * Nm + M1.i0) * m1 * m1) *
                                  (__ldg(T.f_hmf + zr * Nm + M2.i0) * m2 * m2) *

@@ -1176,8 +1176,8 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
     c->opt.unc_eps_val = 5e-6;
     c->opt.unc_eps_sel = 5e-5;
     // register-budget variant of the rule kernels per kind x term (autotuned default:
-    // 6 blocks per SM for NNMap 1h, 8 for the others)
-    for (int g = 0; g < NGROUPS; ++g) c->opt.evalmx_variant[g] = g == 0 ? 1 : 2;
+    // 6 blocks per SM for the 1-halo terms, 8 for the others)
+    for (int g = 0; g < NGROUPS; ++g) c->opt.evalmx_variant[g] = g % 3 == 0 ? 1 : 2;
 
     DevTables &T = c->T;
     T.Nz = t->Nz;

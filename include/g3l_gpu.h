@@ -196,7 +196,7 @@ typedef struct g3l_options {
     double unc_eps_sel;
     /* Register budget of the mixed-precision rule kernel per kind x term
      * (kind * 3 + term - 1): 0, 1, 2 = 4, 6, 8 blocks per SM (128, 80, 64 registers
-     * per thread).  Set by g3l_autotune; default 1 for NNMap 1h, 2 for the others. */
+     * per thread).  Set by g3l_autotune; default 1 for the 1-halo terms, 2 for the others. */
     int evalmx_variant[6];
 } g3l_options;
 int g3l_get_options(g3l_ctx *ctx, g3l_options *opt);
