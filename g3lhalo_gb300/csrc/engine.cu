@@ -15,7 +15,7 @@
 //              independent of thread scheduling.
 //   k_scan   : prefix sum of the per-integral pop counts -> flat work list; sets
 //              the graph's WHILE condition (no host round trip).
-//   k_eval*  : cut + rule evaluation (eval_fp64.cu / eval_mixed.cu).
+//   k_eval*  : cut + rule evaluation (eval_fp64.cu / evalmx_impl.cuh).
 // Compiled with -fmad=false.
 #include <cuda_runtime.h>
 

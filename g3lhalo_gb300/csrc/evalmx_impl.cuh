@@ -1,9 +1,10 @@
 #pragma once
-// eval_mixed.cu -- mixed-precision rule evaluation: FP32 integrand, wide accumulation.
+// evalmx_impl.cuh -- mixed-precision rule evaluation: FP32 integrand, wide accumulation
+// (instantiated in evalmx_k0.cu and evalmx_k1.cu).
 //
 // Same work decomposition as eval_fp64.cu (one warp cuts one parent region and
 // applies the Genz-Malik 7/5 rule to both children), with the arithmetic
-// rearranged for a GPU whose FP64 rate is 1/58 of its FP32 rate:
+// rearranged for a GPU whose FP64 rate is ~1/60 of its FP32 rate:
 //  * Region centres stay FP64 in HBM; each is split into a double-float with
 //    integer operations, and the 7 coordinate variants c, c-+lambda h of every
 //    dimension are formed as double-floats (~48-bit mantissas).
@@ -22,6 +23,9 @@
 //    g(a1) - g(a2) cos(a1 c) + (f(a2) - 1/a2) sin(a1 c) with f(x) - 1/x
 //    evaluated from the difference polynomial.  An FP64 branch remains for
 //    a1 below a threshold (option; counted).
+//  * The u_NFW calls that depend on one l, one mass and z only are evaluated once
+//    per distinct (l, m, z) variant combination of the work item (at most 33 per
+//    child, against 93-241 points) and read by the points.
 //  * Rule sums, fourth differences and the 7th/5th-degree combination are
 //    double-float; the final value and error are formed in FP64 by four lanes
 //    at once.
@@ -644,8 +648,10 @@ __device__ __forceinline__ df hw_sum(df a)
 
 // The bound on the FP32 error of one point value has a relative part (the FP32
 // chain) and an absolute part (values so small that intermediate products may
-// have lost range): T.unc_eps |v| + T.unc_abs.  A decision is escalated to FP64
-// only if its region could move the integral by more than T.tau_impact of it.
+// have lost range): T.unc_eps |v| + T.unc_abs.  A split the bounds do not settle is
+// flagged (bit 7 of split) when the region's error exceeds T.tau_impact of the
+// integral (default 0: always); the selection kernel has it re-taken in FP64 if the
+// region is cut.  The error estimate's bound (unc) decides selection boundaries.
 
 template <int KIND, int TERM>
 __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, double Vcur,

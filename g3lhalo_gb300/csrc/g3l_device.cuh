@@ -57,7 +57,7 @@ struct DevTables {
     const unsigned long long *tie_m_bits;
     const int *tie_m_round, *tie_m_trunc;
     int n_tie_m;
-    // mixed-precision path: FP32 tables in scaled units (see eval_mixed.cu)
+    // mixed-precision path: FP32 tables in scaled units (see evalmx_impl.cuh)
     const float *f_hmf, *f_bh, *f_conc, *f_plin;  // [Nz*Nm] x3, [Nz*Nk]
     const float *f_zA, *f_zB, *f_kw, *f_k200;      // [Nz]
     const float *f_nbar;                           // [slot][Nz]
