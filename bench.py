@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--triplets", type=int, default=0)
     ap.add_argument("--host-loop", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-config2", action="store_true")
     # batched fit sweep: this many HOD vectors in one launch (0 = skip)
     ap.add_argument("--sweep", type=int, default=16)
     return ap.parse_args()
@@ -222,6 +223,39 @@ def sweep_leg(G, ctx, trip, hods, n_hod, max_eval):
             "rounds": st["rounds"], "status_ok": bool((r["status"] == 0).all()),
             "workload": "%d seeded HOD vectors (the fit-sweep box) x 220 triplets x 1h+2h+3h, "
                         "rtol 1e-4, maxEval %d, one g3l_eval call" % (n_hod, max_eval)}
+
+
+def config2_leg(G, trip, max_eval, reps=3):
+    """NMapMap 1h+2h+3h plus two-population NNMap (second HOD and a second lens
+    distribution, Gaussian mu 0.5 sigma 0.07) on all 220 triplets: 1320 integrals per
+    evaluation, mixed precision against the FP64 form."""
+    from g3lhalo_gb300 import workloads as W
+    from g3lhalo_gb300.tables import make_tables
+    T2 = make_tables(Nz=64, Nm=128, Nk=256, lens2=(0.5, 0.07))
+    c2 = G.Context(T2)
+    c2.set_hod(0, W.hod_default())
+    c2.set_hod(1, W.hod_second())
+    specs = [(G.NMAPMAP, t, 0, 0, tuple(th), RTOL, max_eval) for th in trip for t in (1, 2, 3)]
+    specs += [(G.NNMAP, t, 0, 1, tuple(th), RTOL, max_eval) for th in trip for t in (1, 2, 3)]
+    c2.eval(specs, G.MIXED)
+    ms = []
+    for _ in range(reps):
+        r = c2.eval(specs, G.MIXED)
+        ms.append(c2.stats()["device_ms"])
+    st = c2.stats()
+    r64 = c2.eval(specs, G.FP64)
+    ms64 = c2.stats()["device_ms"]
+    rel = np.abs(r["val"] - r64["val"]) / np.abs(r64["val"])
+    c2.close()
+    return {"integrals": len(specs), "evals_per_s": 1e3 / float(np.mean(ms)),
+            "ms": float(np.mean(ms)), "fp64_evals_per_s": 1e3 / ms64,
+            "mixed_over_fp64": ms64 / float(np.mean(ms)),
+            "max_rel_vs_fp64": float(rel.max()), "terms_over_1e-4": int((rel > 1e-4).sum()),
+            "neval_identical": bool(np.array_equal(r["neval"], r64["neval"])),
+            "small_arg_fp64_evaluations": int(st["small_arg_fp64"]),
+            "workload": "NMapMap (HOD 1, lens 1) + NNMap two populations (HOD 1 and 2, lens "
+                        "1 and lens 2 = Gaussian 0.5/0.07), 220 triplets x 3 terms each, rtol "
+                        "1e-4, maxEval %d" % max_eval}
 
 
 def serving_leg(G, ctx, trip, hods, args, n_req=48, rate=12.0, seed=7):
@@ -399,6 +433,8 @@ def main():
             out["serving"] = serving_leg(G, ctx, trip, hods, args)
         if args.sweep:
             out["sweep"] = sweep_leg(G, ctx, trip, hods, args.sweep, args.max_eval)
+        if not args.no_config2:
+            out["nmapmap_twopop"] = config2_leg(G, trip, args.max_eval)
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_sample(T, trip, hods[last_hod], args.max_eval, 4)
         out["config"] = config(len(trip), args.max_eval)
