@@ -101,6 +101,7 @@ def lib():
             L.g3l_ctx_destroy.argtypes = [C.c_void_p]
             L.g3l_set_hod.argtypes = [C.c_void_p, C.c_int, _dp]
             L.g3l_set_correlation.argtypes = [C.c_void_p, C.c_double, C.c_double]
+            L.g3l_set_scaling.argtypes = [C.c_void_p, C.c_int, _dp]
             L.g3l_get_densities.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
             L.g3l_eval.argtypes = [C.c_void_p, C.POINTER(Integral), C.c_int, C.c_int,
                                    C.POINTER(Result)]
@@ -220,6 +221,16 @@ class Context:
 
     def set_correlation(self, A, eps):
         _check(lib().g3l_set_correlation(self.h, A, eps))
+
+    def set_scaling(self, slot, scaling=None):
+        """Satellite-variance rescaling s[j] (j < Nm) of a HOD slot; None resets s = 1."""
+        if scaling is None:
+            _check(lib().g3l_set_scaling(self.h, slot, None))
+            return
+        a = np.ascontiguousarray(scaling, dtype=np.float64)
+        if a.shape != (self.tables.Nm,):
+            raise ValueError("scaling needs Nm values")
+        _check(lib().g3l_set_scaling(self.h, slot, _ptr(a)))
 
     def densities(self, slot):
         rho = np.zeros(self.tables.Nz)
@@ -391,17 +402,24 @@ class NNMapModel:
     case where both type slots point to one HOD (src/HOD.cu:82).
     The per-term methods use the reference's hard-coded budgets (maxEval 5e6,
     rtol 1e-3, 1e-3, 1e-4; src/NNMap_Model.cu:318,343,368) unless overridden.
+    scaling = (scaling1, scaling2) takes the reference's SCALING constructor
+    (src/NNMap_Model.cu:103-200): its same-population pair count reads scaling1 for
+    both types (src/NNMap_Model.cu:563,808; src/HOD.cu:86-87 use scale1 only), so
+    scaling1 goes to both HOD slots and scaling2 is accepted and unused, as there.
     """
 
     RTOL = {1: 1e-3, 2: 1e-3, 3: 1e-4}
     MAX_EVAL = 5_000_000
 
     def __init__(self, tables, hod1, hod2=None, A=0.0, epsilon=0.0, precision=FP64, device=0,
-                 clamp_k=True, ctx=None):
+                 clamp_k=True, ctx=None, scaling=None):
         self.ctx = ctx or Context(tables, device, clamp_k)
         self.precision = precision
         self.updateHODs(hod1, hod2)
         self.ctx.set_correlation(A, epsilon)
+        s1 = None if scaling is None else scaling[0]
+        self.ctx.set_scaling(0, s1)
+        self.ctx.set_scaling(1, s1)
 
     def updateHODs(self, hod1, hod2=None):
         same = hod2 is None or hod2 is hod1

@@ -44,7 +44,10 @@ struct Model64 {
             if (KIND == 0) {
                 S.a[3] = ncen64(h2, m);
                 S.a[4] = nsat64(h2, m);
-                S.a[5] = nsatnsat64(h1, h2, d.same, T.A, T.eps, m);
+                // rescaling s of the hod1 slot at this mass's rounded bin
+                // (src/NNMap_Model.cu:563,808)
+                S.a[5] = nsatnsat64(h1, h2, d.same, T.A, T.eps, m,
+                                    __ldg(T.scale + (size_t)d.hod1 * T.Nm + S.i0));
             }
         } else {  // z
             S.a[0] = x;

@@ -366,8 +366,8 @@ struct ModelF {
                 const float e2 = erfcf(-((x.hi - h2[2]) + (x.lo - h2[3])) * h2[4]);
                 S.f[3] = 0.5f * h2[1] * e2;
                 S.f[4] = 0.5f * e2 * exp10f(h2[7] * ((x.hi - h2[5]) + (x.lo - h2[6])));
-                if (d.same) {
-                    S.f[5] = S.f[2] * S.f[2];
+                if (d.same) {  // (N_s + s^2 - 1) N_s, s^2 - 1 per slot and mass bin
+                    S.f[5] = (S.f[2] + __ldg(T.f_scale + d.hod1 * T.Nm + ir)) * S.f[2];
                 } else {
                     float n12 = S.f[2] * S.f[4];
                     float r = n12 + T.fA * exp10f(T.feps * xm) * sqrtf(n12);

@@ -52,6 +52,8 @@ struct DevTables {
     const double *P_lin;                             // [Nz*Nk]
     const double *nbar;                              // [slot][Nz]
     const double *hod;                               // [slot][6] f, alpha, Mth, sigma, M', beta
+    const double *scale;   // [slot][Nm] satellite-variance rescaling s (1 = none)
+    const float *f_scale;  // [slot][Nm] s^2 - 1 in FP32 (mixed path)
     // exact nearest-bin indices of the tie-prone m-centre values, resolved on the
     // host with the reference's own expression (sorted by bit pattern)
     const unsigned long long *tie_m_bits;

@@ -109,7 +109,8 @@ struct g3l_ctx {
     double A = 0, eps = 0;
     DevTables T{};
     std::vector<void *> allocs;
-    double *d_hod = nullptr, *d_nbar = nullptr;
+    double *d_hod = nullptr, *d_nbar = nullptr, *d_scale = nullptr;
+    float *d_fscale = nullptr;
     // mixed path
     float *d_fnbar = nullptr, *d_fhodp = nullptr;
     std::vector<double> sn;  // per-slot n_bar scale
@@ -1215,6 +1216,20 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
     G3L_CK(cudaMemset(c->d_nbar, 0, sizeof(double) * MAX_HOD_SLOTS * Nz));
     T.hod = c->d_hod;
     T.nbar = c->d_nbar;
+    // satellite-variance rescaling per slot, s = 1 (FP32: s^2 - 1 = 0) until set
+    st |= dalloc(&c->d_scale, (size_t)MAX_HOD_SLOTS * Nm);
+    st |= dalloc(&c->d_fscale, (size_t)MAX_HOD_SLOTS * Nm);
+    if (st) return st;
+    c->allocs.push_back(c->d_scale);
+    c->allocs.push_back(c->d_fscale);
+    {
+        std::vector<double> ones((size_t)MAX_HOD_SLOTS * Nm, 1.0);
+        G3L_CK(cudaMemcpy(c->d_scale, ones.data(), ones.size() * sizeof(double),
+                          cudaMemcpyHostToDevice));
+    }
+    G3L_CK(cudaMemset(c->d_fscale, 0, sizeof(float) * MAX_HOD_SLOTS * Nm));
+    T.scale = c->d_scale;
+    T.f_scale = c->d_fscale;
     // tie-prone mass-centre indices
     host::TieTable tt = host::build_m_ties(c->B);
     unsigned long long *tb;
@@ -1327,6 +1342,33 @@ int g3l_set_correlation(g3l_ctx *c, double A, double eps)
         cudaGraphDestroy(g.graph);
     }
     c->graphs.clear();
+    return G3L_OK;
+}
+
+int g3l_set_scaling(g3l_ctx *c, int slot, const double *scaling)
+{
+    if (!c || slot < 0 || slot >= MAX_HOD_SLOTS) {
+        host::set_error("g3l_set_scaling: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    const int Nm = c->B.Nm;
+    std::vector<double> s(Nm, 1.0);
+    if (scaling) {
+        for (int j = 0; j < Nm; ++j)
+            if (!std::isfinite(scaling[j])) {
+                host::set_error("g3l_set_scaling: non-finite value");
+                return G3L_ERR_INVALID;
+            }
+        std::copy(scaling, scaling + Nm, s.begin());
+    }
+    std::vector<float> q(Nm);
+    for (int j = 0; j < Nm; ++j) q[j] = (float)(s[j] * s[j] - 1.0);
+    G3L_CK(cudaSetDevice(c->device));
+    G3L_CK(cudaMemcpyAsync(c->d_scale + (size_t)Nm * slot, s.data(), Nm * sizeof(double),
+                           cudaMemcpyHostToDevice, c->stream));
+    G3L_CK(cudaMemcpyAsync(c->d_fscale + (size_t)Nm * slot, q.data(), Nm * sizeof(float),
+                           cudaMemcpyHostToDevice, c->stream));
+    G3L_CK(cudaStreamSynchronize(c->stream));
     return G3L_OK;
 }
 

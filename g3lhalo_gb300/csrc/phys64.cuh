@@ -113,10 +113,11 @@ __device__ __forceinline__ double ncen64(const double *h, double m)
 {
     return 0.5 * h[1] * (1 + erf(log(m / h[2]) / h[3] / 1.414213562));
 }
+// scale1: satellite-variance rescaling (1 = none); the reference reads scale1 only
+// (src/HOD.cu:78-94)
 __device__ __forceinline__ double nsatnsat64(const double *h1, const double *h2, int same,
-                                             double A, double eps, double m)
+                                             double A, double eps, double m, double scale1)
 {
-    const double scale1 = 1;
     double Ns1 = nsat64(h1, m);
     if (same) return (Ns1 + scale1 * scale1 - 1) * Ns1;
     double Ns2 = nsat64(h2, m);

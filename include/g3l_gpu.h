@@ -105,6 +105,14 @@ int g3l_set_hod(g3l_ctx *ctx, int slot, const double params[6]);
 int g3l_max_hod_slots(void);
 /* Satellite-pair correlation parameters A, epsilon (src/HOD.cu:90). */
 int g3l_set_correlation(g3l_ctx *ctx, double A, double epsilon);
+/* Satellite-variance rescaling of HOD slot `slot` (the reference's SCALING build:
+ * src/NNMap_Model.cu:103-200, src/NNMap_Model.h:59-62): scaling[j], j < Nm, at the
+ * mass grid m_j.  In the same-population branch of NNMap 1h and 2h the satellite-
+ * pair count becomes (N_s + s^2 - 1) N_s with s = scaling[round mass index] of the
+ * item's hod1 slot (src/HOD.cu:78-87, src/NNMap_Model.cu:563,808).  NULL resets the
+ * slot to s = 1 (no rescaling, the default).  Finite values only.  Like a HOD slot,
+ * it must not change while a queued or running request uses the slot. */
+int g3l_set_scaling(g3l_ctx *ctx, int slot, const double *scaling);
 /* n_bar(z) of a slot and rho_bar(z) as computed by g3l_set_hod ([Nz] each). */
 int g3l_get_densities(g3l_ctx *ctx, int slot, double *rho_bar, double *n_bar);
 

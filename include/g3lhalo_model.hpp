@@ -26,7 +26,12 @@
  *    them; the caller's arrays need not outlive the model here);
  *  - the integrand runs in mixed precision by default (every term within 1e-4 of the
  *    all-FP64 form); setPrecision(G3L_FP64) selects the all-FP64 form;
- *  - calculateAll integrates every triplet and term in one device launch.
+ *  - calculateAll integrates every triplet and term in one device launch;
+ *  - the SCALING constructor is always declared (the reference's needs -DSCALING,
+ *    src/NNMap_Model.h:130-166); it copies scaling1 to the device for both HOD slots,
+ *    which is what the reference computes (its same-population pair count reads only
+ *    scaling1, src/NNMap_Model.cu:563,808, src/HOD.cu:86-87), and does not free() the
+ *    caller's arrays as the reference's destructor does (src/NNMap_Model.cu:231-234).
  */
 #ifndef G3LHALO_MODEL_HPP
 #define G3LHALO_MODEL_HPP
@@ -147,6 +152,24 @@ class NNMap_Model {
         updateHODs(hod1_, hod2_);
     }
 
+    /// The reference's SCALING constructor (src/NNMap_Model.cu:103-200): satellite-
+    /// variance rescaling per mass bin, [Nbins] each
+    NNMap_Model(Cosmology *cosmology_, const double &zmin_, const double &zmax_,
+                const double &kmin_, const double &kmax_, const double &mmin_,
+                const double &mmax_, const int &Nbins_, double *g_, double *p_lens1_,
+                double *p_lens2_, double *w_, double *dwdz_, double *hmf_, double *P_lin_,
+                double *b_h_, double *concentration_, double *scaling1_, double *scaling2_,
+                HOD *hod1_, HOD *hod2_, double A_, double epsilon_)
+        : NNMap_Model(cosmology_, zmin_, zmax_, kmin_, kmax_, mmin_, mmax_, Nbins_, g_, p_lens1_,
+                      p_lens2_, w_, dwdz_, hmf_, P_lin_, b_h_, concentration_, hod1_, hod2_, A_,
+                      epsilon_)
+    {
+        scaling1 = scaling1_;
+        scaling2 = scaling2_;
+        if (!status_) status_ = g3l_set_scaling(eng_.ctx_, 0, scaling1_);
+        if (!status_) status_ = g3l_set_scaling(eng_.ctx_, 1, scaling1_);
+    }
+
     /// New HODs: recomputes n_bar(z) for both (src/NNMap_Model.cu:244-297)
     void updateHODs(HOD *hod1_, HOD *hod2_)
     {
@@ -221,6 +244,7 @@ class NNMap_Model {
     int Nbins;
     double A, epsilon;
     HOD *hod1 = nullptr, *hod2 = nullptr;
+    double *scaling1 = nullptr, *scaling2 = nullptr;  // SCALING constructor only
 
   private:
     // type 1 -> slot 0, type 2 -> slot 1; one HOD object for both types -> one slot,

@@ -25,6 +25,16 @@ for f in HOD generalFunctions NNMap_Model NMapMap_Model; do
     nvcc $NVF -c "$REF/$f.cu" -o "$OUT/obj/$f.o" 2> "$OUT/obj/$f.log" & pids+=($!)
 done
 nvcc $NVF -c "$HERE/ref_harness.cu" -o "$OUT/obj/ref_harness.o" & pids+=($!)
+# the SCALING build (satellite-variance rescaling, src/Makefile:17-21): NNMap model only
+mkdir -p "$OUT/obj_scaling"
+nvcc $NVF -DSCALING=1 -c "$REF/NNMap_Model.cu" -o "$OUT/obj_scaling/NNMap_Model.o" \
+    2> "$OUT/obj_scaling/NNMap_Model.log" & pids+=($!)
+nvcc $NVF -DSCALING=1 -c "$HERE/ref_harness.cu" -o "$OUT/obj_scaling/ref_harness.o" & pids+=($!)
 for p in "${pids[@]}"; do wait "$p"; done
 nvcc -shared -rdc=true -Xcompiler -fopenmp "$OUT"/obj/*.o -o "$OUT/libg3lref.so"
 echo "built $OUT/libg3lref.so"
+common=()
+for f in hcubature Cosmology Params HOD generalFunctions; do common+=("$OUT/obj/$f.o"); done
+nvcc -shared -rdc=true -Xcompiler -fopenmp "${common[@]}" "$OUT"/obj_scaling/*.o \
+    -o "$OUT/libg3lref_scaling.so"
+echo "built $OUT/libg3lref_scaling.so"

@@ -155,11 +155,11 @@ double orc_ncen(const orc_hod *h, double m)
 {
     return 0.5 * h->alpha * (1 + erf(log(m / h->mth) / h->sigma / 1.414213562));
 }
-/* satellite pairs (src/HOD.cu:78-94); same_type mirrors the pointer test. */
+/* satellite pairs (src/HOD.cu:78-94); same_type mirrors the pointer test.  scale1 is
+ * the satellite-variance rescaling (1 without one); the reference never reads scale2. */
 static double nsat_nsat(double m, const orc_hod *h1, const orc_hod *h2, int same_type,
-                        double A, double eps)
+                        double A, double eps, double scale1)
 {
-    const double scale1 = 1;
     double Ns1 = orc_nsat(h1, m);
     if (same_type) return (Ns1 + scale1 * scale1 - 1) * Ns1;
     double Ns2 = orc_nsat(h2, m);
@@ -213,13 +213,13 @@ static double G_g(const orc_model *M, double k, double m, double z, const orc_ho
     return Nc + Ns * orc_u_nfw(M, k, m, z, h->f);
 }
 static double G_gg(const orc_model *M, double k1, double k2, double m, double z,
-                   const orc_hod *h1, const orc_hod *h2, int same_type)
+                   const orc_hod *h1, const orc_hod *h2, int same_type, double scale1)
 {
     double Nc1 = orc_ncen(h1, m);
     double Nc2 = orc_ncen(h2, m);
     double Ns1 = orc_nsat(h1, m);
     double Ns2 = orc_nsat(h2, m);
-    double Nss = nsat_nsat(m, h1, h2, same_type, M->A, M->eps);
+    double Nss = nsat_nsat(m, h1, h2, same_type, M->A, M->eps, scale1);
     double f1 = h1->f, f2 = h2->f;
     return Nc1 * Ns2 * orc_u_nfw(M, k2, m, z, f2) + Nc2 * Ns1 * orc_u_nfw(M, k1, m, z, f1) +
            Nss * orc_u_nfw(M, k1, m, z, f1) * orc_u_nfw(M, k2, m, z, f2);
@@ -234,6 +234,8 @@ static double nnm_1h(const orc_model *M, const double th[3], double l1, double l
 {   /* src/NNMap_Model.cu:544-593 */
     int z_ix = (int)round(z_arg(M, z));
     int m_ix = (int)round(m_arg(M, m));
+    /* SCALING build: scale1 = scaling1[m_ix] (src/NNMap_Model.cu:563) */
+    double scale1 = M->scaling1 ? M->scaling1[m_ix] : 1;
     double nbar1 = n_bar1[z_ix];
     double nbar2 = n_bar2[z_ix];
     double w_ = M->w[z_ix];
@@ -243,7 +245,7 @@ static double nnm_1h(const orc_model *M, const double th[3], double l1, double l
     double k3 = l3 / w_;
     double Bggd = 1. / nbar1 / nbar2 / M->rho_bar[z_ix] * M->hmf[z_ix * M->Nm + m_ix] * m *
                   orc_u_nfw(M, k3, m, z, 1);
-    Bggd *= G_gg(M, k1, k2, m, z, h1, h2, same_type);
+    Bggd *= G_gg(M, k1, k2, m, z, h1, h2, same_type, scale1);
     double bggk = Bggd / M->dwdz[z_ix] * M->g[z_ix] * M->p1[z_ix] * M->p2[z_ix] / w_ / w_ / w_ *
                   (1. + z);
     return l1 * l2 * m * l1 * l2 * orc_aperture(th[0] * l1) * orc_aperture(th[1] * l2) *
@@ -257,6 +259,8 @@ static double nnm_2h(const orc_model *M, const double th[3], double l1, double l
     int z_ix = (int)round(z_arg(M, z));
     int m1_ix = (int)round(m_arg(M, m1));
     int m2_ix = (int)round(m_arg(M, m2));
+    /* SCALING build: scale1 = scaling1[m2_ix] (src/NNMap_Model.cu:808) */
+    double scale1 = M->scaling1 ? M->scaling1[m2_ix] : 1;
     double nbar1 = n_bar1[z_ix];
     double nbar2 = n_bar2[z_ix];
     double w_ = M->w[z_ix];
@@ -270,7 +274,7 @@ static double nnm_2h(const orc_model *M, const double th[3], double l1, double l
     const int Nm = M->Nm;
     double Bggd = 1. / nbar1 / nbar2 / M->rho_bar[z_ix] * M->hmf[z_ix * Nm + m1_ix] *
                   M->hmf[z_ix * Nm + m2_ix] * M->b_h[z_ix * Nm + m1_ix] * M->b_h[z_ix * Nm + m2_ix] *
-                  (m1 * orc_u_nfw(M, k3, m1, z, 1) * G_gg(M, k1, k2, m2, z, h1, h2, same_type) * Pk3 +
+                  (m1 * orc_u_nfw(M, k3, m1, z, 1) * G_gg(M, k1, k2, m2, z, h1, h2, same_type, scale1) * Pk3 +
                    m2 * orc_u_nfw(M, k3, m2, z, 1) * G_g(M, k1, m1, z, h1) * G_g(M, k2, m2, z, h2) * Pk1 +
                    m2 * orc_u_nfw(M, k3, m2, z, 1) * G_g(M, k2, m1, z, h2) * G_g(M, k1, m2, z, h1) * Pk2);
     double bggk = 1. / M->dwdz[z_ix] * M->g[z_ix] * M->p1[z_ix] * M->p2[z_ix] / w_ / w_ / w_ *

@@ -56,6 +56,9 @@ typedef struct {
     orc_cosmo cosmo;
     int clamp_k;    /* 1: clamp P_lin k index at Nk-1 */
     int nthreads;   /* OpenMP threads for integrand evaluation (0 = default) */
+    /* satellite-variance rescaling of the reference's SCALING build
+     * (src/NNMap_Model.h:59-62): [Nm] per mass bin, or NULL for none */
+    const double *scaling1, *scaling2;
 } orc_model;
 
 typedef int (*orc_integrand_v)(unsigned ndim, size_t npt, const double *x,

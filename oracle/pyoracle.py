@@ -6,7 +6,8 @@ produce reference answers.  The product package never imports this module.
 * ``Oracle`` wraps oracle/g3l_oracle.c (built into oracle/_build/), the C
   restatement of the reference's integrands and hcubature engine.
 * ``RefBuild`` wraps oracle/_ref/libg3lref.so, the reference's own CPU path
-  built by oracle/build_ref.sh (only where the reference sources exist).
+  built by oracle/build_ref.sh (only where the reference sources exist), or
+  oracle/_ref/libg3lref_scaling.so, its SCALING build, when given scaling arrays.
 """
 from __future__ import annotations
 
@@ -20,6 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libg3loracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libg3lref.so")
+REF_LIB_SCALING = os.path.join(HERE, "_ref", "libg3lref_scaling.so")
 
 _dp = C.POINTER(C.c_double)
 
@@ -35,14 +37,16 @@ def build_oracle(force: bool = False) -> str:
     return LIB
 
 
-def build_ref() -> str | None:
-    """Build the reference CPU path when its sources are present; None otherwise."""
+def build_ref(scaling: bool = False) -> str | None:
+    """Build the reference CPU path (and its SCALING build) when its sources are
+    present; the requested library's path, or None where it cannot be had."""
+    want = REF_LIB_SCALING if scaling else REF_LIB
     src = os.environ.get("G3L_REF_SRC", "/root/reference/src")
     if not os.path.exists(os.path.join(src, "NNMap_Model.cu")):
-        return REF_LIB if os.path.exists(REF_LIB) else None
-    if not os.path.exists(REF_LIB):
+        return want if os.path.exists(want) else None
+    if not (os.path.exists(REF_LIB) and os.path.exists(REF_LIB_SCALING)):
         subprocess.check_call([os.path.join(HERE, "build_ref.sh")])
-    return REF_LIB
+    return want
 
 
 class _Hod(C.Structure):
@@ -62,7 +66,8 @@ class _Model(C.Structure):
                 ("rho_bar", _dp), ("nbar1", _dp), ("nbar2", _dp),
                 ("hod1", _Hod), ("hod2", _Hod), ("same_pop", C.c_int),
                 ("A", C.c_double), ("eps", C.c_double), ("cosmo", _Cosmo),
-                ("clamp_k", C.c_int), ("nthreads", C.c_int)]
+                ("clamp_k", C.c_int), ("nthreads", C.c_int),
+                ("scaling1", _dp), ("scaling2", _dp)]
 
 
 def _ptr(a: np.ndarray):
@@ -111,7 +116,9 @@ class Oracle:
     """The restated model on one set of tables and two HOD slots."""
 
     def __init__(self, tables, hod1, hod2=None, same_pop=False, A=0.0, eps=0.0, clamp_k=True,
-                 nthreads=0):
+                 nthreads=0, scaling=None):
+        """scaling: None, or (scaling1, scaling2) [Nm] each, the satellite-variance
+        rescaling of the reference's SCALING build."""
         L = lib()
         t = tables
         self._keep = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in t.arrays().items()}
@@ -138,6 +145,11 @@ class Oracle:
         m.cosmo = _Cosmo(c.Om, c.OL, c.Ob, c.s8, c.H0, c.ns)
         m.clamp_k = 1 if clamp_k else 0
         m.nthreads = nthreads
+        if scaling is not None:
+            self._s = [np.ascontiguousarray(a, dtype=np.float64) for a in scaling]
+            if any(a.shape != (t.Nm,) for a in self._s):
+                raise ValueError("scaling arrays must have Nm entries")
+            m.scaling1, m.scaling2 = _ptr(self._s[0]), _ptr(self._s[1])
         self.m = m
         if L.orc_model_init(C.byref(m)):
             raise RuntimeError("orc_model_init failed")
@@ -219,19 +231,25 @@ def oracle_hcubature(f_py, dim, xmin, xmax, maxEval, rtol, reqAbs=0.0, use_ref=F
 # ---------------------------------------------------------------------------
 # the reference's own CPU build
 # ---------------------------------------------------------------------------
-_ref = None
+_ref = {}
 
 
-def ref_lib():
-    global _ref
-    if _ref is None:
-        path = build_ref()
+def ref_lib(scaling: bool = False):
+    """The reference's CPU build, or its SCALING build (NNMap only)."""
+    if scaling not in _ref:
+        path = build_ref(scaling)
         if path is None:
             raise FileNotFoundError("reference CPU build unavailable")
         R = C.CDLL(path)
-        R.ref_nnmap_create.restype = C.c_void_p
-        R.ref_nnmap_create.argtypes = ([_dp] + [C.c_double] * 6 + [C.c_int] + [_dp] * 9 +
-                                       [_dp, _dp, C.c_int, C.c_double, C.c_double])
+        if scaling:
+            R.ref_nnmap_create_scaled.restype = C.c_void_p
+            R.ref_nnmap_create_scaled.argtypes = ([_dp] + [C.c_double] * 6 + [C.c_int] +
+                                                  [_dp] * 11 +
+                                                  [_dp, _dp, C.c_int, C.c_double, C.c_double])
+        else:
+            R.ref_nnmap_create.restype = C.c_void_p
+            R.ref_nnmap_create.argtypes = ([_dp] + [C.c_double] * 6 + [C.c_int] + [_dp] * 9 +
+                                           [_dp, _dp, C.c_int, C.c_double, C.c_double])
         R.ref_nnmap_destroy.argtypes = [C.c_void_p]
         R.ref_nnmap_densities.argtypes = [C.c_void_p, _dp, _dp, _dp]
         R.ref_nnmap_term.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, C.c_int, C.c_size_t,
@@ -240,6 +258,13 @@ def ref_lib():
         R.ref_nnmap_method.restype = C.c_double
         R.ref_nnmap_kernel.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_int, C.c_int]
         R.ref_nnmap_kernel.restype = C.c_double
+        R.ref_hcubature_v.argtypes = [C.c_uint, C.c_void_p, C.c_void_p, C.c_uint, _dp, _dp,
+                                      C.c_size_t, C.c_double, C.c_double, C.c_int, _dp, _dp,
+                                      C.POINTER(C.c_size_t)]
+        R.ref_sici.argtypes = [C.c_double, _dp, _dp]
+        if scaling:
+            _ref[scaling] = R
+            return R
         R.ref_nmapmap_create.restype = C.c_void_p
         R.ref_nmapmap_create.argtypes = ([_dp] + [C.c_double] * 6 + [C.c_int] + [_dp] * 8 +
                                          [_dp])
@@ -251,22 +276,23 @@ def ref_lib():
         R.ref_nmapmap_method.restype = C.c_double
         R.ref_nmapmap_kernel.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
         R.ref_nmapmap_kernel.restype = C.c_double
-        R.ref_hcubature_v.argtypes = [C.c_uint, C.c_void_p, C.c_void_p, C.c_uint, _dp, _dp,
-                                      C.c_size_t, C.c_double, C.c_double, C.c_int, _dp, _dp,
-                                      C.POINTER(C.c_size_t)]
-        R.ref_sici.argtypes = [C.c_double, _dp, _dp]
-        _ref = R
-    return _ref
+        _ref[scaling] = R
+    return _ref[scaling]
 
 
 class RefBuild:
     """The reference's NNMap_Model (kind 0) or NMapMap_Model (kind 1) on square tables."""
 
-    def __init__(self, tables, hod1, hod2=None, same_pop=False, A=0.0, eps=0.0, kind=0):
+    def __init__(self, tables, hod1, hod2=None, same_pop=False, A=0.0, eps=0.0, kind=0,
+                 scaling=None):
+        """scaling: None, or (scaling1, scaling2) [N] each: the SCALING build's
+        constructor (NNMap only)."""
         t = tables
         if not (t.Nz == t.Nm == t.Nk):
             raise ValueError("the reference model needs Nz == Nm == Nk")
-        R = ref_lib()
+        if scaling is not None and kind != 0:
+            raise ValueError("the SCALING build has the NNMap model only")
+        R = ref_lib(scaling is not None)
         self.R = R
         self.kind = kind
         self._keep = {k: np.ascontiguousarray(v, dtype=np.float64) for k, v in t.arrays().items()}
@@ -276,7 +302,19 @@ class RefBuild:
         h2 = np.array(hod_tuple(hod2 if hod2 is not None else hod1))
         self._h = (h1, h2)
         N = t.Nz
-        if kind == 0:
+        if scaling is not None:
+            self._s = [np.ascontiguousarray(a, dtype=np.float64) for a in scaling]
+            if any(a.shape != (N,) for a in self._s):
+                raise ValueError("scaling arrays must have N entries")
+            self.h = R.ref_nnmap_create_scaled(_ptr(self._cosmo), t.zmin, t.zmax, t.kmin,
+                                               t.kmax, t.mmin, t.mmax, N, _ptr(k["g"]),
+                                               _ptr(k["p_lens1"]), _ptr(k["p_lens2"]),
+                                               _ptr(k["w"]), _ptr(k["dwdz"]), _ptr(k["hmf"]),
+                                               _ptr(k["P_lin"]), _ptr(k["b_h"]),
+                                               _ptr(k["conc"]), _ptr(self._s[0]),
+                                               _ptr(self._s[1]), _ptr(h1), _ptr(h2),
+                                               1 if (same_pop or hod2 is None) else 0, A, eps)
+        elif kind == 0:
             self.h = R.ref_nnmap_create(_ptr(self._cosmo), t.zmin, t.zmax, t.kmin, t.kmax, t.mmin,
                                         t.mmax, N, _ptr(k["g"]), _ptr(k["p_lens1"]),
                                         _ptr(k["p_lens2"]), _ptr(k["w"]), _ptr(k["dwdz"]),

@@ -6,6 +6,12 @@
 // path.  It constructs NNMap_Model / NMapMap_Model from arrays (bypassing the
 // ASCII table readers) and exposes a C ABI so that the oracle restatement can
 // be pinned against the reference bit for bit.  Output lives in oracle/_ref/.
+//
+// Compiled a second time with -DSCALING=1 (the reference's satellite-variance
+// rescaling, src/Makefile:17-21) together with a SCALING build of
+// NNMap_Model.cu into libg3lref_scaling.so.  That build has only the NNMap model:
+// the scaled constructor replaces ref_nnmap_create, and the NMapMap entry points
+// are left out (NMapMap_Model.cu does not compile with SCALING set).
 #include "Cosmology.h"
 #include "HOD.h"
 #include "NMapMap_Model.h"
@@ -14,6 +20,7 @@
 #include "cubature.h"
 #include "generalFunctions.h"
 
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -77,6 +84,37 @@ int counting(unsigned ndim, size_t npt, const double *x, void *d, unsigned fdim,
 
 extern "C" {
 
+#if SCALING
+// The reference's SCALING constructor (src/NNMap_Model.cu:103-200).  Its destructor
+// free()s the two arrays (src/NNMap_Model.cu:231-234), so they are handed over as
+// malloc'd copies.  scaling1/2: [N] per mass bin.
+void *ref_nnmap_create_scaled(const double *cosmo, double zmin, double zmax, double kmin,
+                              double kmax, double mmin, double mmax, int N, const double *g,
+                              const double *p1, const double *p2, const double *w,
+                              const double *dwdz, const double *hmf, const double *P_lin,
+                              const double *b_h, const double *conc, const double *scaling1,
+                              const double *scaling2, const double *hod1, const double *hod2,
+                              int same_pop, double A, double eps)
+{
+    RefNNMap *R = new RefNNMap;
+    fill_tables(R->T, N, g, p1, p2, w, dwdz, hmf, P_lin, b_h, conc);
+    double *s1 = (double *)malloc(sizeof(double) * N);
+    double *s2 = (double *)malloc(sizeof(double) * N);
+    std::memcpy(s1, scaling1, sizeof(double) * N);
+    std::memcpy(s2, scaling2, sizeof(double) * N);
+    R->cosmo = new g3lhalo::Cosmology(cosmo[0], cosmo[1], cosmo[2], cosmo[3], cosmo[4], cosmo[5]);
+    R->par1 = make_params(hod1);
+    R->par2 = make_params(hod2);
+    R->hod1 = new g3lhalo::HOD(R->par1);
+    R->hod2 = same_pop ? R->hod1 : new g3lhalo::HOD(R->par2);
+    R->model = new g3lhalo::NNMap_Model(R->cosmo, zmin, zmax, kmin, kmax, mmin, mmax, N,
+                                        R->T.g.data(), R->T.p1.data(), R->T.p2.data(),
+                                        R->T.w.data(), R->T.dwdz.data(), R->T.hmf.data(),
+                                        R->T.P_lin.data(), R->T.b_h.data(), R->T.conc.data(), s1,
+                                        s2, R->hod1, R->hod2, A, eps);
+    return R;
+}
+#else
 // cosmo[6] = {Om, OL, Ob, s8, H0, ns}
 void *ref_nnmap_create(const double *cosmo, double zmin, double zmax, double kmin, double kmax,
                        double mmin, double mmax, int N, const double *g, const double *p1,
@@ -98,6 +136,7 @@ void *ref_nnmap_create(const double *cosmo, double zmin, double zmax, double kmi
                                         R->hod1, R->hod2, A, eps);
     return R;
 }
+#endif
 
 void ref_nnmap_destroy(void *h)
 {
@@ -163,7 +202,13 @@ double ref_nnmap_method(void *h, int term, const double *th, int type1, int type
     return R->model->NNMap_3h(th[0], th[1], th[2], type1, type2);
 }
 
-// Integrand kernel at physical point pt = {l1, l2, phi, m..., z}.
+// Integrand kernel at physical point pt = {l1, l2, phi, m..., z}.  The SCALING build
+// passes the model's scaling arrays, as its integrands do (src/NNMap_Model.cu:527-531).
+#if SCALING
+#define SCALING_ARGS M->scaling1, M->scaling2
+#else
+#define SCALING_ARGS NULL, NULL
+#endif
 double ref_nnmap_kernel(void *h, int term, const double *th, const double *pt, int type1,
                         int type2)
 {
@@ -177,13 +222,13 @@ double ref_nnmap_kernel(void *h, int term, const double *th, const double *pt, i
         return g3lhalo::NNM::kernel_function_1halo(
             th[0], th[1], th[2], pt[0], pt[1], pt[2], pt[3], pt[4], M->zmin, M->zmax, M->mmin,
             M->mmax, M->Nbins, h1, h2, NULL, NULL, M->A, M->epsilon, M->g, M->p_lens1, M->p_lens2,
-            M->w, M->dwdz, M->hmf, M->concentration, M->rho_bar, nb1, nb2);
+            M->w, M->dwdz, M->hmf, M->concentration, M->rho_bar, nb1, nb2, SCALING_ARGS);
     if (term == 2)
         return g3lhalo::NNM::kernel_function_2halo(
             th[0], th[1], th[2], pt[0], pt[1], pt[2], pt[3], pt[4], pt[5], M->zmin, M->zmax,
             M->mmin, M->mmax, M->kmin, M->kmax, M->Nbins, h1, h2, NULL, NULL, M->A, M->epsilon,
             M->g, M->p_lens1, M->p_lens2, M->w, M->dwdz, M->hmf, M->P_lin, M->b_h,
-            M->concentration, M->rho_bar, nb1, nb2);
+            M->concentration, M->rho_bar, nb1, nb2, SCALING_ARGS);
     return g3lhalo::NNM::kernel_function_3halo(
         th[0], th[1], th[2], pt[0], pt[1], pt[2], pt[3], pt[4], pt[5], pt[6], M->zmin, M->zmax,
         M->mmin, M->mmax, M->kmin, M->kmax, M->Nbins, h1, h2, NULL, NULL, M->g, M->p_lens1,
@@ -191,6 +236,7 @@ double ref_nnmap_kernel(void *h, int term, const double *th, const double *pt, i
         nb2);
 }
 
+#if !SCALING
 void *ref_nmapmap_create(const double *cosmo, double zmin, double zmax, double kmin,
                          double kmax, double mmin, double mmax, int N, const double *g,
                          const double *p, const double *w, const double *dwdz, const double *hmf,
@@ -285,6 +331,8 @@ double ref_nmapmap_kernel(void *h, int term, const double *th, const double *pt)
         M->mmin, M->mmax, M->kmin, M->kmax, M->Nbins, M->hod, NULL, M->g, M->p_lens, M->w,
         M->dwdz, M->hmf, M->P_lin, M->b_h, M->concentration, M->rho_bar, M->n_bar);
 }
+
+#endif  // !SCALING
 
 // The reference's cubature engine with a caller-supplied integrand.
 int ref_hcubature_v(unsigned fdim, integrand_v f, void *fdata, unsigned dim, const double *xmin,

@@ -4,7 +4,8 @@
 // File layout (little-endian): int32 N; float64 zmin zmax kmin kmax mmin mmax;
 // cosmology[6] (Om, OL, Ob, sigma8, H0, ns); hod1[6]; hod2[6] (f, alpha, Mth, sigma,
 // M', beta); g, p_lens1, p_lens2, w, dwdz [N]; hmf, P_lin, b_h, concentration [N*N];
-// thetas[4][3] (rad).  argv[2]: 0 = all-FP64 form, 1 = mixed precision.
+// thetas[4][3] (rad); with argv[3] = 1 also scaling1, scaling2 [N], for the SCALING
+// constructor.  argv[2]: 0 = all-FP64 form, 1 = mixed precision.
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -27,6 +28,11 @@ int main(int argc, char **argv)
     for (auto &a : v2) ok = ok && std::fread(a.data(), 8, (size_t)N * N, f) == (size_t)N * N;
     double th[4][3];
     ok = ok && std::fread(th, 8, 12, f) == 12;
+    const bool scaled = argc > 3 && std::atoi(argv[3]) == 1;
+    std::vector<double> s1(N), s2(N);
+    if (scaled)
+        ok = ok && std::fread(s1.data(), 8, N, f) == (size_t)N &&
+             std::fread(s2.data(), 8, N, f) == (size_t)N;
     std::fclose(f);
     if (!ok) return 4;
     g3lhalo::Cosmology c;
@@ -49,6 +55,18 @@ int main(int argc, char **argv)
     g3lhalo::Params p1 = params(h1), p2 = params(h2);
     g3lhalo::HOD hod1(&p1), hod2(&p2);
     const int prec = std::atoi(argv[2]) ? G3L_MIXED : G3L_FP64;
+
+    if (scaled) {  // the SCALING constructor; same-population terms
+        g3lhalo::NNMap_Model ns(&c, bin[0], bin[1], bin[2], bin[3], bin[4], bin[5], N,
+                                v1[0].data(), v1[1].data(), v1[2].data(), v1[3].data(),
+                                v1[4].data(), v2[0].data(), v2[1].data(), v2[2].data(),
+                                v2[3].data(), s1.data(), s2.data(), &hod1, &hod2, 0.0, 0.0);
+        ns.setPrecision(prec);
+        std::printf("S_NNMap_1h %.17g\n", ns.NNMap_1h(th[1][0], th[1][1], th[1][2], 1, 1));
+        std::printf("S_NNMap_2h %.17g\n", ns.NNMap_2h(th[1][0], th[1][1], th[1][2], 1, 1));
+        std::printf("status %d\n", ns.lastStatus());
+        return 0;
+    }
 
     g3lhalo::NNMap_Model nn(&c, bin[0], bin[1], bin[2], bin[3], bin[4], bin[5], N, v1[0].data(),
                             v1[1].data(), v1[2].data(), v1[3].data(), v1[4].data(), v2[0].data(),

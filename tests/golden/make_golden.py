@@ -1,12 +1,14 @@
 """Generate the golden vectors in tests/golden/ from the reference's own CPU build.
 
 Run from the repository root where the reference sources exist:
-    python tests/golden/make_golden.py
-It builds oracle/_ref/libg3lref.so (oracle/build_ref.sh) from the reference's
-unmodified sources, drives NNMap_Model / NMapMap_Model / hcubature_v in memory
-through oracle/ref_harness.cu, and writes tests/golden/ref_n64.npz.  The tables
-the vectors were computed on are stored in the same file, so the fixture does
-not depend on the table generator being bit-identical across platforms.
+    python tests/golden/make_golden.py            # ref_n64.npz
+    python tests/golden/make_golden.py --scaling  # ref_scaling_n64.npz
+It builds oracle/_ref/libg3lref.so and libg3lref_scaling.so (oracle/build_ref.sh)
+from the reference's unmodified sources, drives NNMap_Model / NMapMap_Model /
+hcubature_v in memory through oracle/ref_harness.cu, and writes the fixture.  The
+tables the vectors were computed on are stored in ref_n64.npz, so the fixtures do
+not depend on the table generator being bit-identical across platforms; the
+SCALING vectors are computed on the tables read back from that file.
 """
 from __future__ import annotations
 
@@ -24,6 +26,7 @@ from g3lhalo_gb300.tables import make_tables  # noqa: E402
 import pyoracle as P  # noqa: E402
 
 OUT = os.path.join(ROOT, "tests", "golden", "ref_n64.npz")
+OUT_SCALING = os.path.join(ROOT, "tests", "golden", "ref_scaling_n64.npz")
 
 # analytic integrands for the engine-only vectors (Genz test families)
 def genz_gauss(x):
@@ -132,5 +135,59 @@ def main():
     print("wrote", OUT, os.path.getsize(OUT), "bytes")
 
 
+def scaling_arrays(N):
+    """Satellite-variance rescalings per mass bin: scaling1 in [0.6, 1.4] (below 1 the
+    same-population pair count goes negative at small N_sat, which the reference does
+    not clip), scaling2 a different ramp (the reference never reads it)."""
+    j = np.arange(N)
+    return 1.0 + 0.4 * np.sin(0.23 * j), 0.7 + 0.02 * j
+
+
+def main_scaling():
+    """Vectors of the reference's SCALING build (NNMap 1- and 2-halo terms)."""
+    P.build_ref(scaling=True)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from conftest import tables_from_golden  # noqa: E402
+    g = dict(np.load(OUT))
+    T = tables_from_golden(g)
+    h1, h2 = g["hod1"], g["hod2"]
+    thetas = g["thetas"]
+    s1, s2 = scaling_arrays(T.Nm)
+    out = {"scaling1": s1, "scaling2": s2}
+    rng = np.random.default_rng(20261204)
+    R = P.RefBuild(T, h1, h2, kind=0, scaling=(s1, s2))
+    O = P.Oracle(T, h1, h2, clamp_k=False)
+    for term in (1, 2):
+        lo, hi = O.bounds(term)
+        pts = rng.uniform(lo, hi, size=(48, len(lo)))
+        pts[:, :2] = 10 ** pts[:, :2]
+        pts[:, 3:-1] = 10 ** pts[:, 3:-1]
+        out[f"sc_pts_t{term}"] = pts
+        out[f"sc_kernel_t{term}"] = np.array(
+            [[R.kernel(term, thetas[1], p, t1, t2) for (t1, t2) in ((1, 2), (1, 1), (2, 2))]
+             for p in pts])
+    rows = []
+    for it in (1, 2):
+        for term in (1, 2):
+            for (t1, t2) in ((1, 1), (2, 2), (1, 2)):
+                v, e, n = R.term(term, thetas[it], t1, t2, maxEval=60000, rtol=1e-4)
+                rows.append([it, term, t1, t2, 60000, v, e, n])
+    out["sc_terms"] = np.array(rows, dtype=np.float64)
+    out["sc_stock"] = np.array([[term, R.method(term, thetas[1], 1, 1)] for term in (1, 2)])
+    R.close()
+    R = P.RefBuild(T, h1, None, kind=0, scaling=(s1, s2))
+    rows = []
+    for term in (1, 2):
+        v, e, n = R.term(term, thetas[0], 1, 2, maxEval=40000, rtol=1e-4)
+        rows.append([0, term, 1, 2, 40000, v, e, n])
+    out["sc_same_terms"] = np.array(rows, dtype=np.float64)
+    R.close()
+    np.savez_compressed(OUT_SCALING, **out)
+    print("wrote", OUT_SCALING, os.path.getsize(OUT_SCALING), "bytes")
+
+
 if __name__ == "__main__":
-    main()
+    if "--scaling" in sys.argv[1:]:
+        main_scaling()
+    else:
+        main()

@@ -48,7 +48,7 @@ def test_header_compiles_with_the_reference_classes(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
-def _write_input(path, g):
+def _write_input(path, g, scaling=None):
     meta = g["tab_meta"]
     with open(path, "wb") as f:
         f.write(np.array([int(meta[0])], dtype=np.int32).tobytes())
@@ -61,11 +61,14 @@ def _write_input(path, g):
         for k in ("tab_hmf", "tab_P_lin", "tab_b_h", "tab_conc"):
             f.write(np.ascontiguousarray(g[k], dtype=np.float64).tobytes())
         f.write(np.ascontiguousarray(g["thetas"], dtype=np.float64).tobytes())
+        if scaling is not None:
+            for a in scaling:
+                f.write(np.ascontiguousarray(a, dtype=np.float64).tobytes())
 
 
-def _run(exe, path, mixed):
-    r = subprocess.run([exe, str(path), "1" if mixed else "0"], capture_output=True, text=True,
-                       timeout=600)
+def _run(exe, path, mixed, scaled=False):
+    r = subprocess.run([exe, str(path), "1" if mixed else "0", "1" if scaled else "0"],
+                       capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, (r.returncode, r.stderr)
     out = {}
     for line in r.stdout.splitlines():
@@ -100,3 +103,19 @@ def test_shim_reproduces_the_reference_methods(tmp_path, golden, golden_tables, 
     want = r["result"].reshape(-1, 3).sum(axis=1)
     got = np.array([out["calculateAll_%d" % k][0] for k in range(6)])
     np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mixed,rtol", [(False, 1e-9), (True, 1e-4)])
+def test_shim_scaling_constructor_reproduces_the_scaling_build(tmp_path, golden, mixed, rtol):
+    """The SCALING constructor against the reference's SCALING build (same-population
+    NNMap_1h / NNMap_2h at the stock budgets)."""
+    scal = dict(np.load(os.path.join(ROOT, "tests", "golden", "ref_scaling_n64.npz")))
+    exe = _build_driver(tmp_path)
+    path = tmp_path / "in_scaled.bin"
+    _write_input(path, golden, (scal["scaling1"], scal["scaling2"]))
+    out = _run(exe, path, mixed, scaled=True)
+    assert out["status"] == [0]
+    for t, want in scal["sc_stock"]:
+        got = out["S_NNMap_%dh" % int(t)][0]
+        assert abs(got - want) <= rtol * abs(want), (t, got, want)

@@ -4,6 +4,8 @@ The golden vectors in tests/golden/ref_n64.npz were written by
 tests/golden/make_golden.py from the reference's unmodified sources (its OpenMP
 path).  On x86-64 the restatement must reproduce them bit for bit.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -108,3 +110,49 @@ def test_sici_continuity():
         vals.append((si.value, ci.value))
     assert abs(vals[0][0] - vals[1][0]) < 1e-9
     assert abs(vals[0][1] - vals[1][1]) < 1e-9
+
+
+# --- the reference's SCALING build (satellite-variance rescaling) ---------------------
+GOLDEN_SCALING = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                              "ref_scaling_n64.npz")
+
+
+@pytest.fixture(scope="module")
+def scal():
+    return dict(np.load(GOLDEN_SCALING))
+
+
+@pytest.mark.parametrize("term", [1, 2])
+def test_kernels_nnmap_scaling(golden, golden_tables, scal, term):
+    o = P.Oracle(golden_tables, golden["hod1"], golden["hod2"], clamp_k=False,
+                 scaling=(scal["scaling1"], scal["scaling2"]))
+    th = golden["thetas"][1]
+    got = np.array([[o.kernel(0, term, th, p, t1, t2) for (t1, t2) in ((1, 2), (1, 1), (2, 2))]
+                    for p in scal[f"sc_pts_t{term}"]])
+    assert_close(got, scal[f"sc_kernel_t{term}"], rtol_other=1e-12)
+
+
+def test_terms_nnmap_scaling(golden, golden_tables, scal):
+    s = (scal["scaling1"], scal["scaling2"])
+    o = P.Oracle(golden_tables, golden["hod1"], golden["hod2"], clamp_k=False, scaling=s)
+    _check_terms(o, scal["sc_terms"], golden["thetas"], 0)
+    o = P.Oracle(golden_tables, golden["hod1"], None, clamp_k=False, scaling=s)
+    _check_terms(o, scal["sc_same_terms"], golden["thetas"], 0)
+
+
+def test_stock_methods_prefactor_scaling(golden, golden_tables, scal):
+    o = P.Oracle(golden_tables, golden["hod1"], golden["hod2"], clamp_k=False,
+                 scaling=(scal["scaling1"], scal["scaling2"]))
+    for term, want in scal["sc_stock"]:
+        got = o.term(0, int(term), golden["thetas"][1], 1, 1, maxEval=5_000_000, rtol=1e-3)[3]
+        assert_close(got, want, rtol_other=1e-6)
+
+
+def test_scaling_changes_only_same_population_terms(golden, scal):
+    """The two-population rows of the SCALING vectors equal the unscaled reference's
+    (scaling enters only the same-population pair count, src/HOD.cu:86-87)."""
+    plain = {(int(r[0]), int(r[1]), int(r[2]), int(r[3])): r[5] for r in golden["nn_terms"]}
+    for it, term, t1, t2, me, v, e, n in scal["sc_terms"]:
+        key = (int(it), int(term), int(t1), int(t2))
+        if t1 != t2 and key in plain:
+            assert v == plain[key]
