@@ -135,6 +135,13 @@ def lib():
             L.g3l_host_densities.argtypes = [C.POINTER(Tables), _dp, _dp, _dp]
             L.g3l_hcubature_v.argtypes = [C.c_uint, C.c_void_p, C.c_void_p, C.c_uint, _dp, _dp,
                                           C.c_size_t, C.c_double, C.c_double, C.c_int, _dp, _dp]
+            L.g3l_read_function.argtypes = [C.c_char_p, C.c_double, C.c_int, C.c_double,
+                                            C.c_double, C.c_int, _dp]
+            L.g3l_read_function2d.argtypes = [C.c_char_p, C.c_double, C.c_int, C.c_double,
+                                              C.c_double, C.c_double, C.c_double, _dp]
+            L.g3l_read_hod_params.argtypes = [C.c_char_p, _dp]
+            L.g3l_read_cosmology.argtypes = [C.c_char_p, _dp]
+            L.g3l_read_triplets.argtypes = [C.c_char_p, _dp, C.c_int, C.POINTER(C.c_int)]
             _lib = L
     return _lib
 

@@ -30,7 +30,7 @@ UNITS = {
     "host_api.cu": ["-fmad=false"],
     "probe.cu": ["-fmad=true"],
 }
-HOST_UNITS = ["host_cubature.cpp", "host_model.cpp"]
+HOST_UNITS = ["host_cubature.cpp", "host_model.cpp", "host_io.cpp"]
 
 
 def _sources():

@@ -35,10 +35,11 @@ class Cosmology:
     s8: float = 0.8
     h: float = 0.7
     ns: float = 0.96
+    H0_value: float | None = None  # H0 [km/s/Mpc] as given (a cosmology file), else 100 h
 
     @property
     def H0(self) -> float:
-        return 100.0 * self.h
+        return 100.0 * self.h if self.H0_value is None else self.H0_value
 
     def as_array(self) -> np.ndarray:
         """[Om, OL, Ob, sigma8, H0, ns], the reference's Cosmology value order."""

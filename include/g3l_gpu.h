@@ -300,6 +300,34 @@ int g3l_hcubature_v(unsigned fdim, g3l_integrand_v f, void *fdata, unsigned dim,
                     const double *xmin, const double *xmax, size_t maxEval, double reqAbsError,
                     double reqRelError, int norm, double *val, double *err);
 
+/* The reference's ASCII inputs, read as its drivers read them (host only, no device
+ * work).  Numbers are parsed by C++ stream extraction; reading stops at the first
+ * token that is not a number.  Where the reference exits or reads undefined values,
+ * these return G3L_ERR_INVALID with g3l_last_error().
+ *
+ * A 1-D table of "x y" lines (g3lhalo::Function, src/Function.cpp:6-39), sampled at
+ * nbins bins: linear interpolation, default_value outside [x_first, x_last).
+ * log_bins = 0: x_i = min + i (max-min)/nbins (Function::read, src/Function.cpp:89-105,
+ * the z tables and the SCALING arrays); 1: x_i = exp(log min + i log(max/min)/nbins)
+ * (Function::readLog, src/Function.cpp:108-124).  out: [nbins]. */
+int g3l_read_function(const char *path, double default_value, int nbins, double min, double max,
+                      int log_bins, double *out);
+/* A 2-D table of "x1 x2 y" lines (g3lhalo::Function2D) on nbins x nbins bins, x1
+ * linear in [min1, max1), x2 logarithmic in [min2, max2) (Function2D::read,
+ * src/Function2D.cpp:46-95: the hmf, b_h and concentration tables over (z, m), P_lin
+ * over (z, k)).  out: [nbins * nbins], first index x1. */
+int g3l_read_function2d(const char *path, double default_value, int nbins, double min1,
+                        double max1, double min2, double max2, double *out);
+/* A HOD parameter file ("M_min", "sigma", "M'", "beta", "alpha", "f" lines,
+ * src/Params.cpp:7-74) as {f, alpha, Mth, sigma, M', beta}. */
+int g3l_read_hod_params(const char *path, double params[6]);
+/* A cosmology file ("Omega_m", "Omega_Lambda", "Omega_b", "sigma8", "H0", "ns" lines,
+ * src/Cosmology.cpp:11-72) as {Om, OL, Ob, sigma8, H0, ns}. */
+int g3l_read_cosmology(const char *path, double cosmo[6]);
+/* Aperture triplets "theta1 theta2 theta3" in arcmin (src/calculateNNMap.cu:121-129).
+ * Stores up to cap triplets in thetas[3*cap] and the number in the file in *n. */
+int g3l_read_triplets(const char *path, double *thetas, int cap, int *n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,7 +18,7 @@ mkdir -p "$OUT/obj"
 CXXF="-std=c++17 -O2 -fopenmp -fPIC -ffp-contract=off -I$REF"
 NVF="-std=c++17 -O3 -rdc=true -Xcompiler -fopenmp,-fPIC,-ffp-contract=off -I$REF"
 pids=()
-for f in hcubature Cosmology Params; do
+for f in hcubature Cosmology Params Function Function2D; do
     g++ $CXXF -c "$REF/$f.cpp" -o "$OUT/obj/$f.o" & pids+=($!)
 done
 for f in HOD generalFunctions NNMap_Model NMapMap_Model; do
@@ -34,7 +34,9 @@ for p in "${pids[@]}"; do wait "$p"; done
 nvcc -shared -rdc=true -Xcompiler -fopenmp "$OUT"/obj/*.o -o "$OUT/libg3lref.so"
 echo "built $OUT/libg3lref.so"
 common=()
-for f in hcubature Cosmology Params HOD generalFunctions; do common+=("$OUT/obj/$f.o"); done
+for f in hcubature Cosmology Params Function Function2D HOD generalFunctions; do
+    common+=("$OUT/obj/$f.o")
+done
 nvcc -shared -rdc=true -Xcompiler -fopenmp "${common[@]}" "$OUT"/obj_scaling/*.o \
     -o "$OUT/libg3lref_scaling.so"
 echo "built $OUT/libg3lref_scaling.so"

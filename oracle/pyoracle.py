@@ -262,6 +262,12 @@ def ref_lib(scaling: bool = False):
                                       C.c_size_t, C.c_double, C.c_double, C.c_int, _dp, _dp,
                                       C.POINTER(C.c_size_t)]
         R.ref_sici.argtypes = [C.c_double, _dp, _dp]
+        R.ref_function_read.argtypes = [C.c_char_p, C.c_double, C.c_int, C.c_double,
+                                        C.c_double, C.c_int, _dp]
+        R.ref_function2d_read.argtypes = [C.c_char_p, C.c_double, C.c_int, C.c_double,
+                                          C.c_double, C.c_double, C.c_double, _dp]
+        R.ref_params_read.argtypes = [C.c_char_p, _dp]
+        R.ref_cosmology_read.argtypes = [C.c_char_p, _dp]
         if scaling:
             _ref[scaling] = R
             return R

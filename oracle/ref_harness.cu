@@ -13,6 +13,8 @@
 // the scaled constructor replaces ref_nnmap_create, and the NMapMap entry points
 // are left out (NMapMap_Model.cu does not compile with SCALING set).
 #include "Cosmology.h"
+#include "Function.h"
+#include "Function2D.h"
 #include "HOD.h"
 #include "NMapMap_Model.h"
 #include "NNMap_Model.h"
@@ -347,6 +349,52 @@ int ref_hcubature_v(unsigned fdim, integrand_v f, void *fdata, unsigned dim, con
                          (error_norm)norm, val, err);
     *neval = cnt.n;
     return st;
+}
+
+// The reference's ASCII readers as its drivers use them (src/calculateNNMap.cu:42-72).
+// They exit() or throw on bad input, so callers pass valid files only.
+int ref_function_read(const char *path, double def, int N, double min, double max, int log_bins,
+                      double *out)
+{
+    g3lhalo::Function f(path, def);
+    std::vector<double> v;
+    int st = log_bins ? f.readLog(N, min, max, v) : f.read(N, min, max, v);
+    std::memcpy(out, v.data(), sizeof(double) * v.size());
+    return st;
+}
+
+int ref_function2d_read(const char *path, double def, int N, double min1, double max1,
+                        double min2, double max2, double *out)
+{
+    g3lhalo::Function2D f(path, def);
+    std::vector<double> v;
+    int st = f.read(N, min1, max1, min2, max2, v);
+    std::memcpy(out, v.data(), sizeof(double) * v.size());
+    return st;
+}
+
+// {f, alpha, Mth, sigma, M', beta}
+void ref_params_read(const char *path, double *out)
+{
+    g3lhalo::Params p(path);
+    out[0] = p.f;
+    out[1] = p.alpha;
+    out[2] = p.mmin;
+    out[3] = p.sigma;
+    out[4] = p.mprime;
+    out[5] = p.beta;
+}
+
+// {Om, OL, Ob, sigma8, H0, ns}
+void ref_cosmology_read(const char *path, double *out)
+{
+    g3lhalo::Cosmology c(path);
+    out[0] = c.Omega_m;
+    out[1] = c.Omega_Lambda;
+    out[2] = c.Omega_b;
+    out[3] = c.sigma8;
+    out[4] = c.H0;
+    out[5] = c.ns;
 }
 
 // Physics primitives, for point-level pinning.
