@@ -6,6 +6,7 @@
 // same libm.
 #include <algorithm>
 #include <atomic>
+#include <memory>
 #include <thread>
 #include <vector>
 #include <cmath>
@@ -62,26 +63,112 @@ void rho_bar(const Binning &B, double Om, double OL, double H0, double *out)
 }
 
 namespace {
+// The mass-dependent factors of the n_bar integrand (m, N_c + N_s and the mass bin)
+// do not depend on z, and the 1-D Gauss-Kronrod regions of the Nz integrals come from
+// bisecting the same interval, so most 15-point blocks recur in many z bins (a
+// 64 x 128 table set evaluates ~1.5M points per HOD vector at ~30k distinct
+// abscissae).  A table shared by the worker threads keeps each block's factors;
+// every value is computed by the same expression as without the table, so n_bar is
+// unchanged to the last bit.  A slot is claimed by CAS and published with a release
+// store; a reader that meets a slot being filled computes its block itself.
+constexpr int kGK = 15;  // points per 1-D region
+
+struct BlockFactors {
+    double x[kGK], m[kGK], S[kGK];  // abscissae, m, N_c + N_s
+    int mix[kGK];                   // nearest mass bin
+};
+
+class BlockCache {
+   public:
+    explicit BlockCache(int log2cap)
+        : cap_(1u << log2cap), shift_(64 - log2cap), st_(new std::atomic<unsigned>[cap_]()),
+          dat_(new BlockFactors[cap_])
+    {
+    }
+    // factors of the block at x[0..14]: from the table, or computed by fill() and
+    // (if a slot is free) stored
+    template <class Fill>
+    const BlockFactors *get(const double *x, BlockFactors &local, Fill fill)
+    {
+        unsigned long long k0, k1;
+        std::memcpy(&k0, x, 8);
+        std::memcpy(&k1, x + 1, 8);
+        unsigned idx = (unsigned)(((k0 * 0x9E3779B97F4A7C15ull) ^ (k1 * 0xC2B2AE3D27D4EB4Full)) >> shift_);
+        for (int probe = 0; probe < 32; ++probe, idx = (idx + 1) & (cap_ - 1)) {
+            unsigned s = st_[idx].load(std::memory_order_acquire);
+            if (s == 0) {
+                if (used_.load(std::memory_order_relaxed) >= cap_ / 4 * 3) break;
+                if (st_[idx].compare_exchange_strong(s, 1u, std::memory_order_acq_rel)) {
+                    used_.fetch_add(1, std::memory_order_relaxed);
+                    BlockFactors &b = dat_[idx];
+                    fill(x, b);
+                    st_[idx].store(2u, std::memory_order_release);
+                    return &b;
+                }
+            }
+            if (s == 1) break;  // being filled: compute this block here
+            if (s == 2 && std::memcmp(dat_[idx].x, x, sizeof(double) * kGK) == 0) return &dat_[idx];
+        }
+        fill(x, local);
+        return &local;
+    }
+
+   private:
+    unsigned cap_, shift_;
+    std::unique_ptr<std::atomic<unsigned>[]> st_;
+    std::unique_ptr<BlockFactors[]> dat_;
+    std::atomic<unsigned> used_{0};
+};
+
 struct NbarCtx {
     const Binning *B;
     const double *hmf;
     const double *hod;  // f, alpha, Mth, sigma, M', beta
     double z;
+    BlockCache *cache;
 };
 
+// N_c, N_s (src/HOD.cu:35-76) and the mass bin (src/NNMap_Model.cu:556) at x = log10 m;
+// erf is evaluated once for both occupations (the same argument in the reference)
+inline void mass_factors(const Binning &B, const double *h, double x, double &m, double &S,
+                         int &mix)
+{
+    m = std::pow(10, x);
+    const double e = std::erf(std::log(m / h[2]) / h[3] / 1.414213562);
+    const double Nc = 0.5 * h[1] * (1 + e);
+    const double Ns = 0.5 * (1 + e) * std::pow(m / h[4], h[5]);
+    S = Nc + Ns;
+    mix = (int)std::round(std::log(m / B.mmin) * B.Nm / std::log(B.mmax / B.mmin));
+}
+
+// ln10 m n(m, z) (N_c + N_s) without the ln10 (src/NNMap_Model.cu:262-297,
+// src/generalFunctions.cu:233-245)
 int nbar_integrand(unsigned ndim, size_t npt, const double *x, void *fdata, unsigned, double *fv)
 {
     const NbarCtx *C = (const NbarCtx *)fdata;
     const Binning &B = *C->B;
     const double *h = C->hod;
+    const int z_ix = (int)std::round((C->z - B.zmin) * B.Nz / (B.zmax - B.zmin));
+    const double *row = C->hmf + (size_t)z_ix * B.Nm;
+    if (ndim == 1 && npt % kGK == 0) {
+        auto fill = [&](const double *xb, BlockFactors &b) {
+            for (int k = 0; k < kGK; ++k) {
+                b.x[k] = xb[k];
+                mass_factors(B, h, xb[k], b.m[k], b.S[k], b.mix[k]);
+            }
+        };
+        BlockFactors local;
+        for (size_t i = 0; i < npt; i += kGK) {
+            const BlockFactors *b = C->cache->get(x + i, local, fill);
+            for (int k = 0; k < kGK; ++k) fv[i + k] = b->m[k] * row[b->mix[k]] * b->S[k];
+        }
+        return 0;
+    }
     for (size_t i = 0; i < npt; ++i) {
-        double m = std::pow(10, x[i * ndim]);
-        double Nc = 0.5 * h[1] * (1 + std::erf(std::log(m / h[2]) / h[3] / 1.414213562));
-        double Ns = 0.5 * (1 + std::erf(std::log(m / h[2]) / h[3] / 1.414213562)) *
-                    std::pow(m / h[4], h[5]);
-        int m_ix = (int)std::round(std::log(m / B.mmin) * B.Nm / std::log(B.mmax / B.mmin));
-        int z_ix = (int)std::round((C->z - B.zmin) * B.Nz / (B.zmax - B.zmin));
-        fv[i] = m * C->hmf[(int)(z_ix * B.Nm + m_ix)] * (Nc + Ns);
+        double m, S;
+        int mix;
+        mass_factors(B, h, x[i * ndim], m, S, mix);
+        fv[i] = m * row[mix] * S;
     }
     return 0;
 }
@@ -92,12 +179,13 @@ int n_bar(const Binning &B, const double *hmf, const double hod[6], double *out)
     const double lo[1] = {std::log10(B.mmin)};
     const double hi[1] = {std::log10(B.mmax_integral())};
     const double ln10 = std::log(10.0);
+    BlockCache cache(13);
     // the Nz integrals are independent: spread them over the host cores (each one is
     // the same sequential computation as in a single thread)
     std::atomic<int> next{0}, failed{0};
     auto work = [&]() {
         for (int i; (i = next.fetch_add(1)) < B.Nz;) {
-            NbarCtx C{&B, hmf, hod, B.zmin + i * (B.zmax - B.zmin) / B.Nz};
+            NbarCtx C{&B, hmf, hod, B.zmin + i * (B.zmax - B.zmin) / B.Nz, &cache};
             double val, err;
             if (cubature(1, nbar_integrand, &C, lo, hi, 0, 0, 1e-4, &val, &err, nullptr)) {
                 failed = 1;
