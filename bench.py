@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--host-loop", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-config2", action="store_true")
+    ap.add_argument("--no-precompute", action="store_true")
     # batched fit sweep: this many HOD vectors in one launch (0 = skip)
     ap.add_argument("--sweep", type=int, default=16)
     return ap.parse_args()
@@ -258,6 +259,45 @@ def config2_leg(G, trip, max_eval, reps=3):
                         "1e-4, maxEval %d" % max_eval}
 
 
+PRECOMPUTE_ARGS = (0.001, 2.0, 1e10, 1e17, 1e-4 * 0.7, 1e3 * 0.7, 64)
+PRECOMPUTE_COSMO = (0.3, 0.7, 0.045, 0.8, 70.0, 0.96)
+
+
+def precompute_source_nz():
+    z = np.linspace(0.0, 3.0, 60)
+    nz = z * z * np.exp(-(z / 0.5) ** 1.5)
+    return z, nz / (nz.sum() * (z[1] - z[0]))
+
+
+def precompute_leg(G, reps=3):
+    """The reference's table precomputation (doPrecomputations) for 64 bins on the
+    device: ~25k adaptive 1-D integrals (sigma^2, dsigma^2/dm, M*, distances); device
+    time (CUDA events) of the best of `reps` runs."""
+    z, nz = precompute_source_nz()
+    runs = [G.precompute_tables(PRECOMPUTE_COSMO, z, nz, *PRECOMPUTE_ARGS) for _ in range(reps)]
+    best = min(runs, key=lambda r: r["device_ms"])
+    return best, {"nbins": 64, "device_ms": best["device_ms"], "integrals": best["integrals"],
+                  "points": best["points"],
+                  "points_per_s": best["points"] / (best["device_ms"] * 1e-3),
+                  "workload": "doPrecomputations: g, w, dw/dz, P_lin, concentration (M* from "
+                              "256 sigma^2 per z), Sheth-Tormen n(m, z) and b_h on 64 bins; FP64"}
+
+
+def precompute_cpu(dev):
+    """The oracle restatement of the same precomputation on the host cores (OpenMP over
+    the integrals), and the device tables' largest deviation from it."""
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "oracle"))
+    import pyoracle as P
+    z, nz = precompute_source_nz()
+    t0 = time.perf_counter()
+    o = P.precompute(PRECOMPUTE_COSMO, z, nz, *PRECOMPUTE_ARGS)
+    dt = time.perf_counter() - t0
+    rel = max(float(np.max(np.abs(dev[k] - o[k]) / np.maximum(np.abs(o[k]), 1e-300)))
+              for k in ("g", "w", "dwdz", "P_lin", "conc", "hmf", "b_h"))
+    return {"seconds": dt, "cores": os.cpu_count(), "kind": "port",
+            "device_max_rel_vs_port": rel}
+
+
 def serving_leg(G, ctx, trip, hods, args, n_req=48, rate=12.0, seed=7):
     """Continuous batching: a seeded Poisson stream of model evaluations (triplet
     count log-uniform in 1..220, NNMap or NMapMap, one of 8 HOD vectors) submitted to
@@ -435,8 +475,13 @@ def main():
             out["sweep"] = sweep_leg(G, ctx, trip, hods, args.sweep, args.max_eval)
         if not args.no_config2:
             out["nmapmap_twopop"] = config2_leg(G, trip, args.max_eval)
+        pre = None
+        if not args.no_precompute:
+            pre, out["precompute"] = precompute_leg(G)
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_sample(T, trip, hods[last_hod], args.max_eval, 4)
+            if pre is not None:
+                out["cpu_baseline"]["precompute"] = precompute_cpu(pre)
         out["config"] = config(len(trip), args.max_eval)
         print(json.dumps(out), flush=True)
     if dist:

@@ -58,6 +58,19 @@ class ServerStats(C.Structure):
                 ("free_regions", C.c_uint64)]
 
 
+class PrecomputeIn(C.Structure):
+    _fields_ = [("cosmo", C.c_double * 6), ("nz_z", _dp), ("nz_v", _dp), ("n_nz", C.c_int),
+                ("zmin", C.c_double), ("zmax", C.c_double), ("mmin", C.c_double),
+                ("mmax", C.c_double), ("kmin", C.c_double), ("kmax", C.c_double),
+                ("nbins", C.c_int)]
+
+
+class PrecomputeOut(C.Structure):
+    _fields_ = [("g", _dp), ("w", _dp), ("dwdz", _dp), ("P_lin", _dp), ("conc", _dp),
+                ("hmf", _dp), ("b_h", _dp), ("amplitude", C.c_double), ("device_ms", C.c_double),
+                ("integrals", C.c_longlong), ("points", C.c_longlong)]
+
+
 class Options(C.Structure):
     _fields_ = [("eval_blocks_per_sm", C.c_int), ("eval_warps_per_block", C.c_int),
                 ("use_graph", C.c_int), ("max_rounds", C.c_int), ("unlimited_pool", C.c_uint64),
@@ -135,6 +148,8 @@ def lib():
             L.g3l_host_densities.argtypes = [C.POINTER(Tables), _dp, _dp, _dp]
             L.g3l_hcubature_v.argtypes = [C.c_uint, C.c_void_p, C.c_void_p, C.c_uint, _dp, _dp,
                                           C.c_size_t, C.c_double, C.c_double, C.c_int, _dp, _dp]
+            L.g3l_precompute_tables.argtypes = [C.POINTER(PrecomputeIn), C.c_int,
+                                                C.POINTER(PrecomputeOut)]
             L.g3l_read_function.argtypes = [C.c_char_p, C.c_double, C.c_int, C.c_double,
                                             C.c_double, C.c_int, _dp]
             L.g3l_read_function2d.argtypes = [C.c_char_p, C.c_double, C.c_int, C.c_double,
@@ -182,6 +197,49 @@ def host_densities(tables, hod):
     h = np.ascontiguousarray(hod, dtype=np.float64)
     _check(lib().g3l_host_densities(C.byref(ct), _ptr(h), _ptr(rho), _ptr(nb)))
     return rho, nb
+
+
+def precompute_tables(cosmo, nz_z, nz_v, zmin, zmax, mmin, mmax, kmin, kmax, nbins, device=0):
+    """The reference's doPrecomputations on the device (g3l_precompute_tables).
+
+    cosmo: [Om, OL, Ob, sigma8, H0, ns]; nz_z / nz_v: the source redshift distribution.
+    Returns a dict of g, w, dwdz [nbins] and P_lin, conc, hmf, b_h [nbins, nbins]
+    (z-major), plus amplitude, device_ms, integrals and points."""
+    N = int(nbins)
+    zz = np.ascontiguousarray(nz_z, dtype=np.float64)
+    zv = np.ascontiguousarray(nz_v, dtype=np.float64)
+    if zz.shape != zv.shape or zz.ndim != 1:
+        raise ValueError("nz_z and nz_v must be 1-D arrays of one length")
+    res = {k: np.empty(N) for k in ("g", "w", "dwdz")}
+    res.update({k: np.empty((N, N)) for k in ("P_lin", "conc", "hmf", "b_h")})
+    pin = PrecomputeIn(cosmo=(C.c_double * 6)(*[float(x) for x in cosmo]), nz_z=_ptr(zz),
+                       nz_v=_ptr(zv), n_nz=len(zz), zmin=zmin, zmax=zmax, mmin=mmin, mmax=mmax,
+                       kmin=kmin, kmax=kmax, nbins=N)
+    pout = PrecomputeOut(**{k: _ptr(v) for k, v in res.items()})
+    _check(lib().g3l_precompute_tables(C.byref(pin), device, C.byref(pout)))
+    res.update(amplitude=pout.amplitude, device_ms=pout.device_ms, integrals=pout.integrals,
+               points=pout.points)
+    return res
+
+
+def precomputed_tables(cosmo, nz_z, nz_v, zmin, zmax, mmin, mmax, kmin, kmax, nbins, p_lens1,
+                       p_lens2=None, device=0):
+    """A tables.Tables for the model from precompute_tables and the lens redshift
+    distributions p_lens1/2 [nbins] on the same z grid (the inputs the reference's drivers
+    read next to the precomputed files)."""
+    from .tables import Cosmology, Tables
+    r = precompute_tables(cosmo, nz_z, nz_v, zmin, zmax, mmin, mmax, kmin, kmax, nbins, device)
+    c = [float(x) for x in cosmo]
+    p1 = np.ascontiguousarray(p_lens1, dtype=np.float64)
+    p2 = p1 if p_lens2 is None else np.ascontiguousarray(p_lens2, dtype=np.float64)
+    return Tables(Nz=nbins, Nm=nbins, Nk=nbins, zmin=zmin, zmax=zmax, mmin=mmin, mmax=mmax,
+                  kmin=kmin, kmax=kmax,
+                  cosmo=Cosmology(Om=c[0], OL=c[1], Ob=c[2], s8=c[3], h=c[4] / 100.0, ns=c[5],
+                                  H0_value=c[4]),
+                  g=r["g"], p_lens1=p1, p_lens2=p2, w=r["w"], dwdz=r["dwdz"], hmf=r["hmf"],
+                  P_lin=r["P_lin"], b_h=r["b_h"], conc=r["conc"],
+                  meta={"precompute": {k: r[k] for k in ("amplitude", "device_ms", "integrals",
+                                                         "points")}})
 
 
 def hcubature_v(f, dim, xmin, xmax, max_eval=0, rtol=1e-4, reqabs=0.0):

@@ -29,6 +29,7 @@ UNITS = {
     "evalmx_k1.cu": ["-fmad=true"],
     "host_api.cu": ["-fmad=false"],
     "probe.cu": ["-fmad=true"],
+    "precompute.cu": ["-fmad=false"],
 }
 HOST_UNITS = ["host_cubature.cpp", "host_model.cpp", "host_io.cpp"]
 

@@ -1,0 +1,735 @@
+// precompute.cu -- the reference's table precomputation on the device.
+//
+// doPrecomputations.x (src/doPrecomputations.cpp:40-134) fills the model's lookup
+// tables from a cosmology and a source redshift distribution: the lensing efficiency,
+// comoving distance and its derivative on the z grid (src/Cosmology.cpp:74-193), the
+// linear power spectrum (Eisenstein & Hu transfer function normalised to sigma8,
+// src/Powerspectrum.cpp:9-196), the concentration through M*(z) (:117-150, 296-313)
+// and the Sheth-Tormen mass function and halo bias (src/HMF.cpp:7-84).  Its cost is
+// ~28k adaptive 1-D integrals over k in [0, 1e12] for N = 64 bins (sigma^2 and
+// dsigma^2/dm at every (z, m), sigma^2 at 256 masses per z for M*), each one run by
+// the reference's hcubature_v on the host.
+//
+// Here every integral runs on the device.  One block integrates one integral at a
+// time (grid-stride over the integrals): thread 0 keeps the reference's max-heap of
+// regions with its running value/error sums, its Gladwell batch (pop the largest
+// errors until the rest is within tolerance), its cut and its push order, so the
+// refinement follows the reference's; the block's half-warps evaluate the 15-point
+// Gauss-Kronrod rule of one region each, and lane 0 of each half-warp forms the
+// rule's value and QUADPACK error in the reference's operation order
+// (src/hcubature.cpp:620-765, 772-1021).  The heap and the batch live in shared memory.
+// Integral parameters (radii, growth factors, grids) are computed on the host with
+// the reference's expressions; the integrands and the tables are evaluated here.
+// Compiled with -fmad=false, so results differ from the reference only by the
+// device libm's last-ulp differences in sin, cos, exp, log and pow.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "g3l_gpu.h"
+#include "host_internal.h"
+
+namespace g3l {
+namespace {
+
+constexpr int PC_THREADS = 128;
+// live regions of one integral (the heap) and regions of one round (the batch, at most
+// twice the heap): a first pass with 512 (48 KB of shared memory, 4 blocks per SM)
+// integrates almost everything; integrals that need more run again with 2048.
+constexpr int PC_CAP_SMALL = 512, PC_CAP_LARGE = 2048;
+constexpr int PC_MAX_ROUNDS = 4096;
+constexpr size_t pc_smem(int cap) { return sizeof(double) * 4 * (cap + 2 * cap); }
+
+// QUADPACK qk15 nodes and weights (the reference's rule15gauss, src/hcubature.cpp:626-660)
+__constant__ double cXgk[8] = {0.991455371120812639206854697526329, 0.949107912342758524526189684047851,
+                               0.864864423359769072789712788640926, 0.741531185599394439863864773280788,
+                               0.586087235467691130294144838258730, 0.405845151377397166906606412076961,
+                               0.207784955007898467600689403773245, 0.0};
+__constant__ double cWg[4] = {0.129484966168869693270611432679082, 0.279705391489276667901467771423780,
+                              0.381830050505118944950369775488975, 0.417959183673469387755102040816327};
+__constant__ double cWgk[8] = {0.022935322010529224963732008058970, 0.063092092629978553290700663189204,
+                               0.104790010322250183839876322541518, 0.140653259715525918745189590510238,
+                               0.169004726639267902826583426598550, 0.190350578064785409913256402421014,
+                               0.204432940075298892414161999234649, 0.209482141084727828012999174891714};
+
+constexpr double kPiTrunc = 3.14159;   // src/constants.h:15
+constexpr double kC = 2.99792e5;       // src/constants.h:39
+constexpr double kPi = 3.14159265358979323846;  // std::numbers::pi (src/Powerspectrum.cpp:69)
+
+// cosmology and Eisenstein & Hu transfer-function parameters (src/Powerspectrum.h:14-36)
+struct PkDev {
+    double Om, OL, H0, ns, rho_crit, amplitude;
+    double omhh, obhh, k_equality, sound_horizon, k_silk, alpha_c, beta_c, alpha_b, beta_b,
+        beta_node;
+};
+
+enum PcType { PC_AMP = 0, PC_SIGMA2 = 1, PC_DSIGMA2 = 2, PC_CHI = 3 };
+
+struct PcTask {
+    int type, pad;
+    double R, dR, gz;  // top-hat radius, dR/dm, growth(z)/growth(0)
+    double lo, hi;     // integration range
+};
+
+struct PcOut {
+    double val, err;
+    unsigned long long neval;
+    int status, rounds;
+};
+
+__device__ __forceinline__ double E_of(const PkDev &P, double z)
+{   // src/Cosmology.cpp:84-87
+    return P.Om * (1 + z) * (1 + z) * (1 + z) + P.OL;
+}
+__device__ __forceinline__ double Om_of(const PkDev &P, double z)
+{   // src/Cosmology.cpp:79-82
+    return P.Om * (1 + z) * (1 + z) * (1 + z) / E_of(P, z);
+}
+__device__ __forceinline__ double delta_c(const PkDev &P, double z)
+{   // src/Cosmology.cpp:74-77
+    return 1.686 * (1 + 0.0123 * log10(Om_of(P, z)));
+}
+__device__ __forceinline__ double tophat(double k, double R)
+{   // src/Powerspectrum.cpp:104-108
+    double x = k * R;
+    return 3 / x / x / x * (sin(x) - x * cos(x));
+}
+__device__ __forceinline__ double d_tophat(double k, double R)
+{   // src/Powerspectrum.cpp:110-114
+    double x = k * R;
+    return ((x * x - 3.) * sin(x) + 3. * x * cos(x)) * 3 * k / x / x / x / x;
+}
+
+__device__ double transfer(const PkDev &P, double k)
+{   // src/Powerspectrum.cpp:153-186
+    if (k == 0.0) return 1.0;
+    double q = k / 13.41 / P.k_equality;
+    double xx = k * P.sound_horizon;
+    double T_c_ln_beta = log(2.718282 + 1.8 * P.beta_c * q);
+    double T_c_ln_nobeta = log(2.718282 + 1.8 * q);
+    double T_c_C_alpha = 14.2 / P.alpha_c + 386.0 / (1.0 + 69.9 * pow(q, 1.08));
+    double T_c_C_noalpha = 14.2 + 386.0 / (1 + 69.9 * pow(q, 1.08));
+    double T_c_f = 1.0 / (1.0 + pow(xx / 5.4, 4));
+    double T_c = T_c_f * T_c_ln_beta / (T_c_ln_beta + T_c_C_noalpha * q * q) +
+                 (1. - T_c_f) * T_c_ln_beta / (T_c_ln_beta + T_c_C_alpha * q * q);
+    double s_tilde = P.sound_horizon * pow(1. + pow(P.beta_node / xx, 3), -1. / 3.);
+    double xx_tilde = k * s_tilde;
+    double T_b_T0 = T_c_ln_nobeta / (T_c_ln_nobeta + T_c_C_noalpha * q * q);
+    double T_b = sin(xx_tilde) / (xx_tilde) *
+                 (T_b_T0 / (1. + pow(xx / 5.2, 2)) +
+                  P.alpha_b / (1. + pow(P.beta_b / xx, 3)) * exp(-pow(k / P.k_silk, 1.4)));
+    double f_baryon = P.obhh / P.omhh;
+    return f_baryon * T_b + (1. - f_baryon) * T_c;
+}
+
+// P_lin(k, z) with gz = growth(z)/growth(0) (src/Powerspectrum.cpp:189-196)
+__device__ __forceinline__ double spectrum(const PkDev &P, double k, double gz)
+{
+    double trans = transfer(P, k);
+    return P.amplitude * trans * trans * gz * gz * pow(k, P.ns);
+}
+
+__device__ double integrand(const PkDev &P, const PcTask &t, double x)
+{
+    switch (t.type) {
+    case PC_AMP: {  // src/Powerspectrum.cpp:79-102
+        double R = 8. / P.H0 * 100;
+        double W = tophat(x, R);
+        double T = transfer(P, x);
+        return W * W * T * T * pow(x, P.ns + 2);
+    }
+    case PC_SIGMA2: {  // src/Powerspectrum.cpp:219-243
+        double W = tophat(x, t.R);
+        return x * x * W * W * spectrum(P, x, t.gz);
+    }
+    case PC_DSIGMA2: {  // src/Powerspectrum.cpp:267-293
+        double W = tophat(x, t.R);
+        double Wprime = d_tophat(x, t.R);
+        return x * x * W * Wprime * t.dR * spectrum(P, x, t.gz);
+    }
+    default:  // comoving distance integrand c/H0/sqrt(E(z)) (src/Cosmology.cpp:101-122)
+        return kC / P.H0 / sqrt(E_of(P, x));
+    }
+}
+
+// 15-point Gauss-Kronrod value and QUADPACK error of one region from its point values
+// in the reference's order (centre, then the Gauss pairs, then the Kronrod pairs)
+__device__ void rule_gk15(const double *vk, double hw, double &val, double &err)
+{
+    double rg = vk[0] * cWg[3], rk = vk[0] * cWgk[7];
+    double rabs = fabs(rk);
+    int n = 1;
+    for (int j = 0; j < 3; ++j) {
+        int j2 = 2 * j + 1;
+        double v = vk[n] + vk[n + 1];
+        rg += cWg[j] * v;
+        rk += cWgk[j2] * v;
+        rabs += cWgk[j2] * (fabs(vk[n]) + fabs(vk[n + 1]));
+        n += 2;
+    }
+    for (int j = 0; j < 4; ++j) {
+        int j2 = 2 * j;
+        rk += cWgk[j2] * (vk[n] + vk[n + 1]);
+        rabs += cWgk[j2] * (fabs(vk[n]) + fabs(vk[n + 1]));
+        n += 2;
+    }
+    val = rk * hw;
+    double mean = rk * 0.5;
+    double rasc = cWgk[7] * fabs(vk[0] - mean);
+    n = 1;
+    for (int j = 0; j < 3; ++j) {
+        int j2 = 2 * j + 1;
+        rasc += cWgk[j2] * (fabs(vk[n] - mean) + fabs(vk[n + 1] - mean));
+        n += 2;
+    }
+    for (int j = 0; j < 4; ++j) {
+        int j2 = 2 * j;
+        rasc += cWgk[j2] * (fabs(vk[n] - mean) + fabs(vk[n + 1] - mean));
+        n += 2;
+    }
+    double e = fabs(rk - rg) * hw;
+    rabs *= hw;
+    rasc *= hw;
+    if (rasc != 0 && e != 0) {
+        double scale = pow((200 * e / rasc), 1.5);
+        e = (scale < 1) ? rasc * scale : rasc;
+    }
+    if (rabs > DBL_MIN / (50 * DBL_EPSILON)) {
+        double min_err = 50 * DBL_EPSILON * rabs;
+        if (min_err > e) e = min_err;
+    }
+    err = e;
+}
+
+// the i-th Gauss-Kronrod abscissa of the region (c, hw), in the reference's order
+__device__ __forceinline__ double gk_point(double c, double hw, int i)
+{
+    if (i == 0) return c;
+    const int j = (i - 1) >> 1;  // pair index
+    const double w = i < 7 ? hw * cXgk[2 * j + 1] : hw * cXgk[2 * (j - 3)];
+    return (i & 1) ? c - w : c + w;
+}
+
+struct Heap {
+    double *c, *hw, *val, *err;
+};
+
+__device__ __forceinline__ bool converged(double err, double val)
+{   // src/converged.h:10-14 with reqAbs = 0, reqRel = 1e-4
+    return !(err > 0 && err > fabs(val) * 1e-4);
+}
+
+// the reference's heap discipline (src/hcubature.cpp:772-890), on shared arrays
+__device__ void heap_push(Heap H, int &n, double &hv, double &he, double c, double hw, double v,
+                          double e)
+{
+    hv += v;
+    he += e;
+    int ins = n++;
+    while (ins) {
+        int parent = (ins - 1) / 2;
+        if (e <= H.err[parent]) break;
+        H.c[ins] = H.c[parent];
+        H.hw[ins] = H.hw[parent];
+        H.val[ins] = H.val[parent];
+        H.err[ins] = H.err[parent];
+        ins = parent;
+    }
+    H.c[ins] = c;
+    H.hw[ins] = hw;
+    H.val[ins] = v;
+    H.err[ins] = e;
+}
+
+__device__ void heap_pop(Heap H, int &nn, double &hv, double &he, double &c, double &hw, double &v,
+                         double &e)
+{
+    c = H.c[0];
+    hw = H.hw[0];
+    v = H.val[0];
+    e = H.err[0];
+    const int n = nn - 1;
+    H.c[0] = H.c[n];
+    H.hw[0] = H.hw[n];
+    H.val[0] = H.val[n];
+    H.err[0] = H.err[n];
+    nn = n;
+    int i = 0, child;
+    while ((child = i * 2 + 1) < n) {
+        int largest = (H.err[child] <= H.err[i]) ? i : child;
+        if (++child < n && H.err[largest] < H.err[child]) largest = child;
+        if (largest == i) break;
+        double t;
+        t = H.c[i]; H.c[i] = H.c[largest]; H.c[largest] = t;
+        t = H.hw[i]; H.hw[i] = H.hw[largest]; H.hw[largest] = t;
+        t = H.val[i]; H.val[i] = H.val[largest]; H.val[largest] = t;
+        t = H.err[i]; H.err[i] = H.err[largest]; H.err[largest] = t;
+        i = largest;
+    }
+    hv -= v;
+    he -= e;
+}
+
+// One block per integral at a time.  Status: 0 ok, G3L_ERR_POOL (more than CAP live
+// regions), G3L_ERR_ROUNDS (more than PC_MAX_ROUNDS rounds).  idx: the integrals to run
+// (null: all ntask).
+template <int CAP>
+__global__ void __launch_bounds__(PC_THREADS) k_pc_integrate(const PkDev *__restrict__ Pp,
+                                                             const PcTask *__restrict__ tasks,
+                                                             const int *__restrict__ idx,
+                                                             int ntask, PcOut *__restrict__ out)
+{
+    constexpr int PC_CAP = CAP, PC_BATCH = 2 * CAP;
+    extern __shared__ double sm[];
+    Heap H{sm, sm + PC_CAP, sm + 2 * PC_CAP, sm + 3 * PC_CAP};
+    double *bc = sm + 4 * PC_CAP, *bh = bc + PC_BATCH, *bv = bh + PC_BATCH, *be = bv + PC_BATCH;
+    __shared__ int s_nb, s_done;
+    const PkDev P = *Pp;
+    const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+    const int warp = threadIdx.x >> 5, nwarps = PC_THREADS / 32;
+    for (int tj = blockIdx.x; tj < ntask; tj += gridDim.x) {
+        const int ti = idx ? idx[tj] : tj;
+        const PcTask t = tasks[ti];
+        // thread 0's state: heap size, running sums, counters
+        int n = 0, status = 0, rounds = 0;
+        double hv = 0, he = 0;
+        unsigned long long neval = 15;
+        if (threadIdx.x == 0) {
+            bc[0] = 0.5 * (t.lo + t.hi);
+            bh[0] = 0.5 * (t.hi - t.lo);
+            s_nb = 1;
+            s_done = 0;
+        }
+        __syncthreads();
+        while (true) {
+            // evaluate the batch: one region per half-warp, one point per lane
+            const int nb = s_nb;
+            for (int r0 = 2 * warp; r0 < nb; r0 += 2 * nwarps) {
+                const int r = r0 + half;
+                double f = 0;
+                if (r < nb && hl < 15) f = integrand(P, t, gk_point(bc[r], bh[r], hl));
+                double vk[15];
+#pragma unroll
+                for (int k = 0; k < 15; ++k) vk[k] = __shfl_sync(0xffffffffu, f, k, 16);
+                if (r < nb && hl == 0) rule_gk15(vk, bh[r], bv[r], be[r]);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int b = 0; b < nb; ++b) heap_push(H, n, hv, he, bc[b], bh[b], bv[b], be[b]);
+                int nbn = 0;
+                if (converged(he, hv)) {
+                    s_done = 1;
+                } else if (++rounds > PC_MAX_ROUNDS) {
+                    status = G3L_ERR_ROUNDS;
+                    s_done = 1;
+                } else {
+                    // Gladwell batch: pop until the error left is within tolerance
+                    double eErr = he;
+                    const double eVal = hv;
+                    do {
+                        // after this pop and the pushes the heap holds n + nbn + 1 regions
+                        if (n + nbn + 1 > PC_CAP) {
+                            status = G3L_ERR_POOL;
+                            s_done = 1;
+                            break;
+                        }
+                        double c, hw, v, e;
+                        heap_pop(H, n, hv, he, c, hw, v, e);
+                        eErr -= e;
+                        const double h2 = hw * 0.5;  // cut (src/hcubature.cpp:206-218)
+                        bc[nbn] = c - h2;
+                        bh[nbn] = h2;
+                        bc[nbn + 1] = c + h2;
+                        bh[nbn + 1] = h2;
+                        nbn += 2;
+                        neval += 30;
+                        if (converged(eErr, eVal)) break;
+                    } while (n > 0);
+                }
+                s_nb = nbn;
+            }
+            __syncthreads();
+            if (s_done) break;
+        }
+        if (threadIdx.x == 0) {
+            double v = 0, e = 0;
+            for (int i = 0; i < n; ++i) {
+                v += H.val[i];
+                e += H.err[i];
+            }
+            out[ti] = PcOut{v, e, neval, status, rounds};
+        }
+        __syncthreads();
+    }
+}
+
+// The tables from the integrals (one thread per (z, m/k) bin):
+//   g, w, dwdz [N]; P_lin, conc, hmf, b_h [N*N], z-major.
+struct TableArgs {
+    int N, Ns, Nstar;
+    const double *zs, *ms, *ks;         // grids [N]
+    const double *gz;                   // growth(z)/growth(0) [N]
+    const double *zsrc, *nzsrc;         // source n(z) [Ns]
+    const PcOut *chi_z, *chi_src;       // comoving distances [N], [Ns]
+    const PcOut *sig, *dsig, *sig_star; // [N*N], [N*N], [N*Nstar]
+    const double *mstar_grid;           // [Nstar]
+    double deltaZ;
+    double *g, *w, *dwdz, *P_lin, *conc, *hmf, *b_h;
+    int *mstar_ix;                      // [N]
+};
+
+__global__ void k_pc_zrow(const PkDev *__restrict__ Pp, TableArgs A)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.N) return;
+    const PkDev P = *Pp;
+    const double z = A.zs[i];
+    // lensing efficiency (src/Cosmology.cpp:132-150)
+    const double wz = A.chi_z[i].val;
+    double r = 0;
+    for (int j = 0; j < A.Ns; ++j) {
+        const double zp = A.zsrc[j];
+        const double wp = A.chi_src[j].val;
+        if (zp >= z) r += A.nzsrc[j] * (wp - wz) / wp;
+    }
+    A.g[i] = r * A.deltaZ;
+    A.w[i] = wz;
+    A.dwdz[i] = kC / P.H0 / sqrt(E_of(P, z));  // src/Cosmology.cpp:101-104
+    // M*(z): the first of the masses closest to sigma = delta_c (src/Powerspectrum.cpp:117-140)
+    const double dc = delta_c(P, z);
+    int best = 0;
+    double bd = 0;
+    for (int j = 0; j < A.Nstar; ++j) {
+        const double s2 = A.sig_star[(size_t)i * A.Nstar + j].val / 2 / kPi / kPi;
+        const double diff = dc - sqrt(s2);
+        const double d = sqrt(diff * diff);
+        if (j == 0 || d < bd) {
+            bd = d;
+            best = j;
+        }
+    }
+    A.mstar_ix[i] = best;
+}
+
+__global__ void k_pc_table(const PkDev *__restrict__ Pp, TableArgs A)
+{
+    const int ij = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ij >= A.N * A.N) return;
+    const int i = ij / A.N, j = ij % A.N;
+    const PkDev P = *Pp;
+    const double z = A.zs[i], m = A.ms[j];
+    A.P_lin[ij] = spectrum(P, A.ks[j], A.gz[i]);
+    const double mstar = A.mstar_grid[A.mstar_ix[i]];
+    A.conc[ij] = 9 / (1. + z) * pow(m / mstar, -0.13);  // src/Powerspectrum.cpp:143-150
+    // Sheth-Tormen n(m, z) and b_h (src/HMF.cpp:7-49)
+    const double sigma2 = A.sig[ij].val / 2 / kPi / kPi;
+    const double dsigma2 = A.dsig[ij].val / kPi / kPi;
+    const double dc = delta_c(P, z);
+    {
+        const double Af = 0.322, q = 0.707, p = 0.3;
+        const double rho_mean = Om_of(P, z) * P.rho_crit;
+        const double nuSq = dc * dc / sigma2;
+        A.hmf[ij] = -rho_mean / m / sigma2 * dsigma2 * Af * (1 + pow(q * nuSq, -p)) *
+                    sqrt(q * nuSq / 2 / kPiTrunc) * exp(-0.5 * q * nuSq);
+    }
+    {
+        const double q = 0.707, p = 0.3;
+        A.b_h[ij] = 1 + 1. / dc * (q * dc * dc / sigma2 - 1 + 2 * p / (1 + pow(q * dc * dc / sigma2, p)));
+    }
+}
+
+#define PC_CK(call)                                                                      \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            host::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));         \
+            return G3L_ERR_CUDA;                                                         \
+        }                                                                                \
+    } while (0)
+
+// host-side Om(z), growth and the transfer-function parameters, with the reference's
+// expressions (src/Cosmology.cpp:79-129, src/Powerspectrum.cpp:15-65)
+double h_E(const PkDev &P, double z) { return P.Om * (1 + z) * (1 + z) * (1 + z) + P.OL; }
+double h_Om(const PkDev &P, double z) { return P.Om * (1 + z) * (1 + z) * (1 + z) / h_E(P, z); }
+double h_growth(const PkDev &P, double z)
+{
+    double om_m = h_Om(P, z);
+    return 2.5 / (z + 1) * om_m / (std::pow(om_m, 4. / 7.) - P.OL + (1. + 0.5 * om_m) * (1 + P.OL / 70));
+}
+
+void transfer_parameters(PkDev &P, double Ob)
+{
+    const double h = P.H0 / 100;
+    const double omhh = P.Om * h * h, obhh = Ob * h * h;
+    P.omhh = omhh;
+    P.obhh = obhh;
+    const double f_baryon = obhh / omhh;
+    const double Tcmb = 2.72548;
+    const double theta_cmb = Tcmb / 2.7;
+    const double theta_cmbSq = theta_cmb * theta_cmb;
+    const double theta_cmb4 = theta_cmbSq * theta_cmbSq;
+    const double z_equality = 2.50e4 * omhh / theta_cmb4;
+    P.k_equality = 0.0746 * omhh / theta_cmbSq;
+    const double z_drag_b1 = 0.313 * std::pow(omhh, -0.419) * (1.0 + 0.607 * std::pow(omhh, 0.674));
+    const double z_drag_b2 = 0.238 * std::pow(omhh, 0.223);
+    const double z_drag = 1291.0 * std::pow(omhh, 0.251) / (1.0 + 0.659 * std::pow(omhh, 0.828)) *
+                          (1.0 + z_drag_b1 * std::pow(obhh, z_drag_b2));
+    const double R_drag = 31.5 * obhh / (theta_cmb4) * (1000.0 / (1.0 + z_drag));
+    const double R_equality = 31.5 * obhh / (theta_cmb4) * (1000.0 / z_equality);
+    P.sound_horizon = 2.0 / 3.0 / P.k_equality * std::sqrt(6.0 / R_equality) *
+                      std::log((std::sqrt(1.0 + R_drag) + std::sqrt(R_drag + R_equality)) /
+                               (1.0 + std::sqrt(R_equality)));
+    P.k_silk = 1.6 * std::pow(obhh, 0.52) * std::pow(omhh, 0.73) * (1.0 + std::pow(10.4 * omhh, -0.95));
+    const double alpha_c_a1 = std::pow(46.9 * omhh, 0.670) * (1.0 + std::pow(32.1 * omhh, -0.532));
+    const double alpha_c_a2 = std::pow(12.0 * omhh, 0.424) * (1.0 + std::pow(45.0 * omhh, -0.582));
+    P.alpha_c = std::pow(alpha_c_a1, -f_baryon) * std::pow(alpha_c_a2, -std::pow(f_baryon, 3));
+    const double beta_c_b1 = 0.944 / (1.0 + std::pow(458.0 * omhh, -0.708));
+    const double beta_c_b2 = std::pow(0.395 * omhh, -0.0266);
+    P.beta_c = 1.0 / (1.0 + beta_c_b1 * (std::pow(1.0 - f_baryon, beta_c_b2) - 1.0));
+    const double y = z_equality / (1.0 + z_drag);
+    const double alpha_b_G =
+        y * (-6.0 * std::sqrt(1.0 + y) +
+             (2.0 + 3.0 * y) * std::log((std::sqrt(1.0 + y) + 1.0) / (std::sqrt(1.0 + y) - 1.0)));
+    P.alpha_b = 2.07 * P.k_equality * P.sound_horizon * std::pow(1.0 + R_drag, -0.75) * alpha_b_G;
+    P.beta_node = 8.41 * std::pow(omhh, 0.435);
+    P.beta_b = 0.5 + f_baryon + (3.0 - 2.0 * f_baryon) * std::sqrt(std::pow(17.2 * omhh, 2.0) + 1.0);
+}
+
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+    cudaError_t alloc(size_t n) { return cudaMalloc((void **)&p, (n ? n : 1) * sizeof(T)); }
+};
+
+template <typename T>
+cudaError_t upload(DevBuf<T> &b, const std::vector<T> &v, cudaStream_t s)
+{
+    cudaError_t e = b.alloc(v.size());
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+int run_tasks(const PkDev *dP, const std::vector<PcTask> &tasks, std::vector<PcOut> &res,
+              DevBuf<PcOut> &dres, cudaStream_t s, int nsm)
+{
+    DevBuf<PcTask> dt;
+    PC_CK(upload(dt, tasks, s));
+    PC_CK(dres.alloc(tasks.size()));
+    const int n = (int)tasks.size();
+    k_pc_integrate<PC_CAP_SMALL><<<std::min(n, nsm * 4), PC_THREADS, pc_smem(PC_CAP_SMALL), s>>>(
+        dP, dt.p, nullptr, n, dres.p);
+    PC_CK(cudaGetLastError());
+    res.resize(n);
+    PC_CK(cudaMemcpyAsync(res.data(), dres.p, n * sizeof(PcOut), cudaMemcpyDeviceToHost, s));
+    PC_CK(cudaStreamSynchronize(s));
+    std::vector<int> big;
+    for (int i = 0; i < n; ++i)
+        if (res[i].status == G3L_ERR_POOL) big.push_back(i);
+    if (!big.empty()) {
+        DevBuf<int> di;
+        PC_CK(upload(di, big, s));
+        const int nb = (int)big.size();
+        k_pc_integrate<PC_CAP_LARGE><<<std::min(nb, nsm), PC_THREADS, pc_smem(PC_CAP_LARGE), s>>>(
+            dP, dt.p, di.p, nb, dres.p);
+        PC_CK(cudaGetLastError());
+        PC_CK(cudaMemcpyAsync(res.data(), dres.p, n * sizeof(PcOut), cudaMemcpyDeviceToHost, s));
+        PC_CK(cudaStreamSynchronize(s));
+    }
+    for (const PcOut &o : res)
+        if (o.status) {
+            host::set_error(o.status == G3L_ERR_POOL
+                                ? "g3l_precompute_tables: an integral needed more than 2048 regions"
+                                : "g3l_precompute_tables: an integral exceeded 4096 rounds");
+            return o.status;
+        }
+    return G3L_OK;
+}
+
+}  // namespace
+}  // namespace g3l
+
+using namespace g3l;
+
+extern "C" int g3l_precompute_tables(const g3l_precompute_in *in, int device,
+                                     g3l_precompute_out *out)
+{
+    if (!in || !out || in->nbins < 1 || in->n_nz < 1 || !in->nz_z || !in->nz_v ||
+        !(in->mmin > 0 && in->mmax > in->mmin && in->kmin > 0 && in->kmax > in->kmin &&
+          in->zmax > in->zmin && in->zmin >= 0) ||
+        !out->g || !out->w || !out->dwdz || !out->P_lin || !out->conc || !out->hmf || !out->b_h) {
+        host::set_error("g3l_precompute_tables: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    for (int k = 0; k < 6; ++k)
+        if (!std::isfinite(in->cosmo[k])) {
+            host::set_error("g3l_precompute_tables: non-finite cosmology");
+            return G3L_ERR_INVALID;
+        }
+    PC_CK(cudaSetDevice(device));
+    int nsm = 0;
+    PC_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+    PC_CK(cudaFuncSetAttribute(k_pc_integrate<PC_CAP_SMALL>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)pc_smem(PC_CAP_SMALL)));
+    PC_CK(cudaFuncSetAttribute(k_pc_integrate<PC_CAP_LARGE>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)pc_smem(PC_CAP_LARGE)));
+    cudaStream_t s;
+    PC_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    struct StreamGuard {
+        cudaStream_t s;
+        ~StreamGuard() { cudaStreamDestroy(s); }
+    } sg{s};
+    cudaEvent_t e0, e1;
+    PC_CK(cudaEventCreate(&e0));
+    PC_CK(cudaEventCreate(&e1));
+    struct EvGuard {
+        cudaEvent_t a, b;
+        ~EvGuard()
+        {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } eg{e0, e1};
+    PC_CK(cudaEventRecord(e0, s));
+
+    const int N = in->nbins, Ns = in->n_nz, Nstar = 256;
+    PkDev P{};
+    P.Om = in->cosmo[0];
+    P.OL = in->cosmo[1];
+    P.H0 = in->cosmo[4];
+    P.ns = in->cosmo[5];
+    P.rho_crit = 3 * P.H0 * P.H0 * 3.086e19 / 8 / kPiTrunc / 1.327e11;  // src/Cosmology.h:41-47
+    transfer_parameters(P, in->cosmo[2]);
+    // grids (src/doPrecomputations.cpp:43-54) and M*'s mass grid (src/Powerspectrum.cpp:122-131)
+    const double z_bin = (in->zmax - in->zmin) / N, m_bin = std::log(in->mmax / in->mmin) / N,
+                 k_bin = std::log(in->kmax / in->kmin) / N;
+    std::vector<double> zs(N), ms(N), ks(N), gzs(N), mst(Nstar);
+    for (int i = 0; i < N; ++i) {
+        zs[i] = in->zmin + i * z_bin;
+        ms[i] = std::exp(std::log(in->mmin) + m_bin * i);
+        ks[i] = std::exp(std::log(in->kmin) + k_bin * i);
+        gzs[i] = h_growth(P, zs[i]) / h_growth(P, 0.0);
+    }
+    const double ms_bin = std::log(1e18 / 1e10) / Nstar;
+    for (int j = 0; j < Nstar; ++j) mst[j] = std::exp(std::log(1e10) + ms_bin * j);
+
+    // pass 1: the amplitude (src/Powerspectrum.cpp:67-77) and the comoving distances
+    std::vector<PcTask> t1;
+    t1.push_back(PcTask{PC_AMP, 0, 0, 0, 0, 0.0, 1e12});
+    for (int i = 0; i < N; ++i) t1.push_back(PcTask{PC_CHI, 0, 0, 0, 0, 0.0, zs[i]});
+    for (int j = 0; j < Ns; ++j) t1.push_back(PcTask{PC_CHI, 0, 0, 0, 0, 0.0, in->nz_z[j]});
+    DevBuf<PkDev> dP;
+    PC_CK(dP.alloc(1));
+    PC_CK(cudaMemcpyAsync(dP.p, &P, sizeof P, cudaMemcpyHostToDevice, s));
+    std::vector<PcOut> r1;
+    DevBuf<PcOut> dr1;
+    int st = run_tasks(dP.p, t1, r1, dr1, s, nsm);
+    if (st) return st;
+    const double factor = kPi * in->cosmo[3];
+    P.amplitude = 2 * factor * factor / r1[0].val;
+    PC_CK(cudaMemcpyAsync(dP.p, &P, sizeof P, cudaMemcpyHostToDevice, s));
+
+    // pass 2: sigma^2 and dsigma^2/dm at every (z, m), sigma^2 on M*'s grid
+    // (radii: src/Powerspectrum.cpp:201-202, 249-251)
+    std::vector<PcTask> t2;
+    t2.reserve((size_t)N * (2 * N + Nstar));
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) {
+            const double om = h_Om(P, zs[i]);
+            t2.push_back(PcTask{PC_SIGMA2, 0, std::pow(0.75 / kPi * ms[j] / P.rho_crit / om, 1. / 3.),
+                                0, gzs[i], 0.0, 1e12});
+        }
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) {
+            const double rho_m = P.rho_crit * h_Om(P, zs[i]);
+            t2.push_back(PcTask{PC_DSIGMA2, 0, 0.6204 * std::pow(ms[j] / rho_m, 1. / 3.),
+                                0.2068 * std::pow(rho_m * ms[j] * ms[j], -1. / 3.), gzs[i], 0.0,
+                                1e12});
+        }
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < Nstar; ++j) {
+            const double om = h_Om(P, zs[i]);
+            t2.push_back(PcTask{PC_SIGMA2, 0, std::pow(0.75 / kPi * mst[j] / P.rho_crit / om, 1. / 3.),
+                                0, gzs[i], 0.0, 1e12});
+        }
+    std::vector<PcOut> r2;
+    DevBuf<PcOut> dr2;
+    st = run_tasks(dP.p, t2, r2, dr2, s, nsm);
+    if (st) return st;
+
+    // the tables
+    DevBuf<double> dzs, dms, dks, dgz, dzsrc, dnz, dmst, dg, dw, ddw, dpl, dcn, dhm, dbh;
+    DevBuf<int> dmix;
+    PC_CK(upload(dzs, zs, s));
+    PC_CK(upload(dms, ms, s));
+    PC_CK(upload(dks, ks, s));
+    PC_CK(upload(dgz, gzs, s));
+    PC_CK(upload(dzsrc, std::vector<double>(in->nz_z, in->nz_z + Ns), s));
+    PC_CK(upload(dnz, std::vector<double>(in->nz_v, in->nz_v + Ns), s));
+    PC_CK(upload(dmst, mst, s));
+    const size_t NN = (size_t)N * N;
+    PC_CK(dg.alloc(N));
+    PC_CK(dw.alloc(N));
+    PC_CK(ddw.alloc(N));
+    PC_CK(dpl.alloc(NN));
+    PC_CK(dcn.alloc(NN));
+    PC_CK(dhm.alloc(NN));
+    PC_CK(dbh.alloc(NN));
+    PC_CK(dmix.alloc(N));
+    TableArgs A{};
+    A.N = N;
+    A.Ns = Ns;
+    A.Nstar = Nstar;
+    A.zs = dzs.p;
+    A.ms = dms.p;
+    A.ks = dks.p;
+    A.gz = dgz.p;
+    A.zsrc = dzsrc.p;
+    A.nzsrc = dnz.p;
+    A.chi_z = dr1.p + 1;
+    A.chi_src = dr1.p + 1 + N;
+    A.sig = dr2.p;
+    A.dsig = dr2.p + NN;
+    A.sig_star = dr2.p + 2 * NN;
+    A.mstar_grid = dmst.p;
+    A.deltaZ = (in->nz_z[Ns - 1] - in->nz_z[0]) / Ns;  // src/Cosmology.cpp:137
+    A.g = dg.p;
+    A.w = dw.p;
+    A.dwdz = ddw.p;
+    A.P_lin = dpl.p;
+    A.conc = dcn.p;
+    A.hmf = dhm.p;
+    A.b_h = dbh.p;
+    A.mstar_ix = dmix.p;
+    k_pc_zrow<<<(N + 127) / 128, 128, 0, s>>>(dP.p, A);
+    PC_CK(cudaGetLastError());
+    k_pc_table<<<(int)((NN + 127) / 128), 128, 0, s>>>(dP.p, A);
+    PC_CK(cudaGetLastError());
+    PC_CK(cudaEventRecord(e1, s));
+    PC_CK(cudaMemcpyAsync(out->g, dg.p, N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PC_CK(cudaMemcpyAsync(out->w, dw.p, N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PC_CK(cudaMemcpyAsync(out->dwdz, ddw.p, N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PC_CK(cudaMemcpyAsync(out->P_lin, dpl.p, NN * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PC_CK(cudaMemcpyAsync(out->conc, dcn.p, NN * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PC_CK(cudaMemcpyAsync(out->hmf, dhm.p, NN * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PC_CK(cudaMemcpyAsync(out->b_h, dbh.p, NN * sizeof(double), cudaMemcpyDeviceToHost, s));
+    PC_CK(cudaStreamSynchronize(s));
+    float ms_ = 0;
+    PC_CK(cudaEventElapsedTime(&ms_, e0, e1));
+    out->device_ms = ms_;
+    out->amplitude = P.amplitude;
+    out->integrals = (long long)(t1.size() + t2.size());
+    unsigned long long ne = 0;
+    for (const PcOut &o : r1) ne += o.neval;
+    for (const PcOut &o : r2) ne += o.neval;
+    out->points = (long long)ne;
+    return G3L_OK;
+}

@@ -300,6 +300,34 @@ int g3l_hcubature_v(unsigned fdim, g3l_integrand_v f, void *fdata, unsigned dim,
                     const double *xmin, const double *xmax, size_t maxEval, double reqAbsError,
                     double reqRelError, int norm, double *val, double *err);
 
+/* The reference's table precomputation (doPrecomputations.x,
+ * src/doPrecomputations.cpp:40-134) on the device: from a flat LCDM cosmology and a
+ * source redshift distribution, the lensing efficiency, comoving distance and its
+ * derivative on nbins z bins (src/Cosmology.cpp:74-193), the linear power spectrum
+ * (Eisenstein & Hu transfer function normalised to sigma8, src/Powerspectrum.cpp:9-196)
+ * on z x k, and the concentration, Sheth-Tormen mass function and halo bias on z x m
+ * (src/Powerspectrum.cpp:117-150, src/HMF.cpp:7-84).  Grids as the reference's:
+ * z_i = zmin + i (zmax-zmin)/nbins, m_j and k_j logarithmic from mmin and kmin.
+ * Every adaptive 1-D integral (sigma^2, dsigma^2/dm, M*, the amplitude, the comoving
+ * distances) runs on the device with the reference's refinement.  The lens
+ * distributions p_lens1/2 are inputs of the model, not outputs of this step. */
+typedef struct g3l_precompute_in {
+    double cosmo[6];            /* Om, OL, Ob, sigma8, H0 [km/s/Mpc], ns */
+    const double *nz_z, *nz_v;  /* source n(z): redshifts and values [n_nz], as read
+                                   from the reference's n(z) file */
+    int n_nz;
+    double zmin, zmax, mmin, mmax, kmin, kmax;
+    int nbins;
+} g3l_precompute_in;
+typedef struct g3l_precompute_out {
+    double *g, *w, *dwdz;              /* caller's arrays [nbins] */
+    double *P_lin, *conc, *hmf, *b_h;  /* caller's arrays [nbins*nbins], z-major */
+    double amplitude;                  /* P(k) normalisation [Mpc^3] */
+    double device_ms;                  /* device time of the computation */
+    long long integrals, points;       /* 1-D integrals and integrand evaluations */
+} g3l_precompute_out;
+int g3l_precompute_tables(const g3l_precompute_in *in, int device, g3l_precompute_out *out);
+
 /* The reference's ASCII inputs, read as its drivers read them (host only, no device
  * work).  Numbers are parsed by C++ stream extraction; reading stops at the first
  * token that is not a number.  Where the reference exits or reads undefined values,

@@ -21,6 +21,12 @@ pids=()
 for f in hcubature Cosmology Params Function Function2D; do
     g++ $CXXF -c "$REF/$f.cpp" -o "$OUT/obj/$f.o" & pids+=($!)
 done
+# the table precomputation (doPrecomputations.x); it needs C++20 for <numbers>, and
+# Powerspectrum.cpp uses std::min_element without including <algorithm>
+for f in Powerspectrum HMF; do
+    g++ ${CXXF/-std=c++17/-std=c++20} -include algorithm -c "$REF/$f.cpp" -o "$OUT/obj/$f.o" &
+    pids+=($!)
+done
 for f in HOD generalFunctions NNMap_Model NMapMap_Model; do
     nvcc $NVF -c "$REF/$f.cu" -o "$OUT/obj/$f.o" 2> "$OUT/obj/$f.log" & pids+=($!)
 done

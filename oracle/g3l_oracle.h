@@ -105,6 +105,33 @@ int  orc_rule75_region(const orc_model *M, int kind, int term, const double th[3
                        int type1, int type2, const double *center, const double *halfwidth,
                        double vol, double *val, double *err, int *split);
 
+/* ---- table precomputation (precompute.c; src/doPrecomputations.cpp) ---- */
+typedef struct {
+    double Om, OL, Ob, s8, H0, ns, rho_crit;
+    /* Eisenstein & Hu transfer-function parameters (src/Powerspectrum.h:14-36) */
+    double omhh, obhh, theta_cmb, z_equality, k_equality, z_drag, R_drag, R_equality,
+        sound_horizon, k_silk, alpha_c, beta_c, alpha_b, beta_b, beta_node;
+    double amplitude; /* P(k) normalisation to sigma8 [Mpc^3] */
+} orc_pk;
+
+int    orc_pk_init(orc_pk *P, const double cosmo[6]); /* {Om, OL, Ob, sigma8, H0, ns} */
+double orc_transfer(const orc_pk *P, double k);
+double orc_spectrum(const orc_pk *P, double k, double z);
+double orc_sigma2(const orc_pk *P, double m, double z);
+double orc_dsigma2dm(const orc_pk *P, double m, double z);
+double orc_delta_c(const orc_pk *P, double z);
+double orc_mstar(const orc_pk *P, double z);
+double orc_concentration(double m, double mstar, double z);
+double orc_hmf(const orc_pk *P, double m, double z);
+double orc_halo_bias(const orc_pk *P, double m, double z);
+double orc_comoving(const orc_pk *P, double z);
+double orc_dcomoving(const orc_pk *P, double z);
+/* the whole of doPrecomputations.x on N bins; 2-D outputs z-major [N*N] */
+int orc_precompute(const double cosmo[6], const double *zs_src, const double *nz_src, int Ns,
+                   double zmin, double zmax, double mmin, double mmax, double kmin, double kmax,
+                   int N, double *g, double *w, double *dwdz, double *P_lin, double *conc,
+                   double *hmf, double *b_h);
+
 #ifdef __cplusplus
 }
 #endif

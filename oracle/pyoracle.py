@@ -27,12 +27,14 @@ _dp = C.POINTER(C.c_double)
 
 
 def build_oracle(force: bool = False) -> str:
-    src = os.path.join(HERE, "g3l_oracle.c")
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("g3l_oracle.c", "precompute.c")]
+    deps = srcs + [os.path.join(HERE, "g3l_oracle.h")]
+    if force or not os.path.exists(LIB) or any(os.path.getmtime(LIB) < os.path.getmtime(s)
+                                               for s in deps):
         os.makedirs(BUILD, exist_ok=True)
         tmp = LIB + ".tmp%d" % os.getpid()
         subprocess.check_call(["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-                               "-o", tmp, src, "-lm"])
+                               "-o", tmp] + srcs + ["-lm"])
         os.replace(tmp, LIB)
     return LIB
 
@@ -100,6 +102,22 @@ def lib():
                                       C.POINTER(C.c_size_t)]
         _lib = L
     return _lib
+
+
+def precompute(cosmo, nz_z, nz_v, zmin, zmax, mmin, mmax, kmin, kmax, N):
+    """The restated doPrecomputations pipeline (precompute.c): dict of g, w, dwdz [N] and
+    P_lin, conc, hmf, b_h [N, N], z-major."""
+    L = lib()
+    L.orc_precompute.argtypes = [_dp, _dp, _dp, C.c_int] + [C.c_double] * 6 + [C.c_int] + [_dp] * 7
+    c = np.ascontiguousarray(cosmo, dtype=np.float64)
+    zz = np.ascontiguousarray(nz_z, dtype=np.float64)
+    zv = np.ascontiguousarray(nz_v, dtype=np.float64)
+    N = int(N)
+    res = {k: np.zeros(N) for k in ("g", "w", "dwdz")}
+    res.update({k: np.zeros((N, N)) for k in ("P_lin", "conc", "hmf", "b_h")})
+    L.orc_precompute(_ptr(c), _ptr(zz), _ptr(zv), len(zz), zmin, zmax, mmin, mmax, kmin, kmax, N,
+                     *[_ptr(res[k]) for k in ("g", "w", "dwdz", "P_lin", "conc", "hmf", "b_h")])
+    return res
 
 
 INTEGRAND_V = C.CFUNCTYPE(C.c_int, C.c_uint, C.c_size_t, _dp, C.c_void_p, C.c_uint, _dp)

@@ -15,10 +15,12 @@
 #include "Cosmology.h"
 #include "Function.h"
 #include "Function2D.h"
+#include "HMF.h"
 #include "HOD.h"
 #include "NMapMap_Model.h"
 #include "NNMap_Model.h"
 #include "Params.h"
+#include "Powerspectrum.h"
 #include "cubature.h"
 #include "generalFunctions.h"
 
@@ -350,6 +352,72 @@ int ref_hcubature_v(unsigned fdim, integrand_v f, void *fdata, unsigned dim, con
     *neval = cnt.n;
     return st;
 }
+
+#if !SCALING
+// doPrecomputations.x without its file I/O (src/doPrecomputations.cpp:40-134): the
+// same objects and calls, in the same order, on the same grids.  nz_z / nz_v: the
+// source redshift distribution as the driver holds it (Function x / y values).
+// 2-D outputs are z-major [N*N].  Also returns the power-spectrum amplitude.
+void ref_precompute(const double *cosmo, const double *nz_z, const double *nz_v, int Ns,
+                    double z_min, double z_max, double m_min, double m_max, double k_min,
+                    double k_max, int Nbins, double *g, double *w, double *dwdz, double *P_lin,
+                    double *conc, double *hmf_out, double *b_h, double *amplitude)
+{
+    double z_bin = (z_max - z_min) / Nbins;
+    double m_bin = log(m_max / m_min) / Nbins;
+    double k_bin = log(k_max / k_min) / Nbins;
+    std::vector<double> zs, ms, ks;
+    for (int i = 0; i < Nbins; i++) {
+        zs.push_back(z_min + i * z_bin);
+        ms.push_back(exp(log(m_min) + m_bin * i));
+        ks.push_back(exp(log(k_min) + k_bin * i));
+    }
+    std::vector<double> nzx(nz_z, nz_z + Ns), nzy(nz_v, nz_v + Ns);
+    g3lhalo::Cosmology cosmology(cosmo[0], cosmo[1], cosmo[2], cosmo[3], cosmo[4], cosmo[5]);
+    std::vector<double> v;
+    cosmology.getLensingEfficiency(zs, nzy, nzx, v);
+    std::memcpy(g, v.data(), sizeof(double) * Nbins);
+    v.clear();
+    cosmology.getComovingDistance(zs, v);
+    std::memcpy(w, v.data(), sizeof(double) * Nbins);
+    v.clear();
+    cosmology.getDerivativeComovingDistance(zs, v);
+    std::memcpy(dwdz, v.data(), sizeof(double) * Nbins);
+    g3lhalo::Powerspectrum powerspectrum(&cosmology);
+    *amplitude = powerspectrum.amplitude;
+    v.clear();
+    powerspectrum.getSpectrum(zs, ks, v);
+    std::memcpy(P_lin, v.data(), sizeof(double) * Nbins * Nbins);
+    v.clear();
+    powerspectrum.getConcentration(zs, ms, v);
+    std::memcpy(conc, v.data(), sizeof(double) * Nbins * Nbins);
+    g3lhalo::Halomassfunction hmf(&cosmology, &powerspectrum);
+    v.clear();
+    hmf.getHMF(zs, ms, v);
+    std::memcpy(hmf_out, v.data(), sizeof(double) * Nbins * Nbins);
+    v.clear();
+    hmf.getHaloBias(zs, ms, v);
+    std::memcpy(b_h, v.data(), sizeof(double) * Nbins * Nbins);
+}
+
+// single pieces, for point-level pinning
+double ref_pk_piece(const double *cosmo, int what, double a, double b)
+{
+    g3lhalo::Cosmology c(cosmo[0], cosmo[1], cosmo[2], cosmo[3], cosmo[4], cosmo[5]);
+    g3lhalo::Powerspectrum p(&c);
+    g3lhalo::Halomassfunction h(&c, &p);
+    switch (what) {
+    case 0: return p.amplitude;
+    case 1: return p.transfer(a);
+    case 2: return p.spectrum(a, b);
+    case 3: return p.sigma2(a, b);
+    case 4: return p.mStar(a);
+    case 5: return h.b_h(a, b);
+    case 6: return c.comovingDistance(a);
+    default: return 0;
+    }
+}
+#endif
 
 // The reference's ASCII readers as its drivers use them (src/calculateNNMap.cu:42-72).
 // They exit() or throw on bad input, so callers pass valid files only.

@@ -3,6 +3,7 @@
 Run from the repository root where the reference sources exist:
     python tests/golden/make_golden.py            # ref_n64.npz
     python tests/golden/make_golden.py --scaling  # ref_scaling_n64.npz
+    python tests/golden/make_golden.py --precompute  # ref_precompute.npz
 It builds oracle/_ref/libg3lref.so and libg3lref_scaling.so (oracle/build_ref.sh)
 from the reference's unmodified sources, drives NNMap_Model / NMapMap_Model /
 hcubature_v in memory through oracle/ref_harness.cu, and writes the fixture.  The
@@ -27,6 +28,20 @@ import pyoracle as P  # noqa: E402
 
 OUT = os.path.join(ROOT, "tests", "golden", "ref_n64.npz")
 OUT_SCALING = os.path.join(ROOT, "tests", "golden", "ref_scaling_n64.npz")
+OUT_PRECOMPUTE = os.path.join(ROOT, "tests", "golden", "ref_precompute.npz")
+
+# doPrecomputations inputs: (cosmology [Om, OL, Ob, sigma8, H0, ns], zmin, zmax, mmin, mmax,
+# kmin, kmax, nbins); the source n(z) is a smooth seeded stand-in for the survey's file
+PRECOMPUTE_CASES = [
+    ((0.3, 0.7, 0.045, 0.8, 70.0, 0.96), 0.1, 2.0, 1e10, 1e17, 0.01, 1000.0, 16),
+    ((0.3089, 0.6911, 0.0486, 0.8159, 67.74, 0.9667), 0.001, 1.5, 1e9, 1e16, 1e-3, 1e4, 12),
+]
+
+
+def source_nz(n=60, zmax=3.0, z0=0.5):
+    z = np.linspace(0.0, zmax, n)
+    v = z * z * np.exp(-(z / z0) ** 1.5)
+    return z, v / (v.sum() * (z[1] - z[0]))
 
 # analytic integrands for the engine-only vectors (Genz test families)
 def genz_gauss(x):
@@ -186,8 +201,37 @@ def main_scaling():
     print("wrote", OUT_SCALING, os.path.getsize(OUT_SCALING), "bytes")
 
 
+def main_precompute():
+    """Tables of the reference's doPrecomputations pipeline (in memory, no 6-digit files)."""
+    import ctypes as C
+    P.build_ref()
+    R = P.ref_lib()
+    dp = P._dp
+    R.ref_precompute.argtypes = [dp, dp, dp, C.c_int] + [C.c_double] * 6 + [C.c_int] + [dp] * 8
+    zsrc, nz = source_nz()
+    out = {"nz_z": zsrc, "nz_v": nz}
+    for ci, (cosmo, zmin, zmax, mmin, mmax, kmin, kmax, N) in enumerate(PRECOMPUTE_CASES):
+        c = np.array(cosmo, dtype=np.float64)
+        res = {k: np.zeros(N) for k in ("g", "w", "dwdz")}
+        res.update({k: np.zeros(N * N) for k in ("P_lin", "conc", "hmf", "b_h")})
+        amp = np.zeros(1)
+        R.ref_precompute(P._ptr(c), P._ptr(zsrc), P._ptr(nz), len(zsrc), zmin, zmax, mmin, mmax,
+                         kmin, kmax, N, *[P._ptr(res[k]) for k in
+                                          ("g", "w", "dwdz", "P_lin", "conc", "hmf", "b_h")],
+                         P._ptr(amp))
+        out[f"c{ci}_in"] = np.array([zmin, zmax, mmin, mmax, kmin, kmax, N], dtype=np.float64)
+        out[f"c{ci}_cosmo"] = c
+        out[f"c{ci}_amplitude"] = amp
+        for k, v in res.items():
+            out[f"c{ci}_{k}"] = v.reshape(N, N) if v.size == N * N else v
+    np.savez_compressed(OUT_PRECOMPUTE, **out)
+    print("wrote", OUT_PRECOMPUTE, os.path.getsize(OUT_PRECOMPUTE), "bytes")
+
+
 if __name__ == "__main__":
     if "--scaling" in sys.argv[1:]:
         main_scaling()
+    elif "--precompute" in sys.argv[1:]:
+        main_precompute()
     else:
         main()

@@ -156,3 +156,22 @@ def test_scaling_changes_only_same_population_terms(golden, scal):
         key = (int(it), int(term), int(t1), int(t2))
         if t1 != t2 and key in plain:
             assert v == plain[key]
+
+
+# --- the table precomputation (doPrecomputations.x) -------------------------------
+PRECOMPUTE_KEYS = ("g", "w", "dwdz", "P_lin", "conc", "hmf", "b_h")
+
+
+def test_precompute_oracle_matches_reference():
+    """oracle/precompute.c against the reference's own Cosmology / Powerspectrum / HMF
+    (tests/golden/ref_precompute.npz), bit for bit on x86."""
+    g = dict(np.load(os.path.join(os.path.dirname(GOLDEN_SCALING), "ref_precompute.npz")))
+    ci = 0
+    while f"c{ci}_in" in g:
+        zmin, zmax, mmin, mmax, kmin, kmax, N = g[f"c{ci}_in"]
+        got = P.precompute(g[f"c{ci}_cosmo"], g["nz_z"], g["nz_v"], zmin, zmax, mmin, mmax, kmin,
+                           kmax, int(N))
+        for k in PRECOMPUTE_KEYS:
+            assert_close(got[k], g[f"c{ci}_{k}"], rtol_other=1e-12)
+        ci += 1
+    assert ci == 2
