@@ -17,6 +17,7 @@
 // G3L_ERR_INVALID and set g3l_last_error().
 #include <cmath>
 #include <fstream>
+#include <new>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -30,6 +31,12 @@ int fail(const std::string &msg)
 {
     g3l::host::set_error(msg);
     return G3L_ERR_INVALID;
+}
+
+int fail_nomem(const char *what)
+{
+    g3l::host::set_error(std::string(what) + ": host allocation failed");
+    return G3L_ERR_NOMEM;
 }
 
 // value at x of the piecewise-linear 1-D table (src/Function.cpp:52-73)
@@ -85,9 +92,9 @@ int assign(const char *what, const char *path, const char *const *keys, int nkey
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-int g3l_read_function(const char *path, double default_value, int nbins, double min, double max,
+int g3l_read_function_impl(const char *path, double default_value, int nbins, double min, double max,
                       int log_bins, double *out)
 {
     if (!path || !out || nbins < 1 || (log_bins && !(min > 0 && max > 0)))
@@ -112,7 +119,7 @@ int g3l_read_function(const char *path, double default_value, int nbins, double 
     return G3L_OK;
 }
 
-int g3l_read_function2d(const char *path, double default_value, int nbins, double min1,
+int g3l_read_function2d_impl(const char *path, double default_value, int nbins, double min1,
                         double max1, double min2, double max2, double *out)
 {
     if (!path || !out || nbins < 1 || !(min2 > 0 && max2 > 0))
@@ -148,7 +155,7 @@ int g3l_read_function2d(const char *path, double default_value, int nbins, doubl
     return G3L_OK;
 }
 
-int g3l_read_hod_params(const char *path, double params[6])
+int g3l_read_hod_params_impl(const char *path, double params[6])
 {
     if (!path || !params) return fail("g3l_read_hod_params: invalid arguments");
     std::vector<std::string> names;
@@ -160,7 +167,7 @@ int g3l_read_hod_params(const char *path, double params[6])
     return assign("g3l_read_hod_params", path, keys, 6, names, vals, params);
 }
 
-int g3l_read_cosmology(const char *path, double cosmo[6])
+int g3l_read_cosmology_impl(const char *path, double cosmo[6])
 {
     if (!path || !cosmo) return fail("g3l_read_cosmology: invalid arguments");
     std::vector<std::string> names;
@@ -172,7 +179,7 @@ int g3l_read_cosmology(const char *path, double cosmo[6])
     return assign("g3l_read_cosmology", path, keys, 6, names, vals, cosmo);
 }
 
-int g3l_read_triplets(const char *path, double *thetas, int cap, int *n)
+int g3l_read_triplets_impl(const char *path, double *thetas, int cap, int *n)
 {
     if (!path || !n || cap < 0 || (cap > 0 && !thetas))
         return fail("g3l_read_triplets: invalid arguments");
@@ -190,6 +197,56 @@ int g3l_read_triplets(const char *path, double *thetas, int cap, int *n)
     }
     *n = k;
     return G3L_OK;
+}
+
+}  // namespace
+
+// the C ABI: no exception crosses it (a file too large for host memory reports NOMEM)
+extern "C" {
+
+int g3l_read_function(const char *path, double default_value, int nbins, double min, double max, int log_bins, double *out)
+{
+    try {
+        return g3l_read_function_impl(path, default_value, nbins, min, max, log_bins, out);
+    } catch (const std::bad_alloc &) {
+        return fail_nomem("g3l_read_function");
+    }
+}
+
+int g3l_read_function2d(const char *path, double default_value, int nbins, double min1, double max1, double min2, double max2, double *out)
+{
+    try {
+        return g3l_read_function2d_impl(path, default_value, nbins, min1, max1, min2, max2, out);
+    } catch (const std::bad_alloc &) {
+        return fail_nomem("g3l_read_function2d");
+    }
+}
+
+int g3l_read_hod_params(const char *path, double params[6])
+{
+    try {
+        return g3l_read_hod_params_impl(path, params);
+    } catch (const std::bad_alloc &) {
+        return fail_nomem("g3l_read_hod_params");
+    }
+}
+
+int g3l_read_cosmology(const char *path, double cosmo[6])
+{
+    try {
+        return g3l_read_cosmology_impl(path, cosmo);
+    } catch (const std::bad_alloc &) {
+        return fail_nomem("g3l_read_cosmology");
+    }
+}
+
+int g3l_read_triplets(const char *path, double *thetas, int cap, int *n)
+{
+    try {
+        return g3l_read_triplets_impl(path, thetas, cap, n);
+    } catch (const std::bad_alloc &) {
+        return fail_nomem("g3l_read_triplets");
+    }
 }
 
 }  // extern "C"

@@ -26,6 +26,7 @@
 
 #include <cfloat>
 #include <cmath>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -557,10 +558,29 @@ int run_tasks(const PkDev *dP, const std::vector<PcTask> &tasks, std::vector<PcO
 
 using namespace g3l;
 
+namespace {
+int precompute_impl(const g3l_precompute_in *in, int device, g3l_precompute_out *out);
+}
+
 extern "C" int g3l_precompute_tables(const g3l_precompute_in *in, int device,
                                      g3l_precompute_out *out)
 {
-    if (!in || !out || in->nbins < 1 || in->n_nz < 1 || !in->nz_z || !in->nz_v ||
+    try {
+        return precompute_impl(in, device, out);
+    } catch (const std::bad_alloc &) {
+        host::set_error("g3l_precompute_tables: host allocation failed");
+        return G3L_ERR_NOMEM;
+    } catch (...) {
+        host::set_error("g3l_precompute_tables: unexpected host error");
+        return G3L_ERR_INVALID;
+    }
+}
+
+namespace {
+int precompute_impl(const g3l_precompute_in *in, int device, g3l_precompute_out *out)
+{
+    if (!in || !out || in->nbins < 1 || in->nbins > 4096 || in->n_nz < 1 ||
+        in->n_nz > (1 << 22) || !in->nz_z || !in->nz_v ||
         !(in->mmin > 0 && in->mmax > in->mmin && in->kmin > 0 && in->kmax > in->kmin &&
           in->zmax > in->zmin && in->zmin >= 0) ||
         !out->g || !out->w || !out->dwdz || !out->P_lin || !out->conc || !out->hmf || !out->b_h) {
@@ -733,3 +753,4 @@ extern "C" int g3l_precompute_tables(const g3l_precompute_in *in, int device,
     out->points = (long long)ne;
     return G3L_OK;
 }
+}  // namespace

@@ -317,7 +317,7 @@ typedef struct g3l_precompute_in {
                                    from the reference's n(z) file */
     int n_nz;
     double zmin, zmax, mmin, mmax, kmin, kmax;
-    int nbins;
+    int nbins;                  /* 1..4096 */
 } g3l_precompute_in;
 typedef struct g3l_precompute_out {
     double *g, *w, *dwdz;              /* caller's arrays [nbins] */
