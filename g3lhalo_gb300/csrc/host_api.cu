@@ -8,6 +8,9 @@
 // at the end of the call.
 #include <cuda_runtime.h>
 
+#include <new>
+#include <stdexcept>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -1094,7 +1097,7 @@ int g3l_abi_version(void) { return G3L_ABI_VERSION; }
 int g3l_max_hod_slots(void) { return MAX_HOD_SLOTS; }
 
 int g3l_host_densities(const g3l_tables *t, const double hod[6], double *rho_bar, double *n_bar)
-{
+try {
     if (!t || !hod || !rho_bar || !n_bar || t->Nz < 2 || t->Nm < 2) {
         host::set_error("g3l_host_densities: invalid arguments");
         return G3L_ERR_INVALID;
@@ -1103,10 +1106,16 @@ int g3l_host_densities(const g3l_tables *t, const double hod[6], double *rho_bar
     host::rho_bar(B, t->Om, t->OL, t->H0, rho_bar);
     if (host::n_bar(B, t->hmf, hod, n_bar)) return G3L_ERR_INVALID;
     return G3L_OK;
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_host_densities: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_host_densities: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
-{
+try {
     if (!out) return G3L_ERR_INVALID;
     *out = nullptr;
     if (!t || t->Nz < 2 || t->Nm < 2 || t->Nk < 2 || !t->g || !t->p_lens1 || !t->p_lens2 || !t->w ||
@@ -1252,6 +1261,12 @@ int g3l_ctx_create(const g3l_tables *t, int device, g3l_ctx **out)
     if (st) return st;
     *out = c.release();
     return G3L_OK;
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_ctx_create: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_ctx_create: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 void g3l_ctx_destroy(g3l_ctx *c)
@@ -1282,7 +1297,7 @@ void g3l_ctx_destroy(g3l_ctx *c)
 }
 
 int g3l_set_hod(g3l_ctx *c, int slot, const double params[6])
-{
+try {
     if (!c || !params || slot < 0 || slot >= MAX_HOD_SLOTS) {
         host::set_error("g3l_set_hod: invalid arguments");
         return G3L_ERR_INVALID;
@@ -1326,6 +1341,12 @@ int g3l_set_hod(g3l_ctx *c, int slot, const double params[6])
                            c->stream));
     G3L_CK(cudaStreamSynchronize(c->stream));
     return G3L_OK;
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_set_hod: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_set_hod: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 int g3l_set_correlation(g3l_ctx *c, double A, double eps)
@@ -1346,7 +1367,7 @@ int g3l_set_correlation(g3l_ctx *c, double A, double eps)
 }
 
 int g3l_set_scaling(g3l_ctx *c, int slot, const double *scaling)
-{
+try {
     if (!c || slot < 0 || slot >= MAX_HOD_SLOTS) {
         host::set_error("g3l_set_scaling: invalid arguments");
         return G3L_ERR_INVALID;
@@ -1370,6 +1391,12 @@ int g3l_set_scaling(g3l_ctx *c, int slot, const double *scaling)
                            cudaMemcpyHostToDevice, c->stream));
     G3L_CK(cudaStreamSynchronize(c->stream));
     return G3L_OK;
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_set_scaling: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_set_scaling: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 int g3l_get_densities(g3l_ctx *c, int slot, double *rho, double *nbar)
@@ -1416,7 +1443,7 @@ int g3l_set_options(g3l_ctx *c, const g3l_options *o)
 
 int g3l_autotune(g3l_ctx *c, const g3l_integral *items, int n, int variant_out[6],
                  double *ms_out)
-{
+try {
     if (!c || !items || n < 1 || !variant_out) {
         host::set_error("g3l_autotune: invalid arguments");
         return G3L_ERR_INVALID;
@@ -1454,6 +1481,12 @@ int g3l_autotune(g3l_ctx *c, const g3l_integral *items, int n, int variant_out[6
     }
     const int st2 = g3l_set_options(c, &best);
     return st ? st : st2;
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_autotune: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_autotune: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 int g3l_get_stats(g3l_ctx *c, g3l_stats *s)
@@ -1464,7 +1497,7 @@ int g3l_get_stats(g3l_ctx *c, g3l_stats *s)
 }
 
 int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_result *out)
-{
+try {
     if (!c || n < 0 || (n > 0 && (!items || !out)) ||
         (precision != G3L_FP64 && precision != G3L_MIXED)) {
         host::set_error("g3l_eval: invalid arguments");
@@ -1632,11 +1665,17 @@ int g3l_eval(g3l_ctx *c, const g3l_integral *items, int n, int precision, g3l_re
     }
     if (first_bad) host::set_error("g3l_eval: an integral ended with status " + std::to_string(first_bad));
     return first_bad;
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_eval: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_eval: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 int g3l_debug_pool(g3l_ctx *c, int index, int max_regions, double *centers, int *levels,
                    double *val, double *err, int *split, float *unc, int *n_regions)
-{
+try {
     if (!c || !n_regions || index < 0 || index >= (int)c->last_pos.size() || max_regions < 0) {
         host::set_error("g3l_debug_pool: invalid arguments or no previous g3l_eval");
         return G3L_ERR_INVALID;
@@ -1674,11 +1713,17 @@ int g3l_debug_pool(g3l_ctx *c, int index, int max_regions, double *centers, int 
         G3L_CK(cudaMemcpy(unc + nR, W.P.uval + d.base, nR * sizeof(float), cudaMemcpyDeviceToHost));
     }
     return G3L_OK;
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_debug_pool: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_debug_pool: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 int g3l_debug_region(g3l_ctx *c, const g3l_integral *item, const double *center,
                      const int *levels, int precision, double *values, double out[3])
-{
+try {
     if (!c || !item || !center || !levels || !values || !out ||
         (precision != G3L_FP64 && precision != G3L_MIXED) || !item_ok(c, *item)) {
         host::set_error("g3l_debug_region: invalid arguments");
@@ -1758,6 +1803,12 @@ int g3l_debug_region(g3l_ctx *c, const g3l_integral *item, const double *center,
     if (rc) host::set_error(std::string("g3l_debug_region: ") + cudaGetErrorString(cudaGetLastError()));
     cudaFree(dbg);
     return rc;
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_debug_region: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_debug_region: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 int g3l_measure_peaks(g3l_ctx *c, double *fp32_tflops, double *fp64_tflops)
@@ -1769,7 +1820,7 @@ int g3l_measure_peaks(g3l_ctx *c, double *fp32_tflops, double *fp64_tflops)
 }
 
 int g3l_submit(g3l_ctx *c, const g3l_integral *items, int n, int precision, int64_t *ticket)
-{
+try {
     if (!c || !ticket || (precision != G3L_FP64 && precision != G3L_MIXED)) {
         host::set_error("g3l_submit: invalid arguments");
         return G3L_ERR_INVALID;
@@ -1781,14 +1832,26 @@ int g3l_submit(g3l_ctx *c, const g3l_integral *items, int n, int precision, int6
     st = srv_submit(v, items, n, &t);
     if (!st) *ticket = 2 * t + (precision == G3L_MIXED ? 1 : 0);
     return st;
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_submit: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_submit: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 int g3l_poll(g3l_ctx *c, int64_t ticket, g3l_result *out, int wait)
-{
+try {
     if (!c || ticket < 2) return G3L_ERR_INVALID;
     g3l_server *v = c->srv[ticket & 1];
     if (!v) return G3L_ERR_INVALID;
     return srv_poll(v, ticket >> 1, out, wait ? -1 : 0, nullptr);
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_poll: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_poll: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 int g3l_cancel(g3l_ctx *c, int64_t ticket)
@@ -1801,21 +1864,39 @@ int g3l_cancel(g3l_ctx *c, int64_t ticket)
 
 int g3l_server_create(g3l_ctx *ctx, int precision, int max_items_per_term, uint64_t pool_regions,
                       int rounds_per_launch, g3l_server **out)
-{
+try {
     return srv_create(ctx, precision, max_items_per_term, pool_regions, rounds_per_launch, out);
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_server_create: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_server_create: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 void g3l_server_destroy(g3l_server *srv) { srv_destroy(srv); }
 
 int g3l_server_submit(g3l_server *srv, const g3l_integral *items, int n, int64_t *ticket)
-{
+try {
     return srv_submit(srv, items, n, ticket);
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_server_submit: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_server_submit: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 int g3l_server_poll(g3l_server *srv, int64_t ticket, g3l_result *out, int wait_ms,
                     double *latency_ms)
-{
+try {
     return srv_poll(srv, ticket, out, wait_ms, latency_ms);
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_server_poll: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_server_poll: ") + e.what());
+    return G3L_ERR_INVALID;
 }
 
 int g3l_server_cancel(g3l_server *srv, int64_t ticket) { return srv_cancel(srv, ticket); }
@@ -1921,7 +2002,7 @@ int static_scratch(int device, unsigned char **base)
 
 extern "C" int g3l_eval_static(g3l_ctx *c, const g3l_integral *items, int n, int precision,
                                g3l_result *out)
-{
+try {
     if (!c || n < 0 || (n > 0 && (!items || !out)) ||
         (precision != G3L_FP64 && precision != G3L_MIXED)) {
         host::set_error("g3l_eval_static: invalid arguments");
@@ -2104,4 +2185,10 @@ extern "C" int g3l_eval_static(g3l_ctx *c, const g3l_integral *items, int n, int
     if (first_bad)
         host::set_error("g3l_eval_static: an integral ended with status " + std::to_string(first_bad));
     return first_bad;
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_eval_static: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_eval_static: ") + e.what());
+    return G3L_ERR_INVALID;
 }

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <system_error>
 
 #include "host_internal.h"
 
@@ -197,7 +198,14 @@ int n_bar(const Binning &B, const double *hmf, const double hod[6], double *out)
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
     const int nt = (int)std::min<unsigned>(hw, (unsigned)std::max(1, B.Nz / 2));
     std::vector<std::thread> pool;
-    for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+    pool.reserve(nt);
+    for (int t = 1; t < nt; ++t) {
+        try {
+            pool.emplace_back(work);
+        } catch (const std::system_error &) {
+            break;  // fewer threads: the work loop takes what is left
+        }
+    }
     work();
     for (auto &th : pool) th.join();
     return failed.load() ? 1 : 0;
