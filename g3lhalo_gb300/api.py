@@ -52,6 +52,17 @@ class Result(C.Structure):
                 ("neval", C.c_uint64), ("status", C.c_int32), ("rounds", C.c_int32)]
 
 
+# numpy views of the item and result structs (same fields, offsets and size), so that a
+# batch is converted with array operations instead of a Python loop per integral
+INTEGRAL_DT = np.dtype([("kind", "i4"), ("term", "i4"), ("hod1", "i4"), ("hod2", "i4"),
+                        ("theta", "f8", (3,)), ("rtol", "f8"), ("max_eval", "u8")])
+RESULT_DT = np.dtype([("val", "f8"), ("err", "f8"), ("result", "f8"), ("neval", "u8"),
+                      ("status", "i4"), ("rounds", "i4")])
+for _ct, _dt in ((Integral, INTEGRAL_DT), (Result, RESULT_DT)):
+    assert C.sizeof(_ct) == _dt.itemsize
+    assert all(getattr(_ct, f).offset == _dt.fields[f][1] for f in _dt.names)
+
+
 class ServerStats(C.Structure):
     _fields_ = [("launches", C.c_uint64), ("admitted", C.c_uint64), ("completed", C.c_uint64),
                 ("queued", C.c_int32), ("running_integrals", C.c_int32),
@@ -376,13 +387,15 @@ class Context:
     def make_items(specs):
         """specs: iterable of (kind, term, hod1, hod2, (th1, th2, th3), rtol, max_eval)."""
         specs = list(specs)
-        arr = (Integral * max(1, len(specs)))()
-        for i, (kind, term, h1, h2, th, rtol, me) in enumerate(specs):
-            arr[i].kind, arr[i].term, arr[i].hod1, arr[i].hod2 = kind, term, h1, h2
-            arr[i].theta[0], arr[i].theta[1], arr[i].theta[2] = th
-            arr[i].rtol = rtol
-            arr[i].max_eval = int(me)
-        return arr, len(specs)
+        n = len(specs)
+        a = np.zeros(max(1, n), dtype=INTEGRAL_DT)
+        if n:
+            kind, term, h1, h2, th, rtol, me = zip(*specs)
+            a["kind"][:n], a["term"][:n], a["hod1"][:n], a["hod2"][:n] = kind, term, h1, h2
+            a["theta"][:n] = np.asarray(th, dtype=np.float64).reshape(n, 3)
+            a["rtol"][:n] = rtol
+            a["max_eval"][:n] = [int(x) for x in me]
+        return (Integral * max(1, n)).from_buffer(a), n  # the ctypes array keeps `a` alive
 
     def eval(self, specs, precision=FP64, check=True):
         """Integrate every spec in one launch; returns a structured numpy array."""
@@ -395,13 +408,7 @@ class Context:
 
 
 def results_to_numpy(out, n):
-    dt = np.dtype([("val", "f8"), ("err", "f8"), ("result", "f8"), ("neval", "u8"),
-                   ("status", "i4"), ("rounds", "i4")])
-    r = np.zeros(n, dtype=dt)
-    for i in range(n):
-        o = out[i]
-        r[i] = (o.val, o.err, o.result, o.neval, o.status, o.rounds)
-    return r
+    return np.frombuffer(out, dtype=RESULT_DT, count=n).copy()
 
 
 class Server:
