@@ -415,7 +415,7 @@ def main():
            "gpu_launches": launches, "clocks": clk,
            "stats_last_step": {k: st_last[k] for k in ("rounds", "regions_evaluated",
                                                         "points_evaluated", "escalated",
-                                                        "deferred", "polished",
+                                                        "escalated_full", "deferred", "polished",
                                                         "tie_fallbacks", "small_arg_fp64",
                                                         "group_points")}}
     if rank == 0:
