@@ -18,6 +18,9 @@ Reported (one JSON line on rank 0):
               FMA rate of this device
   cpu_baseline the CPU oracle (restated reference CPU path, OpenMP over all host
               cores) on a bounded sample, extrapolated to one evaluation
+Further legs: serving (continuous batching at a sweep of Poisson arrival rates, and the
+same stream on an FP64 server), sweep (256 HOD vectors in one launch), nmapmap_twopop
+(NMapMap plus two-population NNMap), precompute (the table precomputation on 64 bins).
 --impl reference times the reference's CPU path alone (oracle/_ref where the
 reference compiled, else the oracle restatement) on the same workload.
 """
@@ -68,7 +71,7 @@ def parse():
     ap.add_argument("--no-config2", action="store_true")
     ap.add_argument("--no-precompute", action="store_true")
     # batched fit sweep: this many HOD vectors in one launch (0 = skip)
-    ap.add_argument("--sweep", type=int, default=16)
+    ap.add_argument("--sweep", type=int, default=256)
     return ap.parse_args()
 
 
@@ -298,24 +301,31 @@ def precompute_cpu(dev):
             "device_max_rel_vs_port": rel}
 
 
-def serving_leg(G, ctx, trip, hods, args, n_req=48, rate=12.0, seed=7):
-    """Continuous batching: a seeded Poisson stream of model evaluations (triplet
-    count log-uniform in 1..220, NNMap or NMapMap, one of 8 HOD vectors) submitted to
-    a server while earlier ones run; latency = submit to completion."""
-    rng = np.random.default_rng(seed)
-    for k in range(8):
-        ctx.set_hod(8 + k, hods[(40 + k) % len(hods)])
-    srv = G.Server(ctx, G.MIXED, max_items_per_term=2048, pool_regions=1 << 24,
-                   rounds_per_launch=4)
+SERVING_RATES = (10.0, 100.0, 1000.0, 2000.0)
+SERVING_RTOLS = (1e-3, 1e-4, 1e-5)
+
+
+def serving_requests(trip, n_req, max_eval, rng):
+    """Model evaluations from the config-4 distribution: triplet count log-uniform in
+    1..220, NNMap or NMapMap, rtol in {1e-3, 1e-4, 1e-5}, one of 8 HOD slots."""
     reqs = []
     for _ in range(n_req):
         nt = int(np.clip(np.round(np.exp(rng.uniform(0, np.log(220)))), 1, 220))
         idx = np.sort(rng.choice(len(trip), nt, replace=False))
         kind = int(rng.integers(0, 2))
         slot = 8 + int(rng.integers(0, 8))
-        reqs.append([(kind, t, slot, slot, tuple(trip[i]), RTOL, args.max_eval)
+        rtol = SERVING_RTOLS[int(rng.integers(0, len(SERVING_RTOLS)))]
+        reqs.append([(kind, t, slot, slot, tuple(trip[i]), rtol, max_eval)
                      for i in idx for t in (1, 2, 3)])
-    gaps = rng.exponential(1.0 / rate, n_req)
+    return reqs
+
+
+def serve_stream(G, ctx, precision, reqs, rate, rng):
+    """Submit `reqs` with seeded Poisson gaps while earlier ones run; latency = submit
+    to completion of each request."""
+    srv = G.Server(ctx, precision, max_items_per_term=2048, pool_regions=1 << 24,
+                   rounds_per_launch=4)
+    gaps = rng.exponential(1.0 / rate, len(reqs))
     tickets, lat = [], []
     t0 = time.perf_counter()
     for q, gap in zip(reqs, gaps):
@@ -327,16 +337,39 @@ def serving_leg(G, ctx, trip, hods, args, n_req=48, rate=12.0, seed=7):
     wall = time.perf_counter() - t0
     info = srv.info()
     srv.close()
-    pts_integrals = sum(len(q) for q in reqs)
-    return {"requests": n_req, "arrival_rate_per_s": rate, "integrals": pts_integrals,
+    n_int = sum(len(q) for q in reqs)
+    return {"arrival_rate_per_s": rate, "requests": len(reqs), "integrals": n_int,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(np.mean(lat)), "wall_s": wall,
-            "requests_per_s": n_req / wall,
-            "model_evals_per_s": pts_integrals / 660.0 / wall,
-            "launches": info["launches"],
-            "workload": "Poisson arrivals (seeded), triplets per request log-uniform 1..220, "
-                        "NNMap or NMapMap 1h+2h+3h, rtol 1e-4, maxEval %d, 8 HOD vectors; "
-                        "model_evals_per_s counts 660 integrals as one evaluation" % args.max_eval}
+            "requests_per_s": len(reqs) / wall,
+            "model_evals_per_s": n_int / 660.0 / wall, "launches": info["launches"]}
+
+
+def serving_leg(G, ctx, trip, hods, args, n_req=48, n_fp64=6, seed=7):
+    """Continuous batching at a sweep of Poisson arrival rates (config 4), and the same
+    stream's saturated throughput with an all-FP64 server for comparison."""
+    for k in range(8):
+        ctx.set_hod(8 + k, hods[(40 + k) % len(hods)])
+    rates = []
+    for i, rate in enumerate(SERVING_RATES):
+        rng = np.random.default_rng(seed + i)
+        rates.append(serve_stream(G, ctx, G.MIXED, serving_requests(trip, n_req, args.max_eval,
+                                                                    rng), rate, rng))
+    rng = np.random.default_rng(seed + 100)
+    reqs = serving_requests(trip, n_fp64, args.max_eval, rng)
+    mixed = serve_stream(G, ctx, G.MIXED, reqs, SERVING_RATES[-1], np.random.default_rng(1))
+    fp64 = serve_stream(G, ctx, G.FP64, reqs, SERVING_RATES[-1], np.random.default_rng(1))
+    low = rates[0]
+    return {"p50_ms": low["p50_ms"], "p99_ms": low["p99_ms"],
+            "arrival_rate_per_s": low["arrival_rate_per_s"], "rates": rates,
+            "saturated_same_stream": {"requests": n_fp64, "mixed": mixed, "fp64": fp64,
+                                      "mixed_over_fp64": mixed["model_evals_per_s"] /
+                                                         fp64["model_evals_per_s"]},
+            "workload": "seeded Poisson arrivals at %s req/s, %d requests each; triplets per "
+                        "request log-uniform 1..220, NNMap or NMapMap 1h+2h+3h, rtol in "
+                        "{1e-3, 1e-4, 1e-5}, maxEval %d, 8 HOD vectors from the fit-sweep box; "
+                        "model_evals_per_s counts 660 integrals as one evaluation"
+                        % ("/".join("%g" % r for r in SERVING_RATES), n_req, args.max_eval)}
 
 
 def main():
