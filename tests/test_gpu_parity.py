@@ -141,3 +141,19 @@ def test_converging_integral_stops_on_tolerance(ctx, golden):
     o = P.Oracle(ctx.tables, golden["hod1"], golden["hod2"], clamp_k=False)
     v, e, n, _ = o.term(0, 1, th, 1, 2, maxEval=10_000_000, rtol=0.5)
     assert int(r["neval"][0]) == n and _rel(r["val"][0], v) < FP64_RTOL
+
+
+def test_equal_scale_one_halo_at_full_budget(rect):
+    """The CPU-runnable case: the NNMap 1-halo term on the 5 equal-scale triplets
+    theta in {0.5, 1, 2, 4, 8} arcmin, rtol 1e-4, maxEval 1e6 (128 m x 64 z x 256 k
+    tables), FP64 and mixed against the oracle with identical evaluation counts."""
+    T, O, c = rect
+    ths = W.triplets_equal((0.5, 1.0, 2.0, 4.0, 8.0))
+    specs = [(G.NNMAP, 1, 0, 0, tuple(th), 1e-4, 1_000_000) for th in ths]  # one population
+    want = [O.term(0, 1, th, 1, 1, maxEval=1_000_000, rtol=1e-4) for th in ths]
+    for prec, tol in ((G.FP64, FP64_RTOL), (G.MIXED, TERM_RTOL)):
+        r = c.eval(specs, prec)
+        for k, (v, e, n, _) in enumerate(want):
+            assert r["status"][k] == 0
+            assert int(r["neval"][k]) == n, (prec, k, r["neval"][k], n)
+            assert _rel(r["val"][k], v) < tol, (prec, k, r["val"][k], v)
