@@ -53,6 +53,14 @@ RTOL = 1e-4
 FLOPS_PER_POINT = {"nnmap_2h": 1561.0}
 EXECUTED_FLOPS_PER_POINT = {"nnmap_2h": 909.0}
 DRAM_BYTES_PER_LAUNCH = {"nnmap_2h": 5.04e6}
+# Pipe utilisation (% of peak while the SMs are active) of the dominant kernels, from one
+# `ncu --set full` launch each of the profiled small case (the commands and the captures
+# are summarised in profiles/k_evalmx_nnmap2h.md and profiles/k_re_points_nnmap3h.md).
+PIPES_NCU = {
+    "k_evalmx<NNMap,2h> (FP32 rule)": {"fma": 16.5, "alu": 18.8, "xu_mufu": 4.0, "fp64": 2.6},
+    "k_re_points<NNMap,3h> (FP64 re-evaluation)": {"fp64": 67.3},
+    "k_pc_integrate (table precompute)": {"fp64": 79.2, "fma": 0.5, "xu_mufu": 0.1},
+}
 
 
 def parse():
@@ -497,7 +505,8 @@ def main():
                                                   (ms_g * 1e-3) / 1e12,
                                "peak_source": "measured FP32 FMA rate of this device "
                                               "(g3l_measure_peaks, CUDA events); the measured-peaks "
-                                              "file holds only HBM and bf16 figures", **kern}
+                                              "file holds only HBM and bf16 figures",
+                               "pipes_ncu_pct": PIPES_NCU, **kern}
         else:
             out["roofline"] = {"bound": "fp32", "achieved": None, "peak": p32, "unit": "TFLOP/s",
                                "frac": None, "traffic": None, **kern}
