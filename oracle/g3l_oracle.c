@@ -1,7 +1,7 @@
 /*
  * g3l_oracle.c -- CPU restatement of the G3LHalo hot path (TEST INFRASTRUCTURE).
  *
- * This file is the checker used by tests/, __graft_entry__.smoke() and the
+ * This file is the oracle used by tests/, __graft_entry__.smoke() and the
  * cpu_baseline leg of bench.py.  The product library never links it.
  *
  * Every function follows the reference's IEEE double expression order so

@@ -1,7 +1,7 @@
 /*
  * g3l_oracle.h -- CPU restatement of the G3LHalo aperture-statistics hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker: the parity tests, the smoke
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle: the parity tests, the smoke
  * check and the CPU-baseline leg of bench.py call it to produce the reference
  * answer.  The product library (libg3lgpu.so) never links, loads or calls it.
  *

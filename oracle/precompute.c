@@ -1,5 +1,5 @@
 /* precompute.c -- CPU restatement of the reference's table precomputation
- * (TEST INFRASTRUCTURE ONLY: the checker of the device precompute, never shipped).
+ * (TEST INFRASTRUCTURE ONLY: the oracle of the device precompute, never shipped).
  *
  * Follows doPrecomputations.x (src/doPrecomputations.cpp:40-134): the lensing
  * efficiency, comoving distance and its derivative on the z grid

@@ -4,7 +4,7 @@ Tolerances: the FP64 form evaluates the same IEEE operations as the reference,
 but this device's libm differs from glibc in the last ulp of a transcendental,
 so values agree to ~1e-12 and the adaptive trajectory (regions split, split
 dimensions, evaluation counts) is identical.  The bar required of every term
-is the spec relative tolerance 1e-4; FP64 is checked far tighter.
+is the relative tolerance 1e-4; FP64 is checked far tighter.
 """
 import numpy as np
 import pytest
@@ -17,7 +17,7 @@ from g3lhalo_gb300.tables import make_tables
 pytestmark = pytest.mark.gpu
 
 FP64_RTOL = 1e-9   # FP64 device form vs reference / oracle, per term
-TERM_RTOL = 1e-4   # contract for every term (the benchmark spec)
+TERM_RTOL = 1e-4   # required of every term
 
 
 @pytest.fixture(scope="module")
