@@ -41,7 +41,11 @@ def test_header_compiles_with_the_reference_classes(tmp_path):
     src = tmp_path / "with_ref.cu"
     src.write_text('#include "Cosmology.h"\n#include "HOD.h"\n#include "g3lhalo_model.hpp"\n'
                    "double f(g3lhalo::NNMap_Model &m) { return m.NNMap(1e-3, 1e-3, 1e-3, 1, 2); }\n"
-                   "double h(g3lhalo::NMapMap_Model &m) { return m.NMapMap(1e-3, 1e-3, 1e-3); }\n")
+                   "double h(g3lhalo::NMapMap_Model &m) { return m.NMapMap(1e-3, 1e-3, 1e-3); }\n"
+                   "g3lhalo::NNMap_Model *s(g3lhalo::Cosmology *c, double *t, g3lhalo::HOD *a,\n"
+                   "                        g3lhalo::HOD *b) {  // the SCALING constructor\n"
+                   "    return new g3lhalo::NNMap_Model(c, 0.1, 2., 0.1, 1e3, 1e10, 1e17, 8, t, t, t,\n"
+                   "                                    t, t, t, t, t, t, t, t, a, b, 0., 0.); }\n")
     r = subprocess.run(["nvcc", "-std=c++17", "-c", "-I" + REF_SRC,
                         "-I" + os.path.join(ROOT, "include"), str(src), "-o",
                         str(tmp_path / "with_ref.o")], capture_output=True, text=True)
