@@ -26,6 +26,7 @@
 
 #include <cfloat>
 #include <cmath>
+#include <cstdlib>
 #include <new>
 #include <string>
 #include <vector>
@@ -41,6 +42,10 @@ constexpr int PC_THREADS = 128;
 // twice the heap): a first pass with 512 (48 KB of shared memory, 4 blocks per SM)
 // integrates almost everything; integrals that need more run again with 2048.
 constexpr int PC_CAP_SMALL = 512, PC_CAP_LARGE = 2048;
+// G3L_PC_FIRST_CAP=64 makes the first pass hold only 64 regions, so that most
+// integrals take the 2048-region pass (its results are the same: an integral that
+// overflows starts again from its root region); used to test that pass.
+constexpr int PC_CAP_TINY = 64;
 constexpr int PC_MAX_ROUNDS = 4096;
 constexpr size_t pc_smem(int cap) { return sizeof(double) * 4 * (cap + 2 * cap); }
 
@@ -524,8 +529,13 @@ int run_tasks(const PkDev *dP, const std::vector<PcTask> &tasks, std::vector<PcO
     PC_CK(upload(dt, tasks, s));
     PC_CK(dres.alloc(tasks.size()));
     const int n = (int)tasks.size();
-    k_pc_integrate<PC_CAP_SMALL><<<std::min(n, nsm * 4), PC_THREADS, pc_smem(PC_CAP_SMALL), s>>>(
-        dP, dt.p, nullptr, n, dres.p);
+    const char *fc = std::getenv("G3L_PC_FIRST_CAP");
+    if (fc && std::atoi(fc) == PC_CAP_TINY)
+        k_pc_integrate<PC_CAP_TINY><<<std::min(n, nsm * 8), PC_THREADS, pc_smem(PC_CAP_TINY), s>>>(
+            dP, dt.p, nullptr, n, dres.p);
+    else
+        k_pc_integrate<PC_CAP_SMALL><<<std::min(n, nsm * 4), PC_THREADS, pc_smem(PC_CAP_SMALL),
+                                       s>>>(dP, dt.p, nullptr, n, dres.p);
     PC_CK(cudaGetLastError());
     res.resize(n);
     PC_CK(cudaMemcpyAsync(res.data(), dres.p, n * sizeof(PcOut), cudaMemcpyDeviceToHost, s));

@@ -83,3 +83,18 @@ def test_invalid_precompute_input_is_reported():
     with pytest.raises(G.G3LError):
         G.precompute_tables((np.nan, 0.7, 0.045, 0.8, 70.0, 0.96), z, z, 0.1, 2.0, 1e10, 1e17,
                             0.01, 1000.0, 8)
+
+
+def test_overflow_pass_gives_the_same_tables(gold, monkeypatch):
+    """Integrals that outgrow the first pass's region capacity run again with a larger
+    one from their root region; forcing most of them through that pass (a 64-region
+    first pass) changes no table entry."""
+    zmin, zmax, mmin, mmax, kmin, kmax, N = gold["c1_in"]
+    args = (gold["c1_cosmo"], gold["nz_z"], gold["nz_v"], zmin, zmax, mmin, mmax, kmin, kmax,
+            int(N))
+    a = G.precompute_tables(*args)
+    monkeypatch.setenv("G3L_PC_FIRST_CAP", "64")
+    b = G.precompute_tables(*args)
+    for k in KEYS:
+        assert np.array_equal(a[k], b[k]), k
+    assert a["points"] == b["points"]
