@@ -511,19 +511,37 @@ def main():
             out["roofline"] = {"bound": "fp32", "achieved": None, "peak": p32, "unit": "TFLOP/s",
                                "frac": None, "traffic": None, **kern}
         out["peaks_measured"] = {"fp32_tflops": p32, "fp64_tflops": p64}
+        # secondary legs: a failure is recorded in the line instead of losing it
+        def leg(key, fn):
+            try:
+                return fn()
+            except Exception as e:  # noqa: BLE001
+                out[key] = {"error": "%s: %s" % (type(e).__name__, e)}
+                return None
+
         if not args.no_serving:
-            out["serving"] = serving_leg(G, ctx, trip, hods, args)
+            r = leg("serving", lambda: serving_leg(G, ctx, trip, hods, args))
+            if r is not None:
+                out["serving"] = r
         if args.sweep:
-            out["sweep"] = sweep_leg(G, ctx, trip, hods, args.sweep, args.max_eval)
+            r = leg("sweep", lambda: sweep_leg(G, ctx, trip, hods, args.sweep, args.max_eval))
+            if r is not None:
+                out["sweep"] = r
         if not args.no_config2:
-            out["nmapmap_twopop"] = config2_leg(G, trip, args.max_eval)
+            r = leg("nmapmap_twopop", lambda: config2_leg(G, trip, args.max_eval))
+            if r is not None:
+                out["nmapmap_twopop"] = r
         pre = None
         if not args.no_precompute:
-            pre, out["precompute"] = precompute_leg(G)
+            r = leg("precompute", lambda: precompute_leg(G))
+            if r is not None:
+                pre, out["precompute"] = r
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_sample(T, trip, hods[last_hod], args.max_eval, 4)
             if pre is not None:
-                out["cpu_baseline"]["precompute"] = precompute_cpu(pre)
+                r = leg("cpu_precompute", lambda: precompute_cpu(pre))
+                if r is not None:
+                    out["cpu_baseline"]["precompute"] = r
         out["config"] = config(len(trip), args.max_eval)
         print(json.dumps(out), flush=True)
     if dist:
