@@ -123,3 +123,41 @@ def test_shim_scaling_constructor_reproduces_the_scaling_build(tmp_path, golden,
     for t, want in scal["sc_stock"]:
         got = out["S_NNMap_%dh" % int(t)][0]
         assert abs(got - want) <= rtol * abs(want), (t, got, want)
+
+
+# A prelude forced into the reference's own driver sources: it defines the include
+# guards of the reference's NNMap_Model.h / NMapMap_Model.h, so the drivers' first
+# #include becomes a no-op, and brings in the shim after Cosmology.h and HOD.h.
+PRELUDE = ('#define G3LHALO_NNMAP_MODEL_H\n#define G3LHALO_NMAPMAP_MODEL_H\n'
+           '#include "Cosmology.h"\n#include "HOD.h"\n#include "g3lhalo_model.hpp"\n')
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not mounted")
+@pytest.mark.parametrize("driver,defs", [("calculateNNMap", []), ("calculateNMapMap", []),
+                                         ("calculateNNMap_twoPop", []),
+                                         ("calculateNNMap_twoPop", ["-DSCALING=1"])])
+def test_reference_drivers_link_against_the_library(tmp_path, driver, defs):
+    """The reference's executables, compiled unmodified from their sources with the shim
+    in place of its model classes, link against libg3lgpu.so (src/calculateNNMap.cu,
+    src/calculateNNMap_twoPop.cu with and without SCALING, src/calculateNMapMap.cu)."""
+    import pyoracle as P
+    P.build_ref()  # the reference's own Cosmology, HOD, Params, Function objects
+    obj = os.path.join(ROOT, "oracle", "_ref", "obj")
+    lib = G.library_path()
+    (tmp_path / "prelude.h").write_text(PRELUDE)
+    run = lambda cmd: subprocess.run(cmd, capture_output=True, text=True)  # noqa: E731
+    r = run(["g++", "-std=c++17", "-O1", "-fopenmp", "-fPIC", "-I" + REF_SRC, "-c",
+             os.path.join(REF_SRC, "helpers.cpp"), "-o", str(tmp_path / "helpers.o")])
+    assert r.returncode == 0, r.stderr
+    r = run(["nvcc", "-std=c++17", "-O1", "-rdc=true", "-Xcompiler", "-fopenmp"] + defs +
+            ["-include", str(tmp_path / "prelude.h"), "-I" + os.path.join(ROOT, "include"),
+             "-I" + REF_SRC, "-c", os.path.join(REF_SRC, driver + ".cu"), "-o",
+             str(tmp_path / "driver.o")])
+    assert r.returncode == 0, r.stderr
+    objs = [os.path.join(obj, f + ".o") for f in ("Cosmology", "Params", "Function",
+                                                  "Function2D", "hcubature", "HOD",
+                                                  "generalFunctions")]
+    r = run(["nvcc", "-rdc=true", "-Xcompiler", "-fopenmp", str(tmp_path / "driver.o"),
+             str(tmp_path / "helpers.o")] + objs + ["-L" + os.path.dirname(lib), "-lg3lgpu",
+                                                    "-o", str(tmp_path / (driver + ".x"))])
+    assert r.returncode == 0, r.stderr
