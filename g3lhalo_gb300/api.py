@@ -159,6 +159,9 @@ def lib():
             L.g3l_host_densities.argtypes = [C.POINTER(Tables), _dp, _dp, _dp]
             L.g3l_hcubature_v.argtypes = [C.c_uint, C.c_void_p, C.c_void_p, C.c_uint, _dp, _dp,
                                           C.c_size_t, C.c_double, C.c_double, C.c_int, _dp, _dp]
+            L.g3l_eval_terms.argtypes = [C.c_void_p, C.c_int, _dp, C.c_int, C.c_int, C.c_int,
+                                         C.c_int, C.c_double, C.c_uint64, C.c_int, _dp, _dp, _dp,
+                                         C.POINTER(C.c_uint64)]
             L.g3l_precompute_tables.argtypes = [C.POINTER(PrecomputeIn), C.c_int,
                                                 C.POINTER(PrecomputeOut)]
             L.g3l_read_function.argtypes = [C.c_char_p, C.c_double, C.c_int, C.c_double,
@@ -396,6 +399,20 @@ class Context:
             a["rtol"][:n] = rtol
             a["max_eval"][:n] = [int(x) for x in me]
         return (Integral * max(1, n)).from_buffer(a), n  # the ctypes array keeps `a` alive
+
+    def eval_terms(self, kind, triplets, hod1, hod2, term_mask=7, rtol=1e-4,
+                   max_eval=1_000_000, precision=MIXED):
+        """g3l_eval_terms: (val, err, result) [n, 3] and the total evaluation count."""
+        th = np.ascontiguousarray(triplets, dtype=np.float64).reshape(-1, 3)
+        n = th.shape[0]
+        val, err, res = (np.zeros((max(n, 1), 3)) for _ in range(3))
+        ne = C.c_uint64()
+        st = lib().g3l_eval_terms(self.h, kind, _ptr(th), n, hod1, hod2, term_mask, rtol,
+                                  int(max_eval), precision, _ptr(val), _ptr(err), _ptr(res),
+                                  C.byref(ne))
+        if st not in (0, 4, 5, 7):
+            _check(st)
+        return val[:n], err[:n], res[:n], ne.value
 
     def eval(self, specs, precision=FP64, check=True):
         """Integrate every spec in one launch; returns a structured numpy array."""

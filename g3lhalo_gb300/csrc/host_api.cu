@@ -1489,6 +1489,51 @@ try {
     return G3L_ERR_INVALID;
 }
 
+int g3l_eval_terms(g3l_ctx *c, int kind, const double *triplets, int n, int hod1, int hod2,
+                   int term_mask, double rtol, uint64_t max_eval, int precision, double *val,
+                   double *err, double *result, uint64_t *neval)
+try {
+    if (!c || n < 0 || (n > 0 && (!triplets || !val || !err || !result)) || term_mask < 0 ||
+        term_mask > 7) {
+        host::set_error("g3l_eval_terms: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    std::vector<g3l_integral> items;
+    std::vector<int> where;
+    for (int i = 0; i < n; ++i)
+        for (int t = 1; t <= 3; ++t) {
+            val[3 * i + t - 1] = err[3 * i + t - 1] = result[3 * i + t - 1] = 0;
+            if (!(term_mask >> (t - 1) & 1)) continue;
+            g3l_integral it{};
+            it.kind = kind;
+            it.term = t;
+            it.hod1 = hod1;
+            it.hod2 = hod2;
+            for (int k = 0; k < 3; ++k) it.theta[k] = triplets[3 * i + k];
+            it.rtol = rtol;
+            it.max_eval = max_eval;
+            items.push_back(it);
+            where.push_back(3 * i + t - 1);
+        }
+    if (neval) *neval = 0;
+    if (items.empty()) return G3L_OK;
+    std::vector<g3l_result> out(items.size());
+    const int st = g3l_eval(c, items.data(), (int)items.size(), precision, out.data());
+    if (st == G3L_ERR_INVALID || st == G3L_ERR_CUDA || st == G3L_ERR_NOMEM) return st;
+    uint64_t ne = 0;
+    for (size_t k = 0; k < items.size(); ++k) {
+        val[where[k]] = out[k].val;
+        err[where[k]] = out[k].err;
+        result[where[k]] = out[k].result;
+        ne += out[k].neval;
+    }
+    if (neval) *neval = ne;
+    return st;
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_eval_terms: host allocation failed");
+    return G3L_ERR_NOMEM;
+}
+
 int g3l_get_stats(g3l_ctx *c, g3l_stats *s)
 {
     if (!c || !s) return G3L_ERR_INVALID;

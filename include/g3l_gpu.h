@@ -123,6 +123,14 @@ int g3l_get_densities(g3l_ctx *ctx, int slot, double *rho_bar, double *n_bar);
  * (src/NNMap_Model.cu:382-415).  Returns the first non-OK item status, or OK. */
 int g3l_eval(g3l_ctx *ctx, const g3l_integral *items, int n, int precision,
              g3l_result *out);
+/* g3l_eval in the per-term methods' shape: the terms in term_mask (bit t-1 = term t) of
+ * one kind for n aperture triplets (triplets[3*i + k], radians) and one HOD slot pair,
+ * all in one launch.  val, err and result: [n*3], entry 3*i + t-1, before and after the
+ * prefactor (terms outside the mask are set to 0); neval: the evaluations of all of
+ * them (may be NULL).  Returns the first non-OK status, like g3l_eval. */
+int g3l_eval_terms(g3l_ctx *ctx, int kind, const double *triplets, int n, int hod1, int hod2,
+                   int term_mask, double rtol, uint64_t max_eval, int precision, double *val,
+                   double *err, double *result, uint64_t *neval);
 
 /* Serving with continuous batching.  A server owns a table of integral slots
  * (max_items_per_term for each kind x term) and a pool of pool_regions region slots

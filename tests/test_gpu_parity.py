@@ -157,3 +157,23 @@ def test_equal_scale_one_halo_at_full_budget(rect):
             assert r["status"][k] == 0
             assert int(r["neval"][k]) == n, (prec, k, r["neval"][k], n)
             assert _rel(r["val"][k], v) < tol, (prec, k, r["val"][k], v)
+
+
+def test_eval_terms_is_eval_in_the_per_term_shape(ctx, golden):
+    th = golden["thetas"][:3]
+    for kind, h1, h2, mask in ((G.NNMAP, 0, 1, 7), (G.NNMAP, 0, 0, 5), (G.NMAPMAP, 2, 2, 2)):
+        val, err, res, ne = ctx.eval_terms(kind, th, h1, h2, term_mask=mask, max_eval=20_000,
+                                           precision=G.FP64)
+        terms = [t for t in (1, 2, 3) if mask >> (t - 1) & 1]
+        r = ctx.eval([(kind, t, h1, h2, tuple(x), 1e-4, 20_000) for x in th for t in terms],
+                     G.FP64)
+        k = 0
+        for i in range(len(th)):
+            for t in (1, 2, 3):
+                if t in terms:
+                    assert (val[i, t - 1], err[i, t - 1], res[i, t - 1]) == (
+                        r["val"][k], r["err"][k], r["result"][k])
+                    k += 1
+                else:
+                    assert val[i, t - 1] == 0 and res[i, t - 1] == 0
+        assert ne == int(r["neval"].sum())
