@@ -53,3 +53,21 @@ def test_invalid_arguments_are_reported_not_fatal(golden_tables):
     with pytest.raises(G.G3LError) as ei:
         G.Context(t)
     assert ei.value.status in (1, 8)  # INVALID on a GPU host, NO_DEVICE without one
+
+
+def test_header_is_c_and_a_c_program_links(tmp_path):
+    """include/g3l_gpu.h is plain C (C11, pedantic) and a C program links the library."""
+    import subprocess
+    src = tmp_path / "use.c"
+    src.write_text('#include "g3l_gpu.h"\n'
+                   'int main(void) {\n'
+                   '    g3l_tables t = {0}; g3l_integral it = {0}; g3l_result r = {0};\n'
+                   '    (void)t; (void)it; (void)r;\n'
+                   '    return g3l_abi_version() == G3L_ABI_VERSION ? 0 : 1;\n'
+                   '}\n')
+    lib = G.library_path()
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                        "-I" + os.path.join(ROOT, "include"), str(src), "-o",
+                        str(tmp_path / "use"), "-L" + os.path.dirname(lib), "-lg3lgpu",
+                        "-Wl,-rpath," + os.path.dirname(lib)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
