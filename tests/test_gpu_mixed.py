@@ -168,3 +168,23 @@ def test_autotune_picks_a_variant_per_term_and_keeps_parity(rect):
     b = c.eval(specs, G.MIXED)
     assert np.array_equal(a["neval"], b["neval"])
     assert _rel(b["val"], a["val"]).max() < TERM_RTOL
+
+
+@pytest.mark.parametrize("rtol", [1e-2, 1e-3, 1e-5])
+def test_mixed_matches_fp64_at_other_tolerances(rect, rtol):
+    """The serving stream's tolerances: every term within 1e-4 of the FP64 form and the
+    same evaluation counts, both kinds (rtol sets how many regions each round pops, so
+    each tolerance is its own trajectory)."""
+    T, _ = rect
+    c = G.Context(T, clamp_k=True)
+    hods = W.hod_sweep(16, seed=99)
+    c.set_hod(0, hods[0])
+    c.set_hod(1, hods[1])
+    trip = W.triplets_all()
+    for kind in (G.NNMAP, G.NMAPMAP):
+        specs = [(kind, t, 0, 1 if kind == G.NNMAP else 0, tuple(trip[i]), rtol, 300_000)
+                 for i in range(0, 220, 22) for t in (1, 2, 3)]
+        a = c.eval(specs, G.FP64)
+        b = c.eval(specs, G.MIXED)
+        assert np.array_equal(a["neval"], b["neval"])
+        assert _rel(b["val"], a["val"]).max() < TERM_RTOL
