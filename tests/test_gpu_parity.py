@@ -177,3 +177,23 @@ def test_eval_terms_is_eval_in_the_per_term_shape(ctx, golden):
                 else:
                     assert val[i, t - 1] == 0 and res[i, t - 1] == 0
         assert ne == int(r["neval"].sum())
+
+
+def test_irregular_grid_shapes_match_the_oracle():
+    """33 z x 257 m x 90 k bins (Nm - 1 a power of two: the mass-centre ties fall at
+    every depth): FP64 against the oracle, mixed against FP64, identical counts."""
+    T = make_tables(Nz=33, Nm=257, Nk=90)
+    h1, h2 = W.hod_default(), W.hod_second()
+    c = G.Context(T, clamp_k=True)
+    c.set_hod(0, h1)
+    c.set_hod(1, h2)
+    O = P.Oracle(T, h1, h2, clamp_k=True)
+    trip = W.triplets_all()
+    specs = [(G.NNMAP, t, 0, 1, tuple(trip[i]), 1e-4, 40_000) for i in (3, 77, 150, 219)
+             for t in (1, 2, 3)]
+    a = c.eval(specs, G.FP64)
+    b = c.eval(specs, G.MIXED)
+    for k, (kind, t, _, _, th, rt, me) in enumerate(specs):
+        v, e, n, _ = O.term(0, t, th, 1, 2, maxEval=me, rtol=rt)
+        assert int(a["neval"][k]) == n and _rel(a["val"][k], v) < FP64_RTOL, (k, a["val"][k], v)
+        assert int(b["neval"][k]) == n and _rel(b["val"][k], v) < TERM_RTOL, (k, b["val"][k], v)
