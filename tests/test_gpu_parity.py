@@ -180,8 +180,9 @@ def test_eval_terms_is_eval_in_the_per_term_shape(ctx, golden):
 
 
 def test_irregular_grid_shapes_match_the_oracle():
-    """33 z x 257 m x 90 k bins (Nm - 1 a power of two: the mass-centre ties fall at
-    every depth): FP64 against the oracle, mixed against FP64, identical counts."""
+    """33 z x 257 m x 90 k bins (Nm - 1 = 2^8: region centres hit exact mass-bin ties at
+    bisection depths 0 to 8): FP64 against the oracle, mixed against FP64, identical
+    counts."""
     T = make_tables(Nz=33, Nm=257, Nk=90)
     h1, h2 = W.hod_default(), W.hod_second()
     c = G.Context(T, clamp_k=True)
