@@ -1036,7 +1036,10 @@ int srv_submit(g3l_server *v, const g3l_integral *items, int n, int64_t *ticket)
 
 int srv_poll(g3l_server *v, int64_t ticket, g3l_result *out, int wait_ms, double *latency_ms)
 {
-    if (!v) return G3L_ERR_INVALID;
+    if (!v) {
+        host::set_error("g3l_server_poll: no server");
+        return G3L_ERR_INVALID;
+    }
     std::unique_lock<std::mutex> lk(v->mu);
     auto it = v->reqs.find(ticket);
     if (it == v->reqs.end()) {
@@ -1063,10 +1066,17 @@ int srv_poll(g3l_server *v, int64_t ticket, g3l_result *out, int wait_ms, double
 
 int srv_cancel(g3l_server *v, int64_t ticket)
 {
-    if (!v) return G3L_ERR_INVALID;
+    if (!v) {
+        host::set_error("g3l_server_cancel: no server");
+        return G3L_ERR_INVALID;
+    }
     std::lock_guard<std::mutex> lk(v->mu);
     auto it = v->reqs.find(ticket);
-    if (it == v->reqs.end() || it->second.done) return G3L_ERR_INVALID;
+    if (it == v->reqs.end()) {
+        host::set_error("g3l_server_cancel: unknown or already polled ticket");
+        return G3L_ERR_INVALID;
+    }
+    if (it->second.done) return G3L_OK;  // finished before the cancel: its results stand
     SrvReq &q = it->second;
     q.cancel = true;
     if (!q.admitted) {  // still queued: finish it now

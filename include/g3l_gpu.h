@@ -169,7 +169,9 @@ int g3l_server_submit(g3l_server *srv, const g3l_integral *items, int n, int64_t
 int g3l_server_poll(g3l_server *srv, int64_t ticket, g3l_result *out, int wait_ms,
                     double *latency_ms);
 /* A queued request finishes at once; a running one at the next launch boundary.  Its
- * integrals report G3L_ERR_CANCELLED unless they had already finished. */
+ * integrals report G3L_ERR_CANCELLED unless they had already finished.  A request that
+ * has finished but not been polled is left as it is (G3L_OK); a ticket that is unknown
+ * or already polled is G3L_ERR_INVALID. */
 int g3l_server_cancel(g3l_server *srv, int64_t ticket);
 int g3l_server_info(g3l_server *srv, g3l_server_stats *st);
 

@@ -144,3 +144,80 @@ def test_context_submit_and_poll(ctx):
     out = (A.Result * n)()
     assert A.lib().g3l_poll(ctx.h, t.value, out, 1) == 0
     assert _same(A.results_to_numpy(out, n), ref)
+
+
+def test_randomized_stream_with_cancellations(ctx):
+    """48 random requests (kind, terms, slot pair, rtol and budget drawn per request)
+    from two threads, every fifth cancelled in flight: every integral that finished --
+    including those of cancelled requests -- equals g3l_eval bit for bit, the rest report
+    G3L_ERR_CANCELLED, and the server ends idle."""
+    rng = np.random.default_rng(2026)
+    trip = W.triplets_all()
+    reqs = []
+    for _ in range(48):
+        idx = rng.choice(220, int(rng.integers(1, 10)), replace=False)
+        kind = int(rng.integers(0, 2))
+        s1 = int(rng.integers(0, 6))
+        s2 = s1 if kind == G.NMAPMAP or rng.random() < 0.5 else int(rng.integers(0, 6))
+        rtol = (1e-3, 1e-4, 1e-5)[int(rng.integers(0, 3))]
+        me = int(rng.choice([5_000, 50_000, 200_000]))
+        terms = [t for t in (1, 2, 3) if rng.random() < 0.7] or [2]
+        reqs.append([(kind, t, s1, s2, tuple(trip[i]), rtol, me) for i in idx for t in terms])
+    srv = G.Server(ctx, G.MIXED, max_items_per_term=256, pool_regions=1 << 21,
+                   rounds_per_launch=3)
+    try:
+        tickets, lock = {}, threading.Lock()
+
+        def submit(lo, hi, seed):
+            g = np.random.default_rng(seed)
+            for i in range(lo, hi):
+                t = srv.submit(reqs[i])
+                with lock:
+                    tickets[i] = t
+                time.sleep(float(g.exponential(0.003)))
+
+        th = [threading.Thread(target=submit, args=(0, 24, 1)),
+              threading.Thread(target=submit, args=(24, 48, 2))]
+        for x in th:
+            x.start()
+        time.sleep(0.03)
+        cancelled = set()
+        for i in range(0, 48, 5):
+            with lock:
+                t = tickets.get(i)
+            if t is not None:
+                srv.cancel(t)
+                cancelled.add(i)
+        for x in th:
+            x.join()
+        for i in range(48):
+            r, _ = srv.poll(tickets[i], check=False)
+            ok = r["status"] == 0
+            if i in cancelled:
+                assert np.all(ok | (r["status"] == 6))
+            else:
+                assert np.all(ok)
+            ref = ctx.eval(reqs[i], G.MIXED)
+            assert np.array_equal(r["val"][ok], ref["val"][ok])
+            assert np.array_equal(r["neval"][ok], ref["neval"][ok])
+        assert srv.info()["running_integrals"] == 0
+    finally:
+        srv.close()
+
+
+def test_cancel_after_completion_keeps_the_results(ctx):
+    srv = G.Server(ctx, G.MIXED, max_items_per_term=64, pool_regions=1 << 20)
+    try:
+        A = _request([5], slot=0, max_eval=5_000)
+        t = srv.submit(A)
+        for _ in range(400):  # bounded wait for completion
+            if srv.info()["completed"] >= 1:
+                break
+            time.sleep(0.005)
+        srv.cancel(t)          # finished, not yet polled: a no-op
+        got, _ = srv.poll(t)
+        assert np.all(got["status"] == 0) and _same(got, ctx.eval(A, G.MIXED))
+        with pytest.raises(G.G3LError):
+            srv.cancel(t)      # already polled
+    finally:
+        srv.close()
