@@ -198,3 +198,34 @@ def test_irregular_grid_shapes_match_the_oracle():
         v, e, n, _ = O.term(0, t, th, 1, 2, maxEval=me, rtol=rt)
         assert int(a["neval"][k]) == n and _rel(a["val"][k], v) < FP64_RTOL, (k, a["val"][k], v)
         assert int(b["neval"][k]) == n and _rel(b["val"][k], v) < TERM_RTOL, (k, b["val"][k], v)
+
+
+def test_two_contexts_in_two_threads():
+    """Distinct contexts are independent: two contexts (different tables and HODs)
+    evaluated at the same time from two host threads give their sequential results."""
+    import threading
+    trip = W.triplets_all()
+    ctxs, specs, want = [], [], []
+    for k, (Nz, Nm, Nk) in enumerate(((64, 128, 256), (48, 96, 160))):
+        c = G.Context(make_tables(Nz=Nz, Nm=Nm, Nk=Nk), clamp_k=True)
+        hods = W.hod_sweep(4, seed=31 + k)
+        c.set_hod(0, hods[0])
+        c.set_hod(1, hods[1])
+        s = [(kind, t, 0, 1 if kind == G.NNMAP else 0, tuple(trip[i]), 1e-4, 50_000)
+             for kind in (G.NNMAP, G.NMAPMAP) for i in range(k, 220, 37) for t in (1, 2, 3)]
+        ctxs.append(c)
+        specs.append(s)
+        want.append((c.eval(s, G.MIXED), c.eval(s, G.FP64)))
+    got = [None, None]
+
+    def run(k):
+        got[k] = (ctxs[k].eval(specs[k], G.MIXED), ctxs[k].eval(specs[k], G.FP64))
+
+    th = [threading.Thread(target=run, args=(k,)) for k in range(2)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    for k in range(2):
+        for a, b in zip(got[k], want[k]):
+            assert np.array_equal(a["val"], b["val"]) and np.array_equal(a["neval"], b["neval"])
