@@ -138,3 +138,15 @@ def test_set_scaling_rejects_invalid_input(sctx, golden_tables):
         sctx.set_scaling(G.lib().g3l_max_hod_slots(), None)
     with pytest.raises(ValueError):
         sctx.set_scaling(2, np.ones(golden_tables.Nm + 1))
+
+
+def test_python_model_scaling_constructor(golden, golden_tables, scal):
+    """api.NNMapModel(scaling=...) puts scaling1 on both slots, as the reference's SCALING
+    build reads it, and reproduces that build's stock NNMap_1h / NNMap_2h (type 1, 1)."""
+    from g3lhalo_gb300 import api as A
+    m = A.NNMapModel(golden_tables, golden["hod1"], golden["hod2"], precision=G.FP64,
+                     clamp_k=False, scaling=(scal["scaling1"], scal["scaling2"]))
+    th = golden["thetas"][1]
+    for term, want in scal["sc_stock"]:
+        got = m.term(int(term), *th, type1=1, type2=1)
+        assert _rel(got, want) < 1e-6, (term, got, want)
