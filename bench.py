@@ -53,11 +53,15 @@ RTOL = 1e-4
 FLOPS_PER_POINT = {"nnmap_2h": 1561.0}
 EXECUTED_FLOPS_PER_POINT = {"nnmap_2h": 909.0}
 DRAM_BYTES_PER_LAUNCH = {"nnmap_2h": 5.04e6}
-# Pipe utilisation (% of peak while the SMs are active) of the dominant kernels, from one
-# `ncu --set full` launch each of the profiled small case (the commands and the captures
-# are summarised in profiles/k_evalmx_nnmap2h.md and profiles/k_re_points_nnmap3h.md).
+# Pipe utilisation (% of peak while the SMs are active) of the dominant kernels.  The
+# FP32 rule kernel: fma, alu, issue and warps active time-weighted over all launches of
+# the full workload (one-pass captures), xu and fp64 from one `ncu --set full` launch of
+# the small case; the others from one `--set full` launch each (the commands and the
+# captures are summarised in profiles/k_evalmx_nnmap2h.md, profiles/k_re_points_nnmap3h.md
+# and profiles/k_pc_integrate_precompute.md).
 PIPES_NCU = {
-    "k_evalmx<NNMap,2h> (FP32 rule)": {"fma": 16.5, "alu": 18.8, "xu_mufu": 4.0, "fp64": 2.6},
+    "k_evalmx<NNMap,2h> (FP32 rule)": {"fma": 25.6, "alu": 22.8, "xu_mufu": 4.0, "fp64": 2.6,
+                                       "issue_active": 45.4, "warps_active": 47.0},
     "k_re_points<NNMap,3h> (FP64 re-evaluation)": {"fp64": 67.3},
     "k_pc_integrate (table precompute)": {"fp64": 79.2, "fma": 0.5, "xu_mufu": 0.1},
 }
