@@ -54,3 +54,4 @@ def test_invalid_items_are_rejected_before_any_work(ctx):
         with pytest.raises(G.G3LError) as e:
             ctx.eval([bad], G.MIXED)
         assert e.value.status == 1
+

@@ -71,3 +71,18 @@ def test_header_is_c_and_a_c_program_links(tmp_path):
                         str(tmp_path / "use"), "-L" + os.path.dirname(lib), "-lg3lgpu",
                         "-Wl,-rpath," + os.path.dirname(lib)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("table", ["g", "p_lens1", "w", "dwdz", "hmf", "b_h", "conc", "P_lin"])
+def test_nonfinite_tables_are_rejected_at_creation(table):
+    """A NaN or infinity in any table is refused before any device work (the reference
+    would carry it into every result); no GPU is needed to see it."""
+    from g3lhalo_gb300.tables import make_tables
+    for bad in (np.nan, np.inf):
+        T = make_tables(Nz=8, Nm=8, Nk=8)
+        a = np.array(getattr(T, table), dtype=np.float64)
+        a.flat[a.size // 2] = bad
+        setattr(T, table, a)
+        with pytest.raises(G.G3LError) as e:
+            G.Context(T)
+        assert e.value.status == 1
