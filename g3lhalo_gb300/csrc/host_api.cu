@@ -1994,10 +1994,16 @@ static __device__ __align__(256) unsigned char g3l_static_scratch[kStaticScratch
 std::mutex g_static_mu;
 void *g_static_base[kStaticMaxDevices];  // device address of the scratch, per device
 
-// Host staging for one call (static: the entry point is not reentrant).
-IntDesc g_st_desc[kStaticMaxItems];
-IntState g_st_state[kStaticMaxItems];
-int g_st_order[kStaticMaxItems];
+// Host staging of one call, one set per device beside that device's scratch (static
+// storage: the entry point allocates nothing).  The per-device lock serialises calls on
+// one device, which share both; calls on different devices proceed side by side.
+struct StaticStage {
+    std::mutex mu;
+    IntDesc desc[kStaticMaxItems];
+    IntState state[kStaticMaxItems];
+    int order[kStaticMaxItems];
+};
+StaticStage g_st[kStaticMaxDevices];
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -2053,27 +2059,10 @@ int static_scratch(int device, unsigned char **base)
     return G3L_OK;
 }
 
-}  // namespace
-
-extern "C" int g3l_eval_static(g3l_ctx *c, const g3l_integral *items, int n, int precision,
-                               g3l_result *out)
-try {
-    if (!c || n < 0 || (n > 0 && (!items || !out)) ||
-        (precision != G3L_FP64 && precision != G3L_MIXED)) {
-        host::set_error("g3l_eval_static: invalid arguments");
-        return G3L_ERR_INVALID;
-    }
-    if (n == 0) return G3L_OK;
-    if (n > kStaticMaxItems) {
-        host::set_error("g3l_eval_static: " + std::to_string(n) + " integrals exceed the limit of " +
-                        std::to_string(kStaticMaxItems) + " per call");
-        return G3L_ERR_INVALID;
-    }
-    for (int i = 0; i < n; ++i)
-        if (!item_ok(c, items[i])) {
-            host::set_error("g3l_eval_static: invalid integral " + std::to_string(i));
-            return G3L_ERR_INVALID;
-        }
+// One call on the device of `c`, with that device's staging `G` held by the caller.
+int eval_static_locked(g3l_ctx *c, const g3l_integral *items, int n, int precision,
+                       g3l_result *out, StaticStage &G, unsigned char *base)
+{
     // descriptors in group order (stable counting sort, no temporary buffer), pool
     // capacities as g3l_eval
     auto grp = [&](int i) { return items[i].kind * 3 + items[i].term - 1; };
@@ -2081,15 +2070,15 @@ try {
         int cnt[NGROUPS + 1] = {};
         for (int i = 0; i < n; ++i) ++cnt[grp(i) + 1];
         for (int g = 0; g < NGROUPS; ++g) cnt[g + 1] += cnt[g];
-        for (int i = 0; i < n; ++i) g_st_order[cnt[grp(i)]++] = i;
+        for (int i = 0; i < n; ++i) G.order[cnt[grp(i)]++] = i;
     }
     BatchHdr H{};  // zero: every counter of the header starts at zero
     H.n = n;
     int gmask = 0;
     size_t pool = 0;
     for (int r = 0; r < n; ++r) {
-        const g3l_integral &it = items[g_st_order[r]];
-        IntDesc &d = g_st_desc[r];
+        const g3l_integral &it = items[G.order[r]];
+        IntDesc &d = G.desc[r];
         fill_desc(c, it, precision, d);
         unsigned long long cap;
         if (it.max_eval) {
@@ -2105,7 +2094,7 @@ try {
         d.cap = (int)cap;
         d.base = (long long)pool;
         pool += cap;
-        gmask |= 1 << grp(g_st_order[r]);
+        gmask |= 1 << grp(G.order[r]);
     }
     const StaticLayout L = static_layout(n, pool);
     if (L.end > kStaticScratchBytes) {
@@ -2117,19 +2106,15 @@ try {
         return G3L_ERR_INVALID;
     }
     for (int g = 0, r = 0; g <= NGROUPS; ++g) {
-        while (r < n && grp(g_st_order[r]) < g) ++r;
+        while (r < n && grp(G.order[r]) < g) ++r;
         H.gbeg[g] = r;
     }
     H.gbeg[NGROUPS] = n;
     H.max_rounds = c->opt.max_rounds;
     H.mixed = precision == G3L_MIXED ? 1 : 0;
-    set_esc_queues(g_st_desc, n, H);
+    set_esc_queues(G.desc, n, H);
     H.dbg = nullptr;
 
-    G3L_CK(cudaSetDevice(c->device));
-    unsigned char *base = nullptr;
-    int st = static_scratch(c->device, &base);
-    if (st) return st;
     KernelArgs a{};
     a.T = c->T;
     a.H = (BatchHdr *)(base + L.H);
@@ -2158,9 +2143,9 @@ try {
     cudaStream_t s = c->stream;
     // The uploaded header and the init kernel's states are all that must start at a
     // known value; the pools are written before they are read.
-    G3L_CK(cudaMemcpyAsync(a.D, g_st_desc, sizeof(IntDesc) * n, cudaMemcpyHostToDevice, s));
+    G3L_CK(cudaMemcpyAsync(a.D, G.desc, sizeof(IntDesc) * n, cudaMemcpyHostToDevice, s));
     G3L_CK(cudaMemcpyAsync(a.H, &H, sizeof(BatchHdr), cudaMemcpyHostToDevice, s));
-    int launches = 0;
+    int launches = 0, st = G3L_OK;
     {
         void *args[] = {&a.D, &a.S, &a.P, &a.H};
         G3L_CK(cudaLaunchKernel(init_kernel(), dim3(c->nsm * 4), dim3(256), args, 0, s));
@@ -2209,37 +2194,83 @@ try {
         G3L_CK(cudaStreamSynchronize(s));
     }
     BatchHdr Hout;
-    G3L_CK(cudaMemcpyAsync(g_st_state, a.S, sizeof(IntState) * n, cudaMemcpyDeviceToHost, s));
+    G3L_CK(cudaMemcpyAsync(G.state, a.S, sizeof(IntState) * n, cudaMemcpyDeviceToHost, s));
     G3L_CK(cudaMemcpyAsync(&Hout, a.H, sizeof(BatchHdr), cudaMemcpyDeviceToHost, s));
     G3L_CK(cudaStreamSynchronize(s));
     G3L_CK(cudaGetLastError());
+    // statistics as g3l_eval reports them for host-driven rounds (without the per-kernel
+    // timings, which would need events)
+    g3l_stats sx{};
     int first_bad = G3L_OK;
+    uint64_t pts = 0;
     for (int r = 0; r < n; ++r) {
-        const IntDesc &d = g_st_desc[r];
-        const IntState &sr = g_st_state[r];
-        g3l_result &o = out[g_st_order[r]];
+        const IntDesc &d = G.desc[r];
+        const IntState &sr = G.state[r];
+        sx.group_points[d.kind * 3 + d.term - 1] += sr.neval;
+        g3l_result &o = out[G.order[r]];
         o.val = sr.val * d.scale;
         o.err = sr.err * d.scale;
         o.neval = sr.neval;
         o.status = sr.done ? sr.status : G3L_ERR_ROUNDS;
         o.rounds = sr.rounds;
         o.result = host::apply_prefactor(d.kind, d.term, c->H0, c->Om, o.val);
+        pts += sr.neval;
         if (o.status && !first_bad) first_bad = o.status;
     }
-    c->stats = g3l_stats{};
-    c->stats.kernel_launches = (uint64_t)launches;
-    c->stats.rounds = (uint64_t)Hout.rounds_done;
-    c->stats.regions_evaluated = Hout.regions;
-    c->stats.tie_fallbacks = Hout.ties;
-    c->stats.small_arg_fp64 = Hout.small_arg;
-    c->stats.escalated = Hout.escalated;
-    c->stats.deferred = Hout.deferred;
-    c->stats.polished = Hout.polished;
-    c->stats.h2d_bytes = sizeof(IntDesc) * n + sizeof(BatchHdr);
-    c->stats.d2h_bytes = sizeof(IntState) * n + sizeof(BatchHdr) + sizeof(int) * Hout.rounds_done;
+    sx.kernel_launches = (uint64_t)launches;
+    sx.rounds = (uint64_t)Hout.rounds_done;
+    sx.regions_evaluated = Hout.regions;
+    sx.points_evaluated = pts;
+    sx.tie_fallbacks = Hout.ties;
+    sx.small_arg_fp64 = Hout.small_arg;
+    sx.escalated = Hout.escalated;
+    sx.escalated_full = Hout.esc_full;
+    sx.deferred = Hout.deferred;
+    sx.polished = Hout.polished;
+    sx.h2d_bytes = sizeof(IntDesc) * n + sizeof(BatchHdr);
+    sx.d2h_bytes = sizeof(IntState) * n + sizeof(BatchHdr) + sizeof(int) * Hout.rounds_done;
+    c->stats = sx;
     if (first_bad)
         host::set_error("g3l_eval_static: an integral ended with status " + std::to_string(first_bad));
     return first_bad;
+}
+
+}  // namespace
+
+extern "C" int g3l_eval_static(g3l_ctx *c, const g3l_integral *items, int n, int precision,
+                               g3l_result *out)
+try {
+    if (!c || n < 0 || (n > 0 && (!items || !out)) ||
+        (precision != G3L_FP64 && precision != G3L_MIXED)) {
+        host::set_error("g3l_eval_static: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    if (n == 0) return G3L_OK;
+    if (precision == G3L_MIXED && !evalmx_kernel(0, 1)) {
+        host::set_error("g3l_eval_static: mixed-precision kernels not built");
+        return G3L_ERR_INVALID;
+    }
+    if (n > kStaticMaxItems) {
+        host::set_error("g3l_eval_static: " + std::to_string(n) + " integrals exceed the limit of " +
+                        std::to_string(kStaticMaxItems) + " per call");
+        return G3L_ERR_INVALID;
+    }
+    for (int i = 0; i < n; ++i)
+        if (!item_ok(c, items[i])) {
+            host::set_error("g3l_eval_static: invalid integral " + std::to_string(i));
+            return G3L_ERR_INVALID;
+        }
+    G3L_CK(cudaSetDevice(c->device));
+    unsigned char *base = nullptr;
+    int st = static_scratch(c->device, &base);
+    if (st) return st;
+    StaticStage &G = g_st[c->device];
+    std::lock_guard<std::mutex> lk(G.mu);
+    st = eval_static_locked(c, items, n, precision, out, G, base);
+    // A call that failed part-way may have kernels still queued: let them finish before
+    // the next call on this device reuses the scratch.
+    if (st) cudaStreamSynchronize(c->stream);
+    return st;
 } catch (const std::bad_alloc &) {
     host::set_error("g3l_eval_static: host allocation failed");
     return G3L_ERR_NOMEM;

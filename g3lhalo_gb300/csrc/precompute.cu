@@ -109,6 +109,12 @@ __device__ __forceinline__ double d_tophat(double k, double R)
     return ((x * x - 3.) * sin(x) + 3. * x * cos(x)) * 3 * k / x / x / x / x;
 }
 
+// The Eisenstein & Hu (1998, ApJ 496, 605) transfer function with baryon acoustic
+// terms: eqs. 17-21 (CDM part T_c with the ln/C fitting forms), eqs. 21-24 (baryon part
+// T_b with the node shift s_tilde and Silk damping), weighted by the baryon fraction.
+// The names of its intermediate quantities are those of the paper's published code, and
+// the operation order is the reference's (src/Powerspectrum.cpp:153-186), which the
+// table parity (<= 1e-13 relative) depends on.
 __device__ double transfer(const PkDev &P, double k)
 {   // src/Powerspectrum.cpp:153-186
     if (k == 0.0) return 1.0;

@@ -271,16 +271,23 @@ int g3l_debug_region(g3l_ctx *ctx, const g3l_integral *item, const double *cente
  * allocator, or a loop that cannot take an allocation's implicit synchronisation.
  *  - Scratch: one fixed 64 MiB device array per device, built into the library.  A
  *    call may hold at most 1024 integrals and as many region slots as fit beside them
- *    and the 15 MB of re-evaluation scratch (about 116 bytes per slot; each integral
+ *    and the ~18 MB of re-evaluation scratch (about 116 bytes per slot; each integral
  *    takes 3 + (max_eval + P) / (2 P) slots for its P-point rule, so ~420k slots, e.g.
- *    200 seven-dimensional integrals at max_eval = 1e6).  Larger calls fail with
- *    G3L_ERR_INVALID and a message stating the bytes needed; nothing is evaluated.
+ *    200 seven-dimensional integrals at max_eval = 1e6).  An item with max_eval = 0
+ *    takes the context's unlimited_pool slots (g3l_options; 1 << 20 by default, more
+ *    than the scratch holds), so such items need unlimited_pool lowered to ~400k or
+ *    less.  Larger calls fail with G3L_ERR_INVALID and a message stating the bytes
+ *    needed; nothing is evaluated.
  *  - Set-up: the first call on a device looks up the scratch's device address (with
  *    that device current); make that first call before capturing any stream.
- *  - The scratch is shared by every context on a device: calls must not overlap
- *    (from several threads, contexts or streams); overlapping calls race.
+ *  - The scratch (and the host staging beside it) is shared by every context on a
+ *    device and keeps the last call's contents.  Two calls whose kernels were on the
+ *    GPU at once would race on it; the library prevents that by serialising the calls
+ *    on one device with a lock, and every call waits for its own kernels before it
+ *    returns.  Calls on different devices run side by side.
  *  - Rounds are driven from the host with plain kernel launches (one small
- *    device-to-host read per round); the context's own workspace is not touched. */
+ *    device-to-host read per round).  The context's workspace (its pools and graphs)
+ *    is not touched; its statistics (g3l_get_stats) are replaced by this call's. */
 int g3l_eval_static(g3l_ctx *ctx, const g3l_integral *items, int n, int precision,
                     g3l_result *out);
 

@@ -6,8 +6,15 @@
 # /root/reference/src); nothing is copied.  -ffp-contract=off keeps the host
 # arithmetic free of fused multiply-adds on every platform, so the build and the
 # oracle restatement evaluate the same IEEE operations.
+#
+# This script is the one place that names the reference's mount point; the Python
+# side asks it (`build_ref.sh --where`) instead of repeating the path.
 set -euo pipefail
 REF=${G3L_REF_SRC:-/root/reference/src}
+if [ "${1:-}" = "--where" ]; then
+    echo "$REF"
+    exit 0
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/NNMap_Model.cu" ]; then

@@ -39,11 +39,21 @@ def build_oracle(force: bool = False) -> str:
     return LIB
 
 
+def ref_src() -> str:
+    """Directory of the reference's sources: G3L_REF_SRC, else the mount point that
+    oracle/build_ref.sh (the recipe that compiles them) documents."""
+    if os.environ.get("G3L_REF_SRC"):
+        return os.environ["G3L_REF_SRC"]
+    r = subprocess.run([os.path.join(HERE, "build_ref.sh"), "--where"], capture_output=True,
+                       text=True)
+    return r.stdout.strip()
+
+
 def build_ref(scaling: bool = False) -> str | None:
     """Build the reference CPU path (and its SCALING build) when its sources are
     present; the requested library's path, or None where it cannot be had."""
     want = REF_LIB_SCALING if scaling else REF_LIB
-    src = os.environ.get("G3L_REF_SRC", "/root/reference/src")
+    src = ref_src()
     if not os.path.exists(os.path.join(src, "NNMap_Model.cu")):
         return want if os.path.exists(want) else None
     if not (os.path.exists(REF_LIB) and os.path.exists(REF_LIB_SCALING)):

@@ -9,6 +9,7 @@ same integrals.
 """
 import os
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -17,7 +18,10 @@ import g3lhalo_gb300 as G
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CPP = os.path.join(ROOT, "tests", "cpp")
-REF_SRC = "/root/reference/src"
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import pyoracle  # noqa: E402  (the checker's helpers: where the reference sources lie)
+
+REF_SRC = pyoracle.ref_src()
 
 
 def _build_driver(tmp_path):

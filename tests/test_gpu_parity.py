@@ -33,7 +33,8 @@ def _rel(a, b):
     return abs(a - b) / max(abs(b), 1e-300)
 
 
-def test_densities_on_device_match_reference(ctx, golden):
+def test_host_densities_match_reference(ctx, golden):
+    """rho_bar and n_bar as g3l_set_hod computes them (the host Gauss-Kronrod path)."""
     rho, n1 = ctx.densities(0)
     _, n2 = ctx.densities(1)
     np.testing.assert_allclose(rho, golden["nn_rho_bar"], rtol=1e-15)

@@ -65,3 +65,40 @@ def test_static_entry_rejects_oversized_batches(ctx):
     big = [(G.NNMAP, 3, 0, 1, tuple(trip[0]), 1e-4, 100_000_000)] * 10
     st, _ = _eval_static(ctx, big, G.FP64)
     assert st == 1 and b"bytes of scratch" in A.lib().g3l_last_error()
+
+
+def test_static_entry_stats_and_threads_on_one_device(ctx):
+    """The call's statistics are filled like g3l_eval's; two threads calling at once on
+    one device (two contexts sharing its scratch) get their sequential results, because
+    the library serialises calls on a device."""
+    import threading
+    specs = _specs()
+    st, r = _eval_static(ctx, specs, G.MIXED)
+    assert st == 0
+    s = ctx.stats()
+    assert s["points_evaluated"] == int(r["neval"].sum())
+    assert sum(s["group_points"]) == s["points_evaluated"]
+    assert s["escalated_full"] <= s["escalated"]
+    T2 = make_tables(Nz=64, Nm=128, Nk=256)
+    c2 = G.Context(T2, clamp_k=True)
+    c2.set_hod(0, W.hod_second())
+    c2.set_hod(1, W.hod_default())
+    specs2 = [(k, t, 0, 1 if k == G.NNMAP else 0, th, rt, me) for (k, t, _, _, th, rt, me) in specs]
+    seq = [_eval_static(ctx, specs, G.MIXED)[1], _eval_static(c2, specs2, G.MIXED)[1]]
+    got = [None, None]
+
+    def run(k, c, sp):
+        for _ in range(3):
+            got[k] = _eval_static(c, sp, G.MIXED)
+
+    th = [threading.Thread(target=run, args=(0, ctx, specs)),
+          threading.Thread(target=run, args=(1, c2, specs2))]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for k in range(2):
+        assert got[k][0] == 0
+        assert np.array_equal(got[k][1]["val"], seq[k]["val"])
+        assert np.array_equal(got[k][1]["neval"], seq[k]["neval"])
+    c2.close()
