@@ -17,12 +17,17 @@ Reported (one JSON line on rank 0):
   roofline    the dominant rule kernel (NNMap 2-halo) against the measured FP32
               FMA rate of this device
   cpu_baseline the CPU oracle (restated reference CPU path, OpenMP over all host
-              cores) on a bounded sample, extrapolated to one evaluation
-Further legs: serving (continuous batching at a sweep of Poisson arrival rates, and the
-same stream on an FP64 server), sweep (256 HOD vectors in one launch), nmapmap_twopop
-(NMapMap plus two-population NNMap), precompute (the table precomputation on 64 bins).
---impl reference times the reference's CPU path alone (oracle/_ref where the
-reference compiled, else the oracle restatement) on the same workload.
+              cores) on 11 of the 220 triplets, timed; value = 11/220 of an evaluation
+              per measured second
+Further legs: serving (continuous batching at a sweep of Poisson arrival rates, each
+served result checked against g3l_eval; the same stream on an FP64 server, with every
+term compared), sweep (256 HOD vectors in one launch; the first 16 again in FP64, every
+term compared), nmapmap_twopop (NMapMap plus two-population NNMap), config0 (the FP64
+1-halo term of 5 equal-scale triplets on the host cores and on the device), precompute
+(the table precomputation on 64 bins).
+--impl reference times the reference's CPU path alone (the oracle restatement) on the
+same workload: the timed steps split the 220 triplets round robin, so 20 steps time one
+whole model evaluation, measured, not extrapolated.
 """
 from __future__ import annotations
 
@@ -84,7 +89,15 @@ def parse():
     ap.add_argument("--no-precompute", action="store_true")
     # batched fit sweep: this many HOD vectors in one launch (0 = skip)
     ap.add_argument("--sweep", type=int, default=256)
+    # of which this many are integrated again in the FP64 form and compared term by term
+    ap.add_argument("--sweep-parity", type=int, default=16)
+    ap.add_argument("--no-config0", action="store_true")
     return ap.parse_args()
+
+
+def W_hod_default():
+    from g3lhalo_gb300 import workloads as W
+    return W.hod_default()
 
 
 def workload():
@@ -157,50 +170,79 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(T, trip, hod, me, n_trip):
-    """Oracle on the host cores: n_trip triplets x 3 terms, extrapolated to 220."""
+def _oracle(T, hod):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as P
-    O = P.Oracle(T, hod, hod, clamp_k=True)
-    idx = np.linspace(0, len(trip) - 1, n_trip).astype(int)
+    # one population (hod1 == hod2): the same-population branch, as the device runs it
+    return P.Oracle(T, hod, None, clamp_k=True)
+
+
+def _cpu_terms(O, trip, idx, me, terms=(1, 2, 3)):
+    """The oracle's FP64 terms of triplets idx (NNMap, one population); wall seconds and
+    integrand points."""
     t0 = time.perf_counter()
     pts = 0
     for i in idx:
-        for t in (1, 2, 3):
+        for t in terms:
             pts += O.term(0, t, trip[i], 1, 2, maxEval=me, rtol=RTOL)[2]
-    dt = time.perf_counter() - t0
-    per_eval = dt * len(trip) / n_trip
-    return {"value": 1.0 / per_eval, "unit": "evals/s", "cores": os.cpu_count(),
+    return time.perf_counter() - t0, pts
+
+
+def cpu_sample(T, trip, hod, me, n_trip):
+    """Oracle on the host cores: n_trip evenly spaced triplets x 3 terms, timed; the
+    rate is the fraction of a model evaluation they make (n_trip / 220) per second."""
+    O = _oracle(T, hod)
+    idx = np.linspace(0, len(trip) - 1, n_trip).astype(int)
+    dt, pts = _cpu_terms(O, trip, idx, me)
+    return {"value": (n_trip / len(trip)) / dt, "unit": "evals/s", "cores": os.cpu_count(),
             "kind": "port", "seconds": dt, "points_per_s": pts / dt,
-            "sample": "%d of 220 triplets x 3 terms at maxEval %d (oracle restatement of the "
-                      "reference CPU path, OpenMP over all host cores), extrapolated linearly "
-                      "to 220 triplets" % (n_trip, me)}
+            "sample": "%d evenly spaced of the 220 triplets x 3 terms at maxEval %d (oracle "
+                      "restatement of the reference CPU path, OpenMP over all host cores); "
+                      "value = %d/220 of an evaluation / the measured seconds" % (n_trip, me, n_trip)}
+
+
+def reference_steps(n_trip, steps):
+    """Triplets of each timed step of the reference arm: step s takes every triplet
+    j with j % steps == s % steps, so `steps` consecutive steps cover all of them."""
+    k = max(1, min(steps, n_trip))
+    return [list(range(s % k, n_trip, k)) for s in range(steps)]
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU path (the oracle restatement, OpenMP over all host cores) on
+    the benchmark's model evaluation, measured: the timed steps split the 220 triplets
+    between them (round robin), so --steps 20 time exactly one whole evaluation; the
+    value is the evaluations covered / the measured seconds.  Warm-up steps take one
+    triplet each."""
     if rank != 0:
         return
     T, trip, hods = workload()
-    ref_kind = "port"
-    res = []
-    n_trip = 6
-    for _ in range(args.warmup):
-        pass  # the CPU path has no warm-up state; every step is measured
-    for s in range(args.steps):
-        r = cpu_sample(T, trip, hods[s % len(hods)], args.max_eval, n_trip)
-        res.append(1.0 / r["value"])
-    ms = 1000.0 * float(np.mean(res))
-    value = 1000.0 / ms
+    O = _oracle(T, hods[0])
+    for s in range(args.warmup):
+        _cpu_terms(O, trip, [(7 * s) % len(trip)], args.max_eval)
+    parts = reference_steps(len(trip), args.steps)
+    res, covered = [], 0
+    for idx in parts:
+        dt, _ = _cpu_terms(O, trip, idx, args.max_eval)
+        res.append(dt)
+        covered += len(idx)
+    total = float(np.sum(res))
+    evals = covered / len(trip)
+    value = evals / total
+    sample = ("%d timed steps of %s triplets x 3 terms each (round robin over the 220), "
+              "%.3g model evaluations in %.1f s measured, no extrapolation"
+              % (args.steps, "/".join(sorted({str(len(p)) for p in parts})), evals, total))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
             "config": config(len(trip), args.max_eval),
+            "evaluations_timed": evals,
             "p50_ms": float(np.percentile(np.array(res) * 1e3, 50)),
             "p99_ms": float(np.percentile(np.array(res) * 1e3, 99)),
             "cpu_baseline": {"value": value, "unit": "evals/s", "cores": os.cpu_count(),
-                             "kind": ref_kind,
-                             "sample": "per step %d of 220 triplets x 3 terms, extrapolated" % n_trip},
+                             "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -217,8 +259,19 @@ def max_over_ranks(dev_s, wall_s, dist=None):
     return float(tt[0]), float(tt[1])
 
 
-def sweep_leg(G, ctx, trip, hods, n_hod, max_eval):
-    """Batched fit sweep: n_hod HOD vectors x 220 triplets x 3 terms in one launch."""
+def parity(mixed, fp64):
+    """Largest relative deviation of every mixed-precision term from the FP64 form."""
+    rel = np.abs(mixed["val"] - fp64["val"]) / np.abs(fp64["val"])
+    return {"max_rel": float(rel.max()), "median_rel": float(np.median(rel)),
+            "terms": int(rel.size), "terms_over_1e-4": int((rel > 1e-4).sum()),
+            "neval_identical": bool(np.array_equal(mixed["neval"], fp64["neval"])),
+            "status_ok": bool((mixed["status"] == 0).all() and (fp64["status"] == 0).all())}
+
+
+def sweep_leg(G, ctx, trip, hods, n_hod, max_eval, n_parity):
+    """Batched fit sweep: n_hod HOD vectors x 220 triplets x 3 terms in one launch; the
+    first n_parity vectors are integrated again in the FP64 form (one call) and every
+    one of their terms compared."""
     from g3lhalo_gb300 import workloads as W
     hs = hods[:n_hod] if n_hod <= len(hods) else W.hod_sweep(n_hod, seed=12345)
     t0 = time.perf_counter()
@@ -232,13 +285,54 @@ def sweep_leg(G, ctx, trip, hods, n_hod, max_eval):
     r = ctx.eval(specs, G.MIXED)
     wall = time.perf_counter() - t0
     st = ctx.stats()
-    return {"hod_vectors": n_hod, "integrals": len(specs),
-            "model_evals_per_s": n_hod / (st["device_ms"] * 1e-3),
-            "device_ms": st["device_ms"], "wall_s": wall, "hod_update_s": t_hod,
-            "points_per_s": st["points_evaluated"] / (st["device_ms"] * 1e-3),
-            "rounds": st["rounds"], "status_ok": bool((r["status"] == 0).all()),
-            "workload": "%d seeded HOD vectors (the fit-sweep box) x 220 triplets x 1h+2h+3h, "
-                        "rtol 1e-4, maxEval %d, one g3l_eval call" % (n_hod, max_eval)}
+    out = {"hod_vectors": n_hod, "integrals": len(specs),
+           "model_evals_per_s": n_hod / (st["device_ms"] * 1e-3),
+           "device_ms": st["device_ms"], "wall_s": wall, "hod_update_s": t_hod,
+           "points_per_s": st["points_evaluated"] / (st["device_ms"] * 1e-3),
+           "rounds": st["rounds"], "status_ok": bool((r["status"] == 0).all()),
+           "workload": "%d seeded HOD vectors (the fit-sweep box) x 220 triplets x 1h+2h+3h, "
+                       "rtol 1e-4, maxEval %d, one g3l_eval call" % (n_hod, max_eval)}
+    if n_parity:
+        m = min(n_parity, n_hod) * 3 * len(trip)
+        r64 = ctx.eval(specs[:m], G.FP64)
+        par = parity(r[:m], r64)
+        par["hod_vectors"] = min(n_parity, n_hod)
+        par["fp64_device_ms"] = ctx.stats()["device_ms"]
+        out["parity_vs_fp64"] = par
+    return out
+
+
+def config0_leg(G, T, hod, max_eval):
+    """SURVEY config 0: the FP64 NNMap 1-halo term on the 5 equal-scale triplets
+    (0.5', 1', 2', 4', 8'), rtol 1e-4, maxEval 1e6, on the host cores (the oracle
+    restatement of the reference CPU path, OpenMP over all cores) and on the device in
+    both forms, with the device results against the host's."""
+    from g3lhalo_gb300 import workloads as W
+    tri = W.triplets_equal()
+    O = _oracle(T, hod)
+    t0 = time.perf_counter()
+    cpu = [O.term(0, 1, tuple(th), 1, 2, maxEval=max_eval, rtol=RTOL) for th in tri]
+    cpu_s = time.perf_counter() - t0
+    c = G.Context(T, device=0)
+    c.set_hod(0, hod)
+    specs = [(G.NNMAP, 1, 0, 0, tuple(th), RTOL, max_eval) for th in tri]
+    out = {"integrals": len(specs), "cpu_s": cpu_s, "cpu_cores": os.cpu_count(),
+           "cpu_kind": "port"}
+    vc = np.array([x[0] for x in cpu])
+    nc = np.array([x[2] for x in cpu])
+    for name, prec in (("fp64", G.FP64), ("mixed", G.MIXED)):
+        c.eval(specs, prec)
+        ms = []
+        for _ in range(3):
+            r = c.eval(specs, prec)
+            ms.append(c.stats()["device_ms"])
+        out[name] = {"device_ms": float(np.median(ms)), "speedup_vs_cpu": cpu_s / (np.median(ms) * 1e-3),
+                     "max_rel_vs_cpu": float(np.max(np.abs(r["val"] - vc) / np.abs(vc))),
+                     "neval_identical_to_cpu": bool(np.array_equal(r["neval"], nc))}
+    c.close()
+    out["workload"] = ("NNMap 1-halo, FP64, theta1=theta2=theta3 in {0.5,1,2,4,8} arcmin, rtol "
+                       "1e-4, maxEval %d, benchmark tables, default HOD" % max_eval)
+    return out
 
 
 def config2_leg(G, trip, max_eval, reps=3):
@@ -338,7 +432,7 @@ def serve_stream(G, ctx, precision, reqs, rate, rng):
     srv = G.Server(ctx, precision, max_items_per_term=2048, pool_regions=1 << 24,
                    rounds_per_launch=4)
     gaps = rng.exponential(1.0 / rate, len(reqs))
-    tickets, lat = [], []
+    tickets, lat, res = [], [], []
     t0 = time.perf_counter()
     for q, gap in zip(reqs, gaps):
         time.sleep(gap)
@@ -346,15 +440,27 @@ def serve_stream(G, ctx, precision, reqs, rate, rng):
     for t in tickets:
         r, ms = srv.poll(t)
         lat.append(ms)
+        res.append(r)
     wall = time.perf_counter() - t0
     info = srv.info()
     srv.close()
     n_int = sum(len(q) for q in reqs)
-    return {"arrival_rate_per_s": rate, "requests": len(reqs), "integrals": n_int,
-            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "mean_ms": float(np.mean(lat)), "wall_s": wall,
-            "requests_per_s": len(reqs) / wall,
-            "model_evals_per_s": n_int / 660.0 / wall, "launches": info["launches"]}
+    out = {"arrival_rate_per_s": rate, "requests": len(reqs), "integrals": n_int,
+           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "mean_ms": float(np.mean(lat)), "wall_s": wall,
+           "requests_per_s": len(reqs) / wall,
+           "model_evals_per_s": n_int / 660.0 / wall, "launches": info["launches"]}
+    return out, res
+
+
+def served_equals_eval(G, ctx, precision, reqs, res):
+    """Every served request against g3l_eval of the same integrals in the same form (one
+    call): integrals whose value or evaluation count differ."""
+    flat = [it for q in reqs for it in q]
+    ref = ctx.eval(flat, precision)
+    got = np.concatenate(res)
+    return {"integrals": len(flat),
+            "differ": int(np.sum((got["val"] != ref["val"]) | (got["neval"] != ref["neval"])))}
 
 
 def serving_leg(G, ctx, trip, hods, args, n_req=48, n_fp64=6, seed=7):
@@ -365,18 +471,23 @@ def serving_leg(G, ctx, trip, hods, args, n_req=48, n_fp64=6, seed=7):
     rates = []
     for i, rate in enumerate(SERVING_RATES):
         rng = np.random.default_rng(seed + i)
-        rates.append(serve_stream(G, ctx, G.MIXED, serving_requests(trip, n_req, args.max_eval,
-                                                                    rng), rate, rng))
+        reqs = serving_requests(trip, n_req, args.max_eval, rng)
+        o, res = serve_stream(G, ctx, G.MIXED, reqs, rate, rng)
+        # continuous batching must not change a result: served == g3l_eval, bit for bit
+        o["vs_eval_mixed"] = served_equals_eval(G, ctx, G.MIXED, reqs, res)
+        rates.append(o)
     rng = np.random.default_rng(seed + 100)
     reqs = serving_requests(trip, n_fp64, args.max_eval, rng)
-    mixed = serve_stream(G, ctx, G.MIXED, reqs, SERVING_RATES[-1], np.random.default_rng(1))
-    fp64 = serve_stream(G, ctx, G.FP64, reqs, SERVING_RATES[-1], np.random.default_rng(1))
+    mixed, rm = serve_stream(G, ctx, G.MIXED, reqs, SERVING_RATES[-1], np.random.default_rng(1))
+    fp64, rf = serve_stream(G, ctx, G.FP64, reqs, SERVING_RATES[-1], np.random.default_rng(1))
     low = rates[0]
     return {"p50_ms": low["p50_ms"], "p99_ms": low["p99_ms"],
             "arrival_rate_per_s": low["arrival_rate_per_s"], "rates": rates,
             "saturated_same_stream": {"requests": n_fp64, "mixed": mixed, "fp64": fp64,
                                       "mixed_over_fp64": mixed["model_evals_per_s"] /
-                                                         fp64["model_evals_per_s"]},
+                                                         fp64["model_evals_per_s"],
+                                      "parity_vs_fp64": parity(np.concatenate(rm),
+                                                               np.concatenate(rf))},
             "workload": "seeded Poisson arrivals at %s req/s, %d requests each; triplets per "
                         "request log-uniform 1..220, NNMap or NMapMap 1h+2h+3h, rtol in "
                         "{1e-3, 1e-4, 1e-5}, maxEval %d, 8 HOD vectors from the fit-sweep box; "
@@ -528,20 +639,25 @@ def main():
             if r is not None:
                 out["serving"] = r
         if args.sweep:
-            r = leg("sweep", lambda: sweep_leg(G, ctx, trip, hods, args.sweep, args.max_eval))
+            r = leg("sweep", lambda: sweep_leg(G, ctx, trip, hods, args.sweep, args.max_eval,
+                                               args.sweep_parity))
             if r is not None:
                 out["sweep"] = r
         if not args.no_config2:
             r = leg("nmapmap_twopop", lambda: config2_leg(G, trip, args.max_eval))
             if r is not None:
                 out["nmapmap_twopop"] = r
+        if not args.no_config0:
+            r = leg("config0", lambda: config0_leg(G, T, W_hod_default(), args.max_eval))
+            if r is not None:
+                out["config0"] = r
         pre = None
         if not args.no_precompute:
             r = leg("precompute", lambda: precompute_leg(G))
             if r is not None:
                 pre, out["precompute"] = r
         if not args.no_cpu:
-            out["cpu_baseline"] = cpu_sample(T, trip, hods[last_hod], args.max_eval, 4)
+            out["cpu_baseline"] = cpu_sample(T, trip, hods[last_hod], args.max_eval, 11)
             if pre is not None:
                 r = leg("cpu_precompute", lambda: precompute_cpu(pre))
                 if r is not None:

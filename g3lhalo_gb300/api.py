@@ -26,7 +26,9 @@ NNMAP = 0
 NMAPMAP = 1
 
 STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "POOL", 5: "NONFINITE",
-          6: "CANCELLED", 7: "ROUNDS", 8: "NO_DEVICE", 9: "BUSY"}
+          6: "CANCELLED", 7: "ROUNDS", 8: "NO_DEVICE", 9: "BUSY", 10: "DEADLINE"}
+# statuses of a finished call whose per-integral results are still returned
+_PARTIAL = (4, 5, 6, 7, 10)
 
 _dp = C.POINTER(C.c_double)
 
@@ -89,7 +91,7 @@ class Options(C.Structure):
                 ("unc_tau_abs", C.c_double), ("unc_tau_impact", C.c_double),
                 ("unc_tau_sel", C.c_double), ("unc_tau_val", C.c_double),
                 ("unc_eps_val", C.c_double), ("unc_eps_sel", C.c_double),
-                ("evalmx_variant", C.c_int * 6)]
+                ("evalmx_variant", C.c_int * 6), ("deadline_ms", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -149,6 +151,7 @@ def lib():
             L.g3l_measure_peaks.argtypes = [C.c_void_p, _dp, _dp]
             L.g3l_debug_region.argtypes = [C.c_void_p, C.POINTER(Integral), _dp,
                                            C.POINTER(C.c_int), C.c_int, _dp, _dp]
+            L.g3l_eval_cancel.argtypes = [C.c_void_p]
             L.g3l_eval_static.argtypes = [C.c_void_p, C.POINTER(Integral), C.c_int, C.c_int,
                                           C.POINTER(Result)]
             L.g3l_autotune.argtypes = [C.c_void_p, C.POINTER(Integral), C.c_int,
@@ -410,18 +413,25 @@ class Context:
         st = lib().g3l_eval_terms(self.h, kind, _ptr(th), n, hod1, hod2, term_mask, rtol,
                                   int(max_eval), precision, _ptr(val), _ptr(err), _ptr(res),
                                   C.byref(ne))
-        if st not in (0, 4, 5, 7):
+        if st != 0 and st not in _PARTIAL:
             _check(st)
         return val[:n], err[:n], res[:n], ne.value
 
     def eval(self, specs, precision=FP64, check=True):
-        """Integrate every spec in one launch; returns a structured numpy array."""
+        """Integrate every spec in one launch; returns a structured numpy array.  Calls
+        that end with per-integral statuses (pool, non-finite, cancelled, round cap,
+        deadline) return their results; the statuses are in the array."""
         items, n = self.make_items(specs)
         out = (Result * max(1, n))()
         st = lib().g3l_eval(self.h, items, n, precision, out)
-        if check and st != 0 and st not in (4, 5, 7):
+        if check and st != 0 and st not in _PARTIAL:
             _check(st)
         return results_to_numpy(out, n)
+
+    def cancel_eval(self):
+        """Stop the eval() running on this context from another thread (g3l_eval_cancel):
+        its unfinished integrals end with status 6 at the next refinement round."""
+        _check(lib().g3l_eval_cancel(self.h))
 
 
 def results_to_numpy(out, n):

@@ -208,7 +208,16 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
     __shared__ SelShared sh;
     __shared__ int s_flag[4];  // fin, status, polish passes
     __shared__ double s_tot[2];
+    __shared__ int s_cancel;
     const int n = H->n;
+    // a stop request: k_scan's (cancel or deadline), or a host cancel that arrived since
+    // (one read of the host-mapped word per block)
+    if (threadIdx.x == 0) {
+        int cz = H->cancel;
+        if (!cz && H->cancel_word && *H->cancel_word) cz = 1;
+        s_cancel = cz;
+    }
+    __syncthreads();
     for (int i = blockIdx.x; i < n; i += gridDim.x) {
         if (pass == 1 && !S[i].defer) continue;  // block-uniform
         __syncthreads();
@@ -242,9 +251,9 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
         if (threadIdx.x == 0) {
             IntState st = S[i];
             int fin = 0, status = ST_OK;
-            if (H->cancel) {
+            if (s_cancel) {
                 fin = 1;
-                status = ST_CANCELLED;
+                status = s_cancel == 2 ? ST_DEADLINE : ST_CANCELLED;
             } else if (!isfinite(V) || !isfinite(E)) {
                 fin = 1;
                 status = ST_NONFINITE;
@@ -497,6 +506,13 @@ __global__ void __launch_bounds__(1024) k_scan(IntState *__restrict__ S, long lo
         H->any_active = more;
         H->regions += 2ull * (unsigned long long)tot;
         if (more) H->rounds_done += 1;
+        // a cancel from the host, or the deadline, stops every unfinished integral at the
+        // next round's selection (this round's work still runs, so the pools stay whole)
+        if (!H->cancel) {
+            if (H->cancel_word && *H->cancel_word) H->cancel = 1;
+            else if (H->deadline_ns && global_timer_ns() - H->t0_ns > H->deadline_ns)
+                H->cancel = 2;
+        }
         // a serving launch ends after chunk_rounds rounds; this round's body still runs,
         // so the states are consistent for the host between launches
         int go = more;
@@ -545,6 +561,8 @@ __global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, 
         H->deferred = 0;
         H->polished = 0;
         H->esc_full = 0;
+        H->cancel = 0;
+        H->t0_ns = global_timer_ns();
     }
 }
 

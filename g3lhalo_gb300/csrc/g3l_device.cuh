@@ -26,7 +26,7 @@ constexpr int UC_NF_MAX = 4;             // cached u_NFW functions per integrand
 // status codes (mirror g3l_status)
 enum : int {
     ST_OK = 0, ST_INVALID = 1, ST_CUDA = 2, ST_NOMEM = 3, ST_POOL = 4, ST_NONFINITE = 5,
-    ST_CANCELLED = 6, ST_ROUNDS = 7
+    ST_CANCELLED = 6, ST_ROUNDS = 7, ST_DEADLINE = 10
 };
 
 // Genz-Malik degree 7/5 rule (Genz & Malik 1983; src/hcubature.cpp:458-466).
@@ -134,7 +134,8 @@ struct BatchHdr {
     int n;                       // integrals (sorted by group)
     int gbeg[NGROUPS + 1];       // group g = integrals [gbeg[g], gbeg[g+1])
     int max_rounds;
-    int cancel;                  // set by the host to stop the loop
+    int cancel;                  // nonzero stops the loop at the next selection: 1 =
+                                 //   cancelled, 2 = deadline passed (set by k_scan)
     int any_active;              // written by the scan kernel
     long long total_work;
     unsigned long long points;   // statistics
@@ -153,7 +154,20 @@ struct BatchHdr {
     unsigned long long polished; // statistics: finished integrals polished in FP64
     unsigned long long esc_full; // statistics: whole-rule FP64 re-evaluations queued
     double *dbg;                 // debug: per-point integrand values of one work item
+    // In-flight stop of a call: a host-mapped word the host sets from any thread
+    // (nullptr: none), and a deadline on the device's global timer, measured from the
+    // start of the loop (k_init); both are read once per round by k_scan.
+    const volatile int *cancel_word;
+    unsigned long long t0_ns;
+    unsigned long long deadline_ns;  // 0 = none
 };
+
+__device__ __forceinline__ unsigned long long global_timer_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // u_NFW calls of the integrands that depend on one l, one mass and z only.  The points
 // of one Genz-Malik rule take at most UC_MAX distinct (l, m, z) variant combinations

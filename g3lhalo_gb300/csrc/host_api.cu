@@ -7,6 +7,7 @@
 // The loop condition is set on the device by k_scan, so the host waits once,
 // at the end of the call.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <new>
 #include <stdexcept>
@@ -15,6 +16,7 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -134,9 +136,47 @@ struct g3l_ctx {
     // last g3l_eval: descriptor, live region count and pool position of each item
     std::vector<IntDesc> last_D;
     std::vector<int> last_nR, last_pos;
+    // in-flight cancel of g3l_eval: a host-mapped word the device loop reads once per
+    // round; `running` (under run_mu) tells g3l_eval_cancel whether a call is in flight
+    int *cancel_h = nullptr, *cancel_d = nullptr;
+    std::mutex run_mu;
+    bool running = false;
 };
 
 namespace {
+
+// NVTX range for the lifetime of a scope (shown by Nsight tools; free without them)
+struct NvtxScope {
+    explicit NvtxScope(const char *name) { nvtxRangePushA(name); }
+    ~NvtxScope() { nvtxRangePop(); }
+};
+
+// Marks a context's evaluation call as running for g3l_eval_cancel and clears any
+// earlier cancel request, for the lifetime of the call.
+struct RunGuard {
+    g3l_ctx *c;
+    explicit RunGuard(g3l_ctx *cc) : c(cc)
+    {
+        std::lock_guard<std::mutex> lk(c->run_mu);
+        c->running = true;
+        __atomic_store_n(c->cancel_h, 0, __ATOMIC_SEQ_CST);
+    }
+    ~RunGuard()
+    {
+        std::lock_guard<std::mutex> lk(c->run_mu);
+        c->running = false;
+    }
+};
+
+// the header fields that stop a call in flight
+void set_stop_fields(const g3l_ctx *c, BatchHdr &H)
+{
+    H.cancel = 0;
+    H.cancel_word = c->cancel_d;
+    H.deadline_ns = c->opt.deadline_ms > 0
+                        ? (unsigned long long)std::min(c->opt.deadline_ms * 1e6, 1.8e19)
+                        : 0ull;
+}
 
 int upload(g3l_ctx *c, const double *src, size_t n, const double **dst)
 {
@@ -592,6 +632,7 @@ int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
         return G3L_OK;
     };
     for (int r = 0; r < c->opt.max_rounds + 4; ++r) {
+        NvtxScope nv("round");
         void *sargs[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val, &a.pass0};
         G3L_CK(cudaEventRecord(c->tev[14], s));
         G3L_CK(cudaLaunchKernel(select_kernel(), dim3(c->nsm * 8), dim3(256), sargs, 0, s));
@@ -669,7 +710,17 @@ struct SrvReq {
     int remaining = 0;
     bool admitted = false, done = false, cancel = false;
     double t_submit = 0, t_done = 0;
+    nvtxRangeId_t range = 0;  // NVTX range from submission to completion
 };
+
+// a request is complete: close its NVTX range and record the time
+void req_done(SrvReq &q, double t)
+{
+    q.done = true;
+    q.t_done = t;
+    if (q.range) nvtxRangeEnd(q.range);
+    q.range = 0;
+}
 
 // First-fit allocator of pool slot ranges.
 struct RangeAlloc {
@@ -754,8 +805,7 @@ void srv_admit(g3l_server *v, std::vector<IntDesc> &nd, std::vector<int> &ni)
         if (q.cancel) {
             v->pending.pop_front();
             for (auto &r : q.res) r.status = G3L_ERR_CANCELLED;
-            q.done = true;
-            q.t_done = now_s();
+            req_done(q, now_s());
             continue;
         }
         const int m = (int)q.desc.size();
@@ -802,8 +852,7 @@ void srv_fail_all(g3l_server *v, int st, const std::string &msg)
     for (auto &kv : v->reqs)
         if (!kv.second.done) {
             for (auto &r : kv.second.res) r.status = st;
-            kv.second.done = true;
-            kv.second.t_done = now_s();
+            req_done(kv.second, now_s());
         }
     v->pending.clear();
     v->cv_done.notify_all();
@@ -875,6 +924,7 @@ void srv_loop(g3l_server *v)
             beg += cnt[g];
         }
         SRV_CK(cudaMemcpyAsync(v->W.H, &H, sizeof H, cudaMemcpyHostToDevice, s));
+        NvtxScope nv("server launch");
         SRV_CK(cudaGraphLaunch(v->G.exec, s));
         SRV_CK(cudaMemcpyAsync(v->Sh.data(), v->W.S, sizeof(IntState) * v->n, cudaMemcpyDeviceToHost, s));
         SRV_CK(cudaStreamSynchronize(s));
@@ -902,8 +952,7 @@ void srv_loop(g3l_server *v)
                 v->ra.give(d.base, d.cap);
                 v->active -= 1;
                 if (--q.remaining == 0) {
-                    q.done = true;
-                    q.t_done = t;
+                    req_done(q, t);
                     v->completed_total += 1;
                 }
             }
@@ -921,6 +970,8 @@ void srv_destroy(g3l_server *v)
     }
     v->cv_work.notify_all();
     if (v->th.joinable()) v->th.join();
+    for (auto &kv : v->reqs)
+        if (kv.second.range) nvtxRangeEnd(kv.second.range);
     cudaSetDevice(v->c->device);
     if (v->s) cudaStreamSynchronize(v->s);
     if (v->graph_ok) {
@@ -1027,6 +1078,11 @@ int srv_submit(g3l_server *v, const g3l_integral *items, int n, int64_t *ticket)
     }
     q.t_submit = now_s();
     const int64_t t = v->next_ticket++;
+    {
+        char nm[40];
+        std::snprintf(nm, sizeof nm, "request %lld", (long long)t);
+        q.range = nvtxRangeStartA(nm);
+    }
     v->reqs.emplace(t, std::move(q));
     v->pending.push_back(t);
     *ticket = t;
@@ -1164,6 +1220,9 @@ try {
     G3L_CK(cudaEventCreate(&c->ev1));
     for (auto &e : c->tev) G3L_CK(cudaEventCreate(&e));
     G3L_CK(cudaMallocHost(&c->h_pinned, 64));
+    G3L_CK(cudaHostAlloc((void **)&c->cancel_h, 64, cudaHostAllocMapped));
+    *c->cancel_h = 0;
+    G3L_CK(cudaHostGetDevicePointer((void **)&c->cancel_d, c->cancel_h, 0));
     c->B = host::Binning{t->Nz, t->Nm, t->Nk, t->zmin, t->zmax, t->mmin, t->mmax, t->kmin, t->kmax};
     c->Om = t->Om;
     c->OL = t->OL;
@@ -1297,6 +1356,7 @@ void g3l_ctx_destroy(g3l_ctx *c)
         if (p) cudaFree(p);
     for (void *p : c->allocs) cudaFree(p);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    if (c->cancel_h) cudaFreeHost(c->cancel_h);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (auto &e : c->tev)
@@ -1429,6 +1489,7 @@ int g3l_set_options(g3l_ctx *c, const g3l_options *o)
 {
     if (!c || !o || o->max_rounds < 1 || o->unlimited_pool < 16 || !(o->small_arg >= 0) ||
         !(o->unc_eps_rel > 0) || !(o->unc_eps_val >= 0) || !(o->unc_eps_sel >= 0) ||
+        !(o->deadline_ms >= 0) || !std::isfinite(o->deadline_ms) ||
         std::any_of(o->evalmx_variant, o->evalmx_variant + NGROUPS,
                     [](int v) { return v < 0 || v > 2; })) {
         host::set_error("g3l_set_options: invalid option value");
@@ -1544,6 +1605,17 @@ try {
     return G3L_ERR_NOMEM;
 }
 
+int g3l_eval_cancel(g3l_ctx *c)
+{
+    if (!c) {
+        host::set_error("g3l_eval_cancel: invalid context");
+        return G3L_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(c->run_mu);
+    if (c->running) __atomic_store_n(c->cancel_h, 1, __ATOMIC_SEQ_CST);
+    return G3L_OK;
+}
+
 int g3l_get_stats(g3l_ctx *c, g3l_stats *s)
 {
     if (!c || !s) return G3L_ERR_INVALID;
@@ -1571,6 +1643,8 @@ try {
         }
     }
     G3L_CK(cudaSetDevice(c->device));
+    NvtxScope nv("g3l_eval");
+    RunGuard run(c);
     // order by group
     std::vector<int> order(n);
     for (int i = 0; i < n; ++i) order[i] = i;
@@ -1612,6 +1686,7 @@ try {
     if (st) return st;
     Workspace &W = c->W;
     set_esc_queues(D.data(), n, H);
+    set_stop_fields(c, H);
     H.dbg = nullptr;
     // stage through pinned host memory: descriptors + header in, states + header out
     const size_t in_bytes = sizeof(IntDesc) * n + sizeof(BatchHdr);
@@ -2113,6 +2188,7 @@ int eval_static_locked(g3l_ctx *c, const g3l_integral *items, int n, int precisi
     H.max_rounds = c->opt.max_rounds;
     H.mixed = precision == G3L_MIXED ? 1 : 0;
     set_esc_queues(G.desc, n, H);
+    set_stop_fields(c, H);
     H.dbg = nullptr;
 
     KernelArgs a{};
@@ -2266,6 +2342,8 @@ try {
     if (st) return st;
     StaticStage &G = g_st[c->device];
     std::lock_guard<std::mutex> lk(G.mu);
+    NvtxScope nv("g3l_eval_static");
+    RunGuard run(c);
     st = eval_static_locked(c, items, n, precision, out, G, base);
     // A call that failed part-way may have kernels still queued: let them finish before
     // the next call on this device reuses the scratch.

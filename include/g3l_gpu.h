@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define G3L_ABI_VERSION 1
+#define G3L_ABI_VERSION 2  /* 2: g3l_options.deadline_ms, g3l_eval_cancel, G3L_ERR_DEADLINE */
 
 enum g3l_status {
     G3L_OK = 0,
@@ -38,10 +38,11 @@ enum g3l_status {
     G3L_ERR_NOMEM = 3,      /* device or host allocation failed */
     G3L_ERR_POOL = 4,       /* region pool exhausted (maxEval == 0 beyond the pool cap) */
     G3L_ERR_NONFINITE = 5,  /* an integral's running value or error became NaN/Inf */
-    G3L_ERR_CANCELLED = 6,  /* the call was cancelled through g3l_cancel */
+    G3L_ERR_CANCELLED = 6,  /* cancelled (g3l_eval_cancel, g3l_cancel, g3l_server_cancel) */
     G3L_ERR_ROUNDS = 7,     /* refinement-round cap reached */
     G3L_ERR_NO_DEVICE = 8,  /* no usable CUDA device */
-    G3L_ERR_BUSY = 9        /* serving queue full */
+    G3L_ERR_BUSY = 9,       /* serving queue full */
+    G3L_ERR_DEADLINE = 10   /* the call's deadline (g3l_options.deadline_ms) passed */
 };
 
 enum g3l_kind { G3L_NNMAP = 0, G3L_NMAPMAP = 1 };
@@ -123,6 +124,16 @@ int g3l_get_densities(g3l_ctx *ctx, int slot, double *rho_bar, double *n_bar);
  * (src/NNMap_Model.cu:382-415).  Returns the first non-OK item status, or OK. */
 int g3l_eval(g3l_ctx *ctx, const g3l_integral *items, int n, int precision,
              g3l_result *out);
+/* Stop the g3l_eval (or g3l_eval_terms, g3l_eval_static) call that is running on the
+ * context, from any other thread.  The device loop reads the request once per
+ * refinement round: every unfinished integral ends at the next round's selection with
+ * status G3L_ERR_CANCELLED and the value and error of its regions so far; integrals that
+ * had already finished keep their results and G3L_OK.  The call returns
+ * G3L_ERR_CANCELLED, and the context stays usable.  With no call running this does
+ * nothing (a call starts uncancelled).  The reference has no counterpart: its term
+ * methods run to completion or exit (src/cuda_helpers.h:11-19). */
+int g3l_eval_cancel(g3l_ctx *ctx);
+
 /* g3l_eval in the per-term methods' shape: the terms in term_mask (bit t-1 = term t) of
  * one kind for n aperture triplets (triplets[3*i + k], radians) and one HOD slot pair,
  * all in one launch.  val, err and result: [n*3], entry 3*i + t-1, before and after the
@@ -216,6 +227,12 @@ typedef struct g3l_options {
      * (kind * 3 + term - 1): 0, 1, 2 = 4, 6, 8 blocks per SM (128, 80, 64 registers
      * per thread).  Set by g3l_autotune; default 1 for the 1-halo terms, 2 for the others. */
     int evalmx_variant[6];
+    /* Deadline of a g3l_eval / g3l_eval_terms / g3l_eval_static call in milliseconds,
+     * measured on the device from the start of its refinement loop (0 = none, the
+     * default).  When it passes, every unfinished integral ends at the next round's
+     * selection with status G3L_ERR_DEADLINE and its value so far, as with
+     * g3l_eval_cancel. */
+    double deadline_ms;
 } g3l_options;
 int g3l_get_options(g3l_ctx *ctx, g3l_options *opt);
 int g3l_set_options(g3l_ctx *ctx, const g3l_options *opt);
