@@ -275,8 +275,7 @@ def sweep_leg(G, ctx, trip, hods, n_hod, max_eval, n_parity):
     from g3lhalo_gb300 import workloads as W
     hs = hods[:n_hod] if n_hod <= len(hods) else W.hod_sweep(n_hod, seed=12345)
     t0 = time.perf_counter()
-    for k, h in enumerate(hs):
-        ctx.set_hod(16 + k, h)
+    ctx.set_hods(16 + np.arange(n_hod), hs)  # n_bar of every vector in one device launch
     t_hod = time.perf_counter() - t0
     specs = [(G.NNMAP, t, 16 + k, 16 + k, tuple(th), RTOL, max_eval)
              for k in range(n_hod) for th in trip for t in (1, 2, 3)]

@@ -126,6 +126,7 @@ def lib():
             L.g3l_ctx_create.argtypes = [C.POINTER(Tables), C.c_int, C.POINTER(C.c_void_p)]
             L.g3l_ctx_destroy.argtypes = [C.c_void_p]
             L.g3l_set_hod.argtypes = [C.c_void_p, C.c_int, _dp]
+            L.g3l_set_hods.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp]
             L.g3l_set_correlation.argtypes = [C.c_void_p, C.c_double, C.c_double]
             L.g3l_set_scaling.argtypes = [C.c_void_p, C.c_int, _dp]
             L.g3l_get_densities.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
@@ -300,6 +301,13 @@ class Context:
     def set_hod(self, slot, params):
         p = np.ascontiguousarray(params, dtype=np.float64)
         _check(lib().g3l_set_hod(self.h, slot, _ptr(p)))
+
+    def set_hods(self, slots, params):
+        """set_hod for many slots at once: their n_bar integrals run in one device launch."""
+        sl = np.ascontiguousarray(slots, dtype=np.int32)
+        p = np.ascontiguousarray(params, dtype=np.float64).reshape(len(sl), 6)
+        _check(lib().g3l_set_hods(self.h, len(sl), sl.ctypes.data_as(C.POINTER(C.c_int)),
+                                  _ptr(p)))
 
     def set_correlation(self, A, eps):
         _check(lib().g3l_set_correlation(self.h, A, eps))

@@ -110,6 +110,7 @@ struct g3l_ctx {
     double Om = 0, OL = 0, Ob = 0, s8 = 0, H0 = 0, ns = 0;
     std::vector<double> hmf_h, rho_h;
     std::vector<double> hod_h, nbar_h;
+    std::vector<float> fnbar_h, fhodp_h;  // host copies of the mixed path's per-slot tables
     std::vector<char> hod_set;
     double A = 0, eps = 0;
     DevTables T{};
@@ -141,6 +142,7 @@ struct g3l_ctx {
     int *cancel_h = nullptr, *cancel_d = nullptr;
     std::mutex run_mu;
     bool running = false;
+    host::NbarDevice nbw;  // device buffers of the n_bar integrals (g3l_set_hod)
 };
 
 namespace {
@@ -1235,6 +1237,8 @@ try {
     host::rho_bar(c->B, t->Om, t->OL, t->H0, c->rho_h.data());
     c->hod_h.assign((size_t)MAX_HOD_SLOTS * 6, 0.0);
     c->nbar_h.assign((size_t)MAX_HOD_SLOTS * Nz, 0.0);
+    c->fnbar_h.assign((size_t)MAX_HOD_SLOTS * Nz, 0.f);
+    c->fhodp_h.assign((size_t)MAX_HOD_SLOTS * 8, 0.f);
     c->hod_set.assign(MAX_HOD_SLOTS, 0);
     c->opt.eval_blocks_per_sm = 0;
     c->opt.eval_warps_per_block = 0;
@@ -1357,6 +1361,7 @@ void g3l_ctx_destroy(g3l_ctx *c)
     for (void *p : c->allocs) cudaFree(p);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     if (c->cancel_h) cudaFreeHost(c->cancel_h);
+    host::free_nbar_device(c->nbw);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (auto &e : c->tev)
@@ -1366,56 +1371,117 @@ void g3l_ctx_destroy(g3l_ctx *c)
     delete c;
 }
 
-int g3l_set_hod(g3l_ctx *c, int slot, const double params[6])
-try {
-    if (!c || !params || slot < 0 || slot >= MAX_HOD_SLOTS) {
-        host::set_error("g3l_set_hod: invalid arguments");
-        return G3L_ERR_INVALID;
-    }
+}  // extern "C"
+
+namespace {
+
+bool hod_ok(const double *params, std::string &why)
+{
     for (int k = 0; k < 6; ++k)
         if (!std::isfinite(params[k])) {
-            host::set_error("g3l_set_hod: non-finite HOD parameter");
-            return G3L_ERR_INVALID;
+            why = "non-finite HOD parameter";
+            return false;
         }
     if (!(params[2] > 0) || !(params[3] != 0) || !(params[4] > 0)) {
-        host::set_error("g3l_set_hod: Mth, M' must be > 0 and sigma != 0");
-        return G3L_ERR_INVALID;
+        why = "Mth, M' must be > 0 and sigma != 0";
+        return false;
     }
+    return true;
+}
+
+// A slot's HOD vector and its n_bar(z): the FP64 tables and the mixed path's scaled FP32
+// n_bar and occupation constants, copied on the context's stream (not synchronised).
+int store_hod(g3l_ctx *c, int slot, const double params[6], const double *nb)
+{
     const int Nz = c->B.Nz;
-    std::vector<double> nb(Nz);
-    if (host::n_bar(c->B, c->hmf_h.data(), params, nb.data())) {
-        host::set_error("g3l_set_hod: n_bar integration failed");
-        return G3L_ERR_INVALID;
-    }
     std::copy(params, params + 6, c->hod_h.begin() + 6 * slot);
-    std::copy(nb.begin(), nb.end(), c->nbar_h.begin() + (size_t)Nz * slot);
+    std::copy(nb, nb + Nz, c->nbar_h.begin() + (size_t)Nz * slot);
     c->hod_set[slot] = 1;
-    G3L_CK(cudaSetDevice(c->device));
-    G3L_CK(cudaMemcpyAsync(c->d_hod + 6 * slot, params, 6 * sizeof(double), cudaMemcpyHostToDevice,
-                           c->stream));
+    G3L_CK(cudaMemcpyAsync(c->d_hod + 6 * slot, c->hod_h.data() + 6 * slot, 6 * sizeof(double),
+                           cudaMemcpyHostToDevice, c->stream));
     G3L_CK(cudaMemcpyAsync(c->d_nbar + (size_t)Nz * slot, c->nbar_h.data() + (size_t)Nz * slot,
                            Nz * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     // mixed path: n_bar scaled to max 1 and the occupation constants in FP32
     double mx = 0;
-    for (double v : nb) mx = std::max(mx, std::fabs(v));
+    for (int i = 0; i < Nz; ++i) mx = std::max(mx, std::fabs(nb[i]));
     c->sn[slot] = mx > 0 ? 1 / mx : 1;
-    std::vector<float> fnb(Nz);
+    float *fnb = c->fnbar_h.data() + (size_t)Nz * slot;
     for (int i = 0; i < Nz; ++i) fnb[i] = (float)(nb[i] * c->sn[slot]);
     const float2 lmth = dsplit(std::log10(params[2])), lmp = dsplit(std::log10(params[4]));
-    float hp[8] = {(float)params[0], (float)params[1], lmth.x, lmth.y,
-                   (float)(std::log(10.0) / (params[3] * 1.414213562)), lmp.x, lmp.y,
-                   (float)params[5]};
-    G3L_CK(cudaMemcpyAsync(c->d_fnbar + (size_t)Nz * slot, fnb.data(), Nz * sizeof(float),
+    float *hp = c->fhodp_h.data() + 8 * slot;
+    const float h8[8] = {(float)params[0], (float)params[1], lmth.x, lmth.y,
+                         (float)(std::log(10.0) / (params[3] * 1.414213562)), lmp.x, lmp.y,
+                         (float)params[5]};
+    std::copy(h8, h8 + 8, hp);
+    G3L_CK(cudaMemcpyAsync(c->d_fnbar + (size_t)Nz * slot, fnb, Nz * sizeof(float),
                            cudaMemcpyHostToDevice, c->stream));
-    G3L_CK(cudaMemcpyAsync(c->d_fhodp + 8 * slot, hp, sizeof hp, cudaMemcpyHostToDevice,
+    G3L_CK(cudaMemcpyAsync(c->d_fhodp + 8 * slot, hp, 8 * sizeof(float), cudaMemcpyHostToDevice,
                            c->stream));
+    return G3L_OK;
+}
+
+// n_bar of n HOD vectors on the device, stored in their slots; one synchronisation
+int set_hods_impl(g3l_ctx *c, int n, const int *slots, const double *params, const char *who)
+{
+    for (int k = 0; k < n; ++k) {
+        std::string why;
+        if (slots[k] < 0 || slots[k] >= MAX_HOD_SLOTS) {
+            host::set_error(std::string(who) + ": slot out of range");
+            return G3L_ERR_INVALID;
+        }
+        if (!hod_ok(params + 6 * k, why)) {
+            host::set_error(std::string(who) + ": " + why);
+            return G3L_ERR_INVALID;
+        }
+    }
+    G3L_CK(cudaSetDevice(c->device));
+    NvtxScope nv("n_bar");
+    const int Nz = c->B.Nz;
+    std::vector<double> nb((size_t)n * Nz);
+    int st = host::n_bar_device(c->nbw, c->B, c->T.hmf, params, n, (void *)c->stream, c->nsm,
+                                nb.data());
+    if (st) return st;
+    // the host copies must not be overwritten while an earlier slot's copy is in flight
+    for (int k = 0; k < n; ++k) {
+        st = store_hod(c, slots[k], params + 6 * k, nb.data() + (size_t)Nz * k);
+        if (st) return st;
+    }
     G3L_CK(cudaStreamSynchronize(c->stream));
     return G3L_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int g3l_set_hod(g3l_ctx *c, int slot, const double params[6])
+try {
+    if (!c || !params) {
+        host::set_error("g3l_set_hod: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    return set_hods_impl(c, 1, &slot, params, "g3l_set_hod");
 } catch (const std::bad_alloc &) {
     host::set_error("g3l_set_hod: host allocation failed");
     return G3L_ERR_NOMEM;
 } catch (const std::exception &e) {
     host::set_error(std::string("g3l_set_hod: ") + e.what());
+    return G3L_ERR_INVALID;
+}
+
+int g3l_set_hods(g3l_ctx *c, int n, const int *slots, const double *params)
+try {
+    if (!c || n < 0 || (n > 0 && (!slots || !params))) {
+        host::set_error("g3l_set_hods: invalid arguments");
+        return G3L_ERR_INVALID;
+    }
+    if (n == 0) return G3L_OK;
+    return set_hods_impl(c, n, slots, params, "g3l_set_hods");
+} catch (const std::bad_alloc &) {
+    host::set_error("g3l_set_hods: host allocation failed");
+    return G3L_ERR_NOMEM;
+} catch (const std::exception &e) {
+    host::set_error(std::string("g3l_set_hods: ") + e.what());
     return G3L_ERR_INVALID;
 }
 

@@ -30,6 +30,17 @@ struct Binning {
 void rho_bar(const Binning &B, double Om, double OL, double H0, double *out);
 // n_bar(z_i) for one HOD (src/NNMap_Model.cu:244-297, src/generalFunctions.cu:149-245)
 int n_bar(const Binning &B, const double *hmf, const double hod[6], double *out);
+// n_bar(z_i) on the device (precompute.cu): device buffers a context keeps between calls
+struct NbarDevice {
+    void *tasks = nullptr, *out = nullptr, *idx = nullptr, *cache = nullptr;
+    double *hods = nullptr;
+    size_t ntask_cap = 0, nhod_cap = 0, cache_entries = 0;
+};
+void free_nbar_device(NbarDevice &W);
+// n_bar(z_i) of nh HOD vectors (hods: [nh][6] on the host) on the current device from its
+// FP64 mass function d_hmf [Nz][Nm]; out: [nh][Nz] on the host.  stream: a cudaStream_t.
+int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const double *hods,
+                 int nh, void *stream, int nsm, double *out);
 // the reference's prefactor chain applied to a raw integral
 double apply_prefactor(int kind, int term, double H0, double Om, double raw);
 

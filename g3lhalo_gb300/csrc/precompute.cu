@@ -24,6 +24,7 @@
 // device libm's last-ulp differences in sin, cos, exp, log and pow.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdlib>
@@ -285,96 +286,278 @@ __device__ void heap_pop(Heap H, int &nn, double &hv, double &he, double &c, dou
     he -= e;
 }
 
-// One block per integral at a time.  Status: 0 ok, G3L_ERR_POOL (more than CAP live
-// regions), G3L_ERR_ROUNDS (more than PC_MAX_ROUNDS rounds).  idx: the integrals to run
-// (null: all ntask).
+// One adaptive 15-point Gauss-Kronrod integral over [lo, hi] by the whole block, with
+// the reference's refinement: thread 0 keeps the heap, the Gladwell batch and the cut;
+// ev(nb, bc, bh, bv, be) is called by every thread and evaluates the batch's regions
+// (centres bc, half-widths bh) into their values bv and errors be.  Status: 0 ok,
+// G3L_ERR_POOL (more than CAP live regions), G3L_ERR_ROUNDS (more than PC_MAX_ROUNDS
+// rounds).  The result is valid in thread 0; the block is synchronised on return.
+template <int CAP, class Eval>
+__device__ PcOut gk_integrate(double lo, double hi, double *sm, const Eval &ev)
+{
+    constexpr int PC_CAP = CAP, PC_BATCH = 2 * CAP;
+    Heap H{sm, sm + PC_CAP, sm + 2 * PC_CAP, sm + 3 * PC_CAP};
+    double *bc = sm + 4 * PC_CAP, *bh = bc + PC_BATCH, *bv = bh + PC_BATCH, *be = bv + PC_BATCH;
+    __shared__ int s_nb, s_done;
+    // thread 0's state: heap size, running sums, counters
+    int n = 0, status = 0, rounds = 0;
+    double hv = 0, he = 0;
+    unsigned long long neval = 15;
+    if (threadIdx.x == 0) {
+        bc[0] = 0.5 * (lo + hi);
+        bh[0] = 0.5 * (hi - lo);
+        s_nb = 1;
+        s_done = 0;
+    }
+    __syncthreads();
+    while (true) {
+        ev(s_nb, bc, bh, bv, be);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int nb = s_nb;
+            for (int b = 0; b < nb; ++b) heap_push(H, n, hv, he, bc[b], bh[b], bv[b], be[b]);
+            int nbn = 0;
+            if (converged(he, hv)) {
+                s_done = 1;
+            } else if (++rounds > PC_MAX_ROUNDS) {
+                status = G3L_ERR_ROUNDS;
+                s_done = 1;
+            } else {
+                // Gladwell batch: pop until the error left is within tolerance
+                double eErr = he;
+                const double eVal = hv;
+                do {
+                    // after this pop and the pushes the heap holds n + nbn + 1 regions
+                    if (n + nbn + 1 > PC_CAP) {
+                        status = G3L_ERR_POOL;
+                        s_done = 1;
+                        break;
+                    }
+                    double c, hw, v, e;
+                    heap_pop(H, n, hv, he, c, hw, v, e);
+                    eErr -= e;
+                    const double h2 = hw * 0.5;  // cut (src/hcubature.cpp:206-218)
+                    bc[nbn] = c - h2;
+                    bh[nbn] = h2;
+                    bc[nbn + 1] = c + h2;
+                    bh[nbn + 1] = h2;
+                    nbn += 2;
+                    neval += 30;
+                    if (converged(eErr, eVal)) break;
+                } while (n > 0);
+            }
+            s_nb = nbn;
+        }
+        __syncthreads();
+        if (s_done) break;
+    }
+    PcOut o{0, 0, neval, status, rounds};
+    if (threadIdx.x == 0) {
+        double v = 0, e = 0;
+        for (int i = 0; i < n; ++i) {
+            v += H.val[i];
+            e += H.err[i];
+        }
+        o.val = v;
+        o.err = e;
+    }
+    __syncthreads();
+    return o;
+}
+
+// The batch of one precompute integral: one region per half-warp, one point per lane.
+struct PcEval {
+    const PkDev &P;
+    const PcTask &t;
+    __device__ void operator()(int nb, const double *bc, const double *bh, double *bv,
+                               double *be) const
+    {
+        const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+        const int warp = threadIdx.x >> 5, nwarps = blockDim.x / 32;
+        for (int r0 = 2 * warp; r0 < nb; r0 += 2 * nwarps) {
+            const int r = r0 + half;
+            double f = 0;
+            if (r < nb && hl < 15) f = integrand(P, t, gk_point(bc[r], bh[r], hl));
+            double vk[15];
+#pragma unroll
+            for (int k = 0; k < 15; ++k) vk[k] = __shfl_sync(0xffffffffu, f, k, 16);
+            if (r < nb && hl == 0) rule_gk15(vk, bh[r], bv[r], be[r]);
+        }
+    }
+};
+
+// One block per integral at a time (grid-stride).  idx: the integrals to run (null:
+// all ntask).
 template <int CAP>
 __global__ void __launch_bounds__(PC_THREADS) k_pc_integrate(const PkDev *__restrict__ Pp,
                                                              const PcTask *__restrict__ tasks,
                                                              const int *__restrict__ idx,
                                                              int ntask, PcOut *__restrict__ out)
 {
-    constexpr int PC_CAP = CAP, PC_BATCH = 2 * CAP;
     extern __shared__ double sm[];
-    Heap H{sm, sm + PC_CAP, sm + 2 * PC_CAP, sm + 3 * PC_CAP};
-    double *bc = sm + 4 * PC_CAP, *bh = bc + PC_BATCH, *bv = bh + PC_BATCH, *be = bv + PC_BATCH;
-    __shared__ int s_nb, s_done;
     const PkDev P = *Pp;
-    const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
-    const int warp = threadIdx.x >> 5, nwarps = PC_THREADS / 32;
     for (int tj = blockIdx.x; tj < ntask; tj += gridDim.x) {
         const int ti = idx ? idx[tj] : tj;
         const PcTask t = tasks[ti];
-        // thread 0's state: heap size, running sums, counters
-        int n = 0, status = 0, rounds = 0;
-        double hv = 0, he = 0;
-        unsigned long long neval = 15;
-        if (threadIdx.x == 0) {
-            bc[0] = 0.5 * (t.lo + t.hi);
-            bh[0] = 0.5 * (t.hi - t.lo);
-            s_nb = 1;
-            s_done = 0;
-        }
-        __syncthreads();
-        while (true) {
-            // evaluate the batch: one region per half-warp, one point per lane
-            const int nb = s_nb;
-            for (int r0 = 2 * warp; r0 < nb; r0 += 2 * nwarps) {
-                const int r = r0 + half;
-                double f = 0;
-                if (r < nb && hl < 15) f = integrand(P, t, gk_point(bc[r], bh[r], hl));
-                double vk[15];
-#pragma unroll
-                for (int k = 0; k < 15; ++k) vk[k] = __shfl_sync(0xffffffffu, f, k, 16);
-                if (r < nb && hl == 0) rule_gk15(vk, bh[r], bv[r], be[r]);
+        const PcOut o = gk_integrate<CAP>(t.lo, t.hi, sm, PcEval{P, t});
+        if (threadIdx.x == 0) out[ti] = o;
+    }
+}
+
+// ------------------------------------------------------------------ n_bar(z) per HOD
+// The galaxy number density of each HOD vector at every z bin, the reference's
+// updateDensities (src/NNMap_Model.cu:244-297): n_bar(z) = ln10 * integral over
+// log10 m of m n(m, z) (N_c + N_s) with the nearest mass bin of the FP64 mass function,
+// each z bin one adaptive Gauss-Kronrod integral at rtol 1e-4
+// (src/generalFunctions.cu:149-245, src/hcubature.cpp:620-765).
+//
+// The mass factors (m, N_c + N_s, mass bin) do not depend on z, and every z bin bisects
+// the same interval, so most 15-point blocks recur across the z bins of one HOD vector
+// (a 64 x 128 table set evaluates ~1.5M points per vector at ~30k distinct abscissae).
+// A block's factors are kept in a device hash table keyed by the region (centre and
+// half-width bits) and the HOD vector: the first half-warp to claim a key computes and
+// publishes them, later ones read them; a half-warp that meets a key being filled
+// computes its block itself (no waiting).  Every value is computed by the same
+// expression either way, so the result does not depend on who computed it.
+struct NbarTask {
+    double lo, hi;
+    int z_ix, hod;
+};
+
+struct NbarArgs {
+    const double *hmf;   // FP64 mass function [Nz][Nm]
+    const double *hods;  // [hod][6] f, alpha, Mth, sigma, M', beta
+    int Nm;
+    double mmin, ln_mratio;  // mass bin = round(log(m / mmin) Nm / ln_mratio)
+    // block-factor table: state (0 empty, 1 being filled, 2 published), key, factors
+    unsigned *st;
+    unsigned long long *kc, *kh;
+    int *kg;
+    double *fm, *fS;
+    int *fmix;
+    unsigned mask;  // entries - 1 (a power of two)
+};
+
+constexpr size_t kNbarEntryBytes = 4 + 8 + 8 + 4 + 15 * (8 + 8 + 4);
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// N_c + N_s (src/HOD.cu:35-76; erf taken once, the same argument in both) and the
+// nearest mass bin (src/NNMap_Model.cu:556) at x = log10 m
+__device__ __forceinline__ void nbar_factors(const NbarArgs &A, const double *h, double x,
+                                             double &m, double &S, int &mix)
+{
+    m = pow(10.0, x);
+    const double e = erf(log(m / h[2]) / h[3] / 1.414213562);
+    const double Nc = 0.5 * h[1] * (1 + e);
+    const double Ns = 0.5 * (1 + e) * pow(m / h[4], h[5]);
+    S = Nc + Ns;
+    mix = (int)round(log(m / A.mmin) * A.Nm / A.ln_mratio);
+    mix = min(max(mix, 0), A.Nm - 1);  // in range for every abscissa of the interval
+}
+
+// Find the region's block in the table (lane 0 of a half-warp).  mode 0: published,
+// read it at `slot`; 1: claimed, fill `slot`; 2: compute only.
+__device__ void nbar_probe(const NbarArgs &A, double c, double hw, int hod, int &mode, int &slot)
+{
+    const unsigned long long kc = (unsigned long long)__double_as_longlong(c);
+    const unsigned long long kh = (unsigned long long)__double_as_longlong(hw);
+    unsigned long long x = kc * 0x9E3779B97F4A7C15ull;
+    x ^= (kh + 0x632BE59BD9B4E019ull) * 0xC2B2AE3D27D4EB4Full;
+    x ^= (unsigned long long)(hod + 1) * 0x165667B19E3779F9ull;
+    x ^= x >> 29;
+    unsigned idx = (unsigned)x & A.mask;
+    mode = 2;
+    slot = 0;
+    for (int probe = 0; probe < 16; ++probe, idx = (idx + 1) & A.mask) {
+        unsigned s = ld_acquire_u32(A.st + idx);
+        if (s == 0) {
+            s = atomicCAS(A.st + idx, 0u, 1u);
+            if (s == 0) {
+                A.kc[idx] = kc;
+                A.kh[idx] = kh;
+                A.kg[idx] = hod;
+                mode = 1;
+                slot = (int)idx;
+                return;
             }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                for (int b = 0; b < nb; ++b) heap_push(H, n, hv, he, bc[b], bh[b], bv[b], be[b]);
-                int nbn = 0;
-                if (converged(he, hv)) {
-                    s_done = 1;
-                } else if (++rounds > PC_MAX_ROUNDS) {
-                    status = G3L_ERR_ROUNDS;
-                    s_done = 1;
+            if (s == 2) s = ld_acquire_u32(A.st + idx);
+        }
+        if (s == 1) return;  // being filled: compute this block here
+        if (__ldcg(A.kc + idx) == kc && __ldcg(A.kh + idx) == kh && __ldcg(A.kg + idx) == hod) {
+            mode = 0;
+            slot = (int)idx;
+            return;
+        }
+    }
+}
+
+// The batch of one n_bar integral: one region per half-warp, one point per lane.
+struct NbarEval {
+    const NbarArgs &A;
+    const NbarTask &t;
+    __device__ void operator()(int nb, const double *bc, const double *bh, double *bv,
+                               double *be) const
+    {
+        const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+        const int warp = threadIdx.x >> 5, nwarps = blockDim.x / 32;
+        const double *h = A.hods + 6 * t.hod;
+        const double *row = A.hmf + (size_t)t.z_ix * A.Nm;
+        for (int r0 = 2 * warp; r0 < nb; r0 += 2 * nwarps) {
+            const int r = r0 + half;
+            const bool live = r < nb;
+            const double c = live ? bc[r] : 0.0, hw = live ? bh[r] : 0.0;
+            int mode = 2, slot = 0;
+            if (live && hl == 0) nbar_probe(A, c, hw, t.hod, mode, slot);
+            __syncwarp();  // orders lane 0's acquire before the other lanes' reads
+            mode = __shfl_sync(0xffffffffu, mode, 0, 16);
+            slot = __shfl_sync(0xffffffffu, slot, 0, 16);
+            double f = 0;
+            if (live && hl < 15) {
+                double m, S;
+                int mix;
+                const size_t k = (size_t)slot * 15 + hl;
+                if (mode == 0) {
+                    m = __ldcg(A.fm + k);
+                    S = __ldcg(A.fS + k);
+                    mix = __ldcg(A.fmix + k);
                 } else {
-                    // Gladwell batch: pop until the error left is within tolerance
-                    double eErr = he;
-                    const double eVal = hv;
-                    do {
-                        // after this pop and the pushes the heap holds n + nbn + 1 regions
-                        if (n + nbn + 1 > PC_CAP) {
-                            status = G3L_ERR_POOL;
-                            s_done = 1;
-                            break;
-                        }
-                        double c, hw, v, e;
-                        heap_pop(H, n, hv, he, c, hw, v, e);
-                        eErr -= e;
-                        const double h2 = hw * 0.5;  // cut (src/hcubature.cpp:206-218)
-                        bc[nbn] = c - h2;
-                        bh[nbn] = h2;
-                        bc[nbn + 1] = c + h2;
-                        bh[nbn + 1] = h2;
-                        nbn += 2;
-                        neval += 30;
-                        if (converged(eErr, eVal)) break;
-                    } while (n > 0);
+                    nbar_factors(A, h, gk_point(c, hw, hl), m, S, mix);
+                    if (mode == 1) {
+                        A.fm[k] = m;
+                        A.fS[k] = S;
+                        A.fmix[k] = mix;
+                    }
                 }
-                s_nb = nbn;
+                f = m * row[mix] * S;  // src/generalFunctions.cu:233-245
             }
-            __syncthreads();
-            if (s_done) break;
+            if (mode == 1) __threadfence();
+            __syncwarp();
+            if (live && hl == 0 && mode == 1) atomicExch(A.st + slot, 2u);  // publish
+            double vk[15];
+#pragma unroll
+            for (int q = 0; q < 15; ++q) vk[q] = __shfl_sync(0xffffffffu, f, q, 16);
+            if (live && hl == 0) rule_gk15(vk, hw, bv[r], be[r]);
         }
-        if (threadIdx.x == 0) {
-            double v = 0, e = 0;
-            for (int i = 0; i < n; ++i) {
-                v += H.val[i];
-                e += H.err[i];
-            }
-            out[ti] = PcOut{v, e, neval, status, rounds};
-        }
-        __syncthreads();
+    }
+};
+
+template <int CAP>
+__global__ void __launch_bounds__(PC_THREADS) k_nbar(NbarArgs A, const NbarTask *__restrict__ tasks,
+                                                     const int *__restrict__ idx, int ntask,
+                                                     PcOut *__restrict__ out)
+{
+    extern __shared__ double sm[];
+    for (int tj = blockIdx.x; tj < ntask; tj += gridDim.x) {
+        const int ti = idx ? idx[tj] : tj;
+        const NbarTask t = tasks[ti];
+        const PcOut o = gk_integrate<CAP>(t.lo, t.hi, sm, NbarEval{A, t});
+        if (threadIdx.x == 0) out[ti] = o;
     }
 }
 
@@ -570,6 +753,125 @@ int run_tasks(const PkDev *dP, const std::vector<PcTask> &tasks, std::vector<PcO
 }
 
 }  // namespace
+
+namespace host {
+
+void free_nbar_device(NbarDevice &W)
+{
+    for (void *p : {W.tasks, W.out, W.idx, W.cache, (void *)W.hods})
+        if (p) cudaFree(p);
+    W = NbarDevice{};
+}
+
+namespace {
+constexpr int kNbarChunk = 256;          // HOD vectors per launch
+constexpr int kNbarCapSmall = 1024;      // live regions of the first pass
+}  // namespace
+
+int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const double *hods,
+                 int nh, void *stream, int nsm, double *out)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    const int Nz = B.Nz;
+    const double lo = std::log10(B.mmin), hi = std::log10(B.mmax_integral());
+    const double ln10 = std::log(10.0);
+    PC_CK(cudaFuncSetAttribute(k_nbar<kNbarCapSmall>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)pc_smem(kNbarCapSmall)));
+    PC_CK(cudaFuncSetAttribute(k_nbar<PC_CAP_LARGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)pc_smem(PC_CAP_LARGE)));
+    std::vector<NbarTask> tasks;
+    std::vector<PcOut> res;
+    std::vector<int> big;
+    for (int h0 = 0; h0 < nh; h0 += kNbarChunk) {
+        const int nk = std::min(kNbarChunk, nh - h0);
+        const int ntask = nk * Nz;
+        tasks.resize(ntask);
+        for (int k = 0; k < nk; ++k)
+            for (int i = 0; i < Nz; ++i) {
+                const double z = B.zmin + i * (B.zmax - B.zmin) / B.Nz;
+                const int z_ix = (int)std::round((z - B.zmin) * B.Nz / (B.zmax - B.zmin));
+                tasks[(size_t)k * Nz + i] = NbarTask{lo, hi, z_ix, k};
+            }
+        // ~2000 distinct blocks per vector: a table at most half full
+        size_t entries = 8192;
+        while (entries < (size_t)nk * 8192) entries <<= 1;
+        if ((size_t)ntask > W.ntask_cap) {
+            for (void **p : {&W.tasks, &W.out, &W.idx})
+                if (*p) cudaFree(*p), *p = nullptr;
+            W.ntask_cap = 0;
+            PC_CK(cudaMalloc(&W.tasks, sizeof(NbarTask) * ntask));
+            PC_CK(cudaMalloc(&W.out, sizeof(PcOut) * ntask));
+            PC_CK(cudaMalloc(&W.idx, sizeof(int) * ntask));
+            W.ntask_cap = (size_t)ntask;
+        }
+        if ((size_t)nk > W.nhod_cap) {
+            if (W.hods) cudaFree(W.hods);
+            W.hods = nullptr;
+            W.nhod_cap = 0;
+            PC_CK(cudaMalloc((void **)&W.hods, sizeof(double) * 6 * nk));
+            W.nhod_cap = (size_t)nk;
+        }
+        if (entries > W.cache_entries) {
+            if (W.cache) cudaFree(W.cache);
+            W.cache = nullptr;
+            W.cache_entries = 0;
+            PC_CK(cudaMalloc(&W.cache, entries * kNbarEntryBytes));
+            W.cache_entries = entries;
+        }
+        const size_t E = W.cache_entries;
+        char *cb = (char *)W.cache;
+        NbarArgs A{};
+        A.hmf = d_hmf;
+        A.hods = W.hods;
+        A.Nm = B.Nm;
+        A.mmin = B.mmin;
+        A.ln_mratio = std::log(B.mmax / B.mmin);
+        A.kc = (unsigned long long *)cb;
+        A.kh = A.kc + E;
+        A.fm = (double *)(A.kh + E);
+        A.fS = A.fm + 15 * E;
+        A.st = (unsigned *)(A.fS + 15 * E);
+        A.kg = (int *)(A.st + E);
+        A.fmix = A.kg + E;
+        A.mask = (unsigned)(E - 1);
+        PC_CK(cudaMemcpyAsync(W.tasks, tasks.data(), sizeof(NbarTask) * ntask,
+                              cudaMemcpyHostToDevice, s));
+        PC_CK(cudaMemcpyAsync(W.hods, hods + (size_t)6 * h0, sizeof(double) * 6 * nk,
+                              cudaMemcpyHostToDevice, s));
+        PC_CK(cudaMemsetAsync(A.st, 0, sizeof(unsigned) * E, s));
+        k_nbar<kNbarCapSmall><<<std::min(ntask, nsm * 2), PC_THREADS, pc_smem(kNbarCapSmall), s>>>(
+            A, (const NbarTask *)W.tasks, nullptr, ntask, (PcOut *)W.out);
+        PC_CK(cudaGetLastError());
+        res.resize(ntask);
+        PC_CK(cudaMemcpyAsync(res.data(), W.out, sizeof(PcOut) * ntask, cudaMemcpyDeviceToHost, s));
+        PC_CK(cudaStreamSynchronize(s));
+        big.clear();
+        for (int i = 0; i < ntask; ++i)
+            if (res[i].status == G3L_ERR_POOL) big.push_back(i);
+        if (!big.empty()) {  // the rest with the larger heap, from their root regions
+            const int nb = (int)big.size();
+            PC_CK(cudaMemcpyAsync(W.idx, big.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+            k_nbar<PC_CAP_LARGE><<<std::min(nb, nsm), PC_THREADS, pc_smem(PC_CAP_LARGE), s>>>(
+                A, (const NbarTask *)W.tasks, (const int *)W.idx, nb, (PcOut *)W.out);
+            PC_CK(cudaGetLastError());
+            PC_CK(cudaMemcpyAsync(res.data(), W.out, sizeof(PcOut) * ntask, cudaMemcpyDeviceToHost,
+                                  s));
+            PC_CK(cudaStreamSynchronize(s));
+        }
+        for (int i = 0; i < ntask; ++i) {
+            if (res[i].status) {
+                set_error(res[i].status == G3L_ERR_POOL
+                              ? "n_bar: an integral needed more than 2048 regions"
+                              : "n_bar: an integral exceeded 4096 rounds");
+                return res[i].status;
+            }
+            out[(size_t)h0 * Nz + i] = ln10 * res[i].val;
+        }
+    }
+    return G3L_OK;
+}
+
+}  // namespace host
 }  // namespace g3l
 
 using namespace g3l;

@@ -99,10 +99,14 @@ void g3l_ctx_destroy(g3l_ctx *ctx);
 
 /* Set HOD slot `slot` (0 <= slot < g3l_max_hod_slots()) to
  * params = {f, alpha, Mth, sigma, M', beta} (the reference's device order,
- * src/HOD.cu:15-20) and compute rho_bar(z) and n_bar(z) for it with the 1-D
- * adaptive Gauss-Kronrod integral of the reference (updateDensities,
- * src/NNMap_Model.cu:244-297). */
+ * src/HOD.cu:15-20) and compute n_bar(z) for it with the 1-D adaptive Gauss-Kronrod
+ * integral of the reference (updateDensities, src/NNMap_Model.cu:244-297), on the
+ * device: one integral per z bin, the reference's refinement, FP64. */
 int g3l_set_hod(g3l_ctx *ctx, int slot, const double params[6]);
+/* g3l_set_hod for n slots at once (slots[n], params[n][6]): the n_bar integrals of all
+ * of them run in one device launch (the reference updates one model's HODs at a time,
+ * src/NNMap_Model.cu:236-297). */
+int g3l_set_hods(g3l_ctx *ctx, int n, const int *slots, const double *params);
 int g3l_max_hod_slots(void);
 /* Satellite-pair correlation parameters A, epsilon (src/HOD.cu:90). */
 int g3l_set_correlation(g3l_ctx *ctx, double A, double epsilon);

@@ -30,9 +30,9 @@ def ctx():
     return c
 
 
-def _batch():
+def _batch(short_cap=20_000):
     trip = W.triplets_all()
-    short = [(G.NNMAP, t, 0, 1, tuple(trip[i]), 1e-4, 20_000) for i in (5, 60) for t in (1, 2, 3)]
+    short = [(G.NNMAP, t, 0, 1, tuple(trip[i]), 1e-4, short_cap) for i in (5, 60) for t in (1, 2, 3)]
     long_ = [(G.NNMAP, 2, 0, 1, tuple(trip[i]), 1e-12, LONG_CAP) for i in range(0, 220, 5)]
     return short, long_
 
@@ -79,9 +79,11 @@ def test_cancel_from_another_thread(ctx):
 
 @pytest.mark.parametrize("use_graph", [1, 0])
 def test_deadline(ctx, use_graph):
-    short, long_ = _batch()
+    # short integrals of a few rounds: they finish while the long ones' rounds are still
+    # cheap, well before the deadline (FP64 rounds of the long integrals double in cost)
+    short, long_ = _batch(short_cap=3_000)
     ref_short = ctx.eval(short, G.FP64)
-    ctx.set_options(use_graph=use_graph, deadline_ms=150.0)
+    ctx.set_options(use_graph=use_graph, deadline_ms=300.0)
     try:
         r, t = _timed(ctx, short + long_, G.FP64)
     finally:

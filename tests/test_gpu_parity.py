@@ -33,8 +33,9 @@ def _rel(a, b):
     return abs(a - b) / max(abs(b), 1e-300)
 
 
-def test_host_densities_match_reference(ctx, golden):
-    """rho_bar and n_bar as g3l_set_hod computes them (the host Gauss-Kronrod path)."""
+def test_set_hod_densities_match_reference(ctx, golden):
+    """n_bar as g3l_set_hod computes it on the device (one adaptive Gauss-Kronrod integral
+    per z bin) and rho_bar, against the reference build's."""
     rho, n1 = ctx.densities(0)
     _, n2 = ctx.densities(1)
     np.testing.assert_allclose(rho, golden["nn_rho_bar"], rtol=1e-15)
