@@ -565,12 +565,13 @@ def main():
                    "d2h_bytes_per_step": int(st_last["d2h_bytes"]),
                    "p50_ms": float(np.percentile(wall_ms, 50)),
                    "p99_ms": float(np.percentile(wall_ms, 99)),
-                   "includes": "HOD update (host n_bar integrals + upload), descriptor H2D, "
+                   "includes": "HOD update (device n_bar integrals, copies), descriptor H2D, "
                                "device loop, result D2H"},
            "gpu_launches": launches, "clocks": clk,
            "stats_last_step": {k: st_last[k] for k in ("rounds", "regions_evaluated",
                                                         "points_evaluated", "escalated",
                                                         "escalated_full", "deferred", "polished",
+                                                        "thr_checks",
                                                         "tie_fallbacks", "small_arg_fp64",
                                                         "group_points")}}
     if rank == 0:

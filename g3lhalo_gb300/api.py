@@ -91,7 +91,8 @@ class Options(C.Structure):
                 ("unc_tau_abs", C.c_double), ("unc_tau_impact", C.c_double),
                 ("unc_tau_sel", C.c_double), ("unc_tau_val", C.c_double),
                 ("unc_eps_val", C.c_double), ("unc_eps_sel", C.c_double),
-                ("evalmx_variant", C.c_int * 6), ("deadline_ms", C.c_double)]
+                ("evalmx_variant", C.c_int * 6), ("deadline_ms", C.c_double),
+                ("unc_thr", C.c_double), ("unc_tau_thr", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -103,7 +104,7 @@ class Stats(C.Structure):
                 ("group_ms", C.c_double * 6), ("group_points", C.c_uint64 * 6),
                 ("reeval_ms", C.c_double), ("select_ms", C.c_double),
                 ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
-                ("escalated_full", C.c_uint64)]
+                ("escalated_full", C.c_uint64), ("thr_checks", C.c_uint64)]
 
 
 INTEGRAND_V = C.CFUNCTYPE(C.c_int, C.c_uint, C.c_size_t, _dp, C.c_void_p, C.c_uint, _dp)

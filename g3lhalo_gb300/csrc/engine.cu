@@ -198,6 +198,42 @@ __device__ void radix_select(const double *err, const unsigned long long *q, lon
     __syncthreads();
 }
 
+// Mixed precision: queue for FP64 re-evaluation the regions of integral i with the
+// largest uncertainty keys (P.key, filled by the caller; U their sum), until the keys
+// left sum to at most `keep`, and let the integral's selection wait for them.  Used
+// when a threshold decision (convergence, the Gladwell count) lies within the FP32
+// uncertainty of the sums it compares.
+__device__ void escalate_keys(const IntDesc &d, IntState *S, const Pool &P, BatchHdr *H, int i,
+                              long long base, int R, double U, double keep, SelShared &sh)
+{
+    const double sc = 1152921504606846976.0 / U;  // 2^60 / U
+    unsigned long long ql = 0;
+    for (int j = threadIdx.x; j < R; j += SEL_BS) {
+        const double t = P.key[base + j] * sc;
+        const unsigned long long qq = t >= 1.8e19 ? 0xFFFFFFFFFFFFFFFFull : (unsigned long long)t;
+        P.q[base + j] = qq;
+        ql += qq;
+    }
+    const unsigned long long Qk = block_sum(ql, sh.ured);
+    const double kq = keep * sc;
+    const unsigned long long qk = kq >= 1.8e19 ? 0xFFFFFFFFFFFFFFFFull : (unsigned long long)kq;
+    const unsigned long long needp = Qk > qk ? Qk - qk : 1;
+    unsigned long long pb, ps;
+    unsigned int pc;
+    radix_select(P.key, P.q, base, R, true, needp, sh, pb, pc, ps);
+    for (int j = threadIdx.x; j < R; j += SEL_BS) {
+        const unsigned long long kb = (unsigned long long)__double_as_longlong(P.key[base + j]);
+        if (kb >= pb && P.key[base + j] > 0.0) push_esc(H, P, d.kind * 3 + d.term - 1, i, j | (1 << 30));
+    }
+    if (threadIdx.x == 0) {
+        S[i].K = 0;
+        S[i].defer = 1;
+        atomicAdd(&H->deferred, 1ull);
+        atomicAdd(&H->thr_checks, 1ull);
+    }
+    __syncthreads();
+}
+
 // pass 0 selects for every live integral; pass 1 (mixed precision) selects again, in
 // the same round, for the integrals pass 0 deferred, once the FP64 re-evaluation of
 // their ambiguous boundary regions has run.
@@ -207,8 +243,11 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
 {
     __shared__ SelShared sh;
     __shared__ int s_flag[4];  // fin, status, polish passes
-    __shared__ double s_tot[2];
+    __shared__ double s_tot[4];
     __shared__ int s_cancel;
+    // threshold guard (mixed precision): bound multiplier (gthr) and the value bounds' basis
+    const double gthr = H->mixed ? (double)H->thr_ratio : 0.0;
+    const double vr = (double)H->val_ratio;
     const int n = H->n;
     // a stop request: k_scan's (cancel or deadline), or a host cancel that arrived since
     // (one read of the host-mapped word per block)
@@ -240,14 +279,24 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
             __syncthreads();
             continue;
         }
-        // totals over live regions
-        double sv = 0, se = 0;
+        // totals over live regions (mixed: and the FP32 uncertainty of each total)
+        double sv = 0, se = 0, sue = 0, suv = 0;
         for (int j = threadIdx.x; j < R; j += SEL_BS) {
-            sv += P.val[base + j];
-            se += P.err[base + j];
+            const double v = P.val[base + j], e = P.err[base + j];
+            sv += v;
+            se += e;
+            if (gthr > 0.0) {
+                sue += e * (double)P.unc[base + j];
+                suv += fabs(v) * (double)P.uval[base + j];
+            }
         }
         double V = block_sum(sv, sh.dred);
         double E = block_sum(se, sh.dred);
+        double UE = 0, UV = 0;
+        if (gthr > 0.0) {
+            UE = gthr * block_sum(sue, sh.dred);
+            UV = gthr * vr * block_sum(suv, sh.dred);
+        }
         if (threadIdx.x == 0) {
             IntState st = S[i];
             int fin = 0, status = ST_OK;
@@ -272,8 +321,26 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
             s_flag[2] = st.pad;  // polish passes so far
             s_tot[0] = V;
             s_tot[1] = E;
+            // the convergence test E <= rtol |V| decided within the FP32 uncertainty
+            const bool tested = !s_cancel && isfinite(V) && isfinite(E) &&
+                                !(d.max_eval && st.neval >= d.max_eval);
+            s_flag[3] = gthr > 0.0 && tested && (UE + d.rtol * UV) > 0.0 &&
+                        fabs(E - fabs(V) * d.rtol) <= UE + d.rtol * UV;
         }
         __syncthreads();
+        if (s_flag[3]) {
+            const double margin = fabs(s_tot[1] - fabs(s_tot[0]) * d.rtol);
+            double ul = 0;
+            for (int j = threadIdx.x; j < R; j += SEL_BS) {
+                const double kj = gthr * (P.err[base + j] * (double)P.unc[base + j] +
+                                         d.rtol * vr * fabs(P.val[base + j]) * (double)P.uval[base + j]);
+                P.key[base + j] = kj;
+                ul += kj;
+            }
+            const double U = block_sum(ul, sh.dred);
+            escalate_keys(d, S, P, H, i, base, R, U, 0.9 * margin, sh);
+            continue;
+        }
         if (s_flag[0]) {
             // Mixed precision: before reporting, bound the FP32 noise left in the value.
             // If the regions' value bounds sum to more than tau_val |V|, re-evaluate in
@@ -372,6 +439,42 @@ __global__ void __launch_bounds__(SEL_BS) k_select(const IntDesc *__restrict__ D
             unsigned long long rest = need - sum_above;
             tneed = qb ? (rest + qb - 1) / qb : 1;
             Kconv = (unsigned long long)cnt_above + tneed;
+            // Mixed precision: the Gladwell count is the first k whose popped errors reach
+            // `need` (the error left is <= rtol |V|).  If either neighbouring count is within
+            // the FP32 uncertainty of the sums this compares (the errors not popped before
+            // the boundary, and rtol |V|), and the choice can matter (it moves a region of
+            // error b, and neighbours only where the budget allows), re-evaluate the regions
+            // carrying that uncertainty first.
+            const double b = __longlong_as_double((long long)bkey);
+            if (gthr > 0.0 && qb && Kconv <= Kcap && b > H->tau_thr * fabs(V)) {
+                const unsigned long long m_hi = sum_above + tneed * qb - need;  // < qb
+                const unsigned long long m_lo = qb - m_hi;
+                unsigned long long m = 0xFFFFFFFFFFFFFFFFull;
+                if (Kconv < Kcap && Kconv < (unsigned long long)R) m = m_hi;
+                if (Kconv > 1 && m_lo < m) m = m_lo;
+                if (m != 0xFFFFFFFFFFFFFFFFull) {
+                    double ur = 0;
+                    for (int j = threadIdx.x; j < R; j += SEL_BS)
+                        if (ekey(P.err, base + j) <= bkey)
+                            ur += P.err[base + j] * (double)P.unc[base + j];
+                    const double dlt = gthr * block_sum(ur, sh.dred) + d.rtol * UV;
+                    const double m_abs = (double)m / scale;
+                    if (dlt > 0.0 && m_abs <= dlt) {
+                        double ul = 0;
+                        for (int j = threadIdx.x; j < R; j += SEL_BS) {
+                            const double e = P.err[base + j];
+                            const double kj =
+                                (ekey(P.err, base + j) <= bkey ? gthr * e * (double)P.unc[base + j] : 0.0) +
+                                d.rtol * gthr * vr * fabs(P.val[base + j]) * (double)P.uval[base + j];
+                            P.key[base + j] = kj;
+                            ul += kj;
+                        }
+                        const double U = block_sum(ul, sh.dred);
+                        escalate_keys(d, S, P, H, i, base, R, U, 0.9 * m_abs, sh);
+                        continue;
+                    }
+                }
+            }
         }
         unsigned long long K = Kconv < Kcap ? Kconv : Kcap;
         if (K < 1) K = 1;
@@ -561,6 +664,7 @@ __global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, 
         H->deferred = 0;
         H->polished = 0;
         H->esc_full = 0;
+        H->thr_checks = 0;
         H->cancel = 0;
         H->t0_ns = global_timer_ns();
     }

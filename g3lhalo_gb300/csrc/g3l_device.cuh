@@ -160,6 +160,12 @@ struct BatchHdr {
     const volatile int *cancel_word;
     unsigned long long t0_ns;
     unsigned long long deadline_ns;  // 0 = none
+    // Mixed precision, threshold decisions (convergence, the Gladwell count): multiplier
+    // of the regions' FP32 bounds (0 = unguarded) and the value bounds' conversion to the
+    // selection bounds' basis (eps_sel / eps_val)
+    float thr_ratio, val_ratio;
+    double tau_thr;                  //   checked only if the region moved carries > tau_thr |V|
+    unsigned long long thr_checks;   // statistics: threshold decisions re-taken in FP64
 };
 
 __device__ __forceinline__ unsigned long long global_timer_ns()

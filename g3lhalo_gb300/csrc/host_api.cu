@@ -173,6 +173,9 @@ struct RunGuard {
 // the header fields that stop a call in flight
 void set_stop_fields(const g3l_ctx *c, BatchHdr &H)
 {
+    H.thr_ratio = (float)c->opt.unc_thr;
+    H.tau_thr = c->opt.unc_tau_thr;
+    H.val_ratio = (float)(c->opt.unc_eps_sel / std::max(c->opt.unc_eps_val, 1e-30));
     H.cancel = 0;
     H.cancel_word = c->cancel_d;
     H.deadline_ns = c->opt.deadline_ms > 0
@@ -919,6 +922,9 @@ void srv_loop(g3l_server *v)
         H.max_rounds = v->c->opt.max_rounds;
         H.mixed = v->precision == G3L_MIXED ? 1 : 0;
         H.chunk_rounds = v->chunk;
+        H.thr_ratio = (float)v->c->opt.unc_thr;
+        H.tau_thr = v->c->opt.unc_tau_thr;
+        H.val_ratio = (float)(v->c->opt.unc_eps_sel / std::max(v->c->opt.unc_eps_val, 1e-30));
         long long beg = 0;
         for (int g = 0; g < NGROUPS; ++g) {
             H.esc_beg[g] = beg;
@@ -1258,6 +1264,8 @@ try {
     c->opt.unc_tau_val = 5e-5;
     c->opt.unc_eps_val = 5e-6;
     c->opt.unc_eps_sel = 5e-5;
+    c->opt.unc_thr = 0.1;
+    c->opt.unc_tau_thr = 1e-6;
     // register-budget variant of the rule kernels per kind x term (autotuned default:
     // 6 blocks per SM for the 1-halo terms, 8 for the others)
     for (int g = 0; g < NGROUPS; ++g) c->opt.evalmx_variant[g] = g % 3 == 0 ? 1 : 2;
@@ -1556,6 +1564,7 @@ int g3l_set_options(g3l_ctx *c, const g3l_options *o)
     if (!c || !o || o->max_rounds < 1 || o->unlimited_pool < 16 || !(o->small_arg >= 0) ||
         !(o->unc_eps_rel > 0) || !(o->unc_eps_val >= 0) || !(o->unc_eps_sel >= 0) ||
         !(o->deadline_ms >= 0) || !std::isfinite(o->deadline_ms) ||
+        !(o->unc_thr >= 0) || !std::isfinite(o->unc_thr) || !(o->unc_tau_thr >= 0) ||
         std::any_of(o->evalmx_variant, o->evalmx_variant + NGROUPS,
                     [](int v) { return v < 0 || v > 2; })) {
         host::set_error("g3l_set_options: invalid option value");
@@ -1834,6 +1843,7 @@ try {
     sx.deferred = Hout.deferred;
     sx.polished = Hout.polished;
     sx.escalated_full = Hout.esc_full;
+    sx.thr_checks = Hout.thr_checks;
     sx.device_ms = ms;
     int first_bad = G3L_OK;
     uint64_t pts = 0;
@@ -2367,6 +2377,7 @@ int eval_static_locked(g3l_ctx *c, const g3l_integral *items, int n, int precisi
     sx.small_arg_fp64 = Hout.small_arg;
     sx.escalated = Hout.escalated;
     sx.escalated_full = Hout.esc_full;
+    sx.thr_checks = Hout.thr_checks;
     sx.deferred = Hout.deferred;
     sx.polished = Hout.polished;
     sx.h2d_bytes = sizeof(IntDesc) * n + sizeof(BatchHdr);

@@ -547,8 +547,11 @@ struct NbarEval {
     }
 };
 
+// 16 warps per integral: the batch of a round (up to ~800 regions) takes a few passes
+constexpr int NBAR_THREADS = 512;
+
 template <int CAP>
-__global__ void __launch_bounds__(PC_THREADS) k_nbar(NbarArgs A, const NbarTask *__restrict__ tasks,
+__global__ void __launch_bounds__(NBAR_THREADS) k_nbar(NbarArgs A, const NbarTask *__restrict__ tasks,
                                                      const int *__restrict__ idx, int ntask,
                                                      PcOut *__restrict__ out)
 {
@@ -839,7 +842,7 @@ int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const dou
         PC_CK(cudaMemcpyAsync(W.hods, hods + (size_t)6 * h0, sizeof(double) * 6 * nk,
                               cudaMemcpyHostToDevice, s));
         PC_CK(cudaMemsetAsync(A.st, 0, sizeof(unsigned) * E, s));
-        k_nbar<kNbarCapSmall><<<std::min(ntask, nsm * 2), PC_THREADS, pc_smem(kNbarCapSmall), s>>>(
+        k_nbar<kNbarCapSmall><<<std::min(ntask, nsm * 2), NBAR_THREADS, pc_smem(kNbarCapSmall), s>>>(
             A, (const NbarTask *)W.tasks, nullptr, ntask, (PcOut *)W.out);
         PC_CK(cudaGetLastError());
         res.resize(ntask);
@@ -851,7 +854,7 @@ int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const dou
         if (!big.empty()) {  // the rest with the larger heap, from their root regions
             const int nb = (int)big.size();
             PC_CK(cudaMemcpyAsync(W.idx, big.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
-            k_nbar<PC_CAP_LARGE><<<std::min(nb, nsm), PC_THREADS, pc_smem(PC_CAP_LARGE), s>>>(
+            k_nbar<PC_CAP_LARGE><<<std::min(nb, nsm), NBAR_THREADS, pc_smem(PC_CAP_LARGE), s>>>(
                 A, (const NbarTask *)W.tasks, (const int *)W.idx, nb, (PcOut *)W.out);
             PC_CK(cudaGetLastError());
             PC_CK(cudaMemcpyAsync(res.data(), W.out, sizeof(PcOut) * ntask, cudaMemcpyDeviceToHost,

@@ -237,6 +237,15 @@ typedef struct g3l_options {
      * selection with status G3L_ERR_DEADLINE and its value so far, as with
      * g3l_eval_cancel. */
     double deadline_ms;
+    /* Mixed precision: the threshold decisions of the refinement loop -- the
+     * convergence test err <= rtol |val| and the number of regions the Gladwell rule
+     * pops -- compare sums over many regions of FP32-derived values.  When one is closer
+     * to its threshold than unc_thr times the sum of the regions' bounds (the bounds of
+     * the selection, unc_eps_sel, and of the values, unc_eps_val), the regions carrying
+     * that uncertainty are re-evaluated in FP64 before deciding (default 0.1: the errors
+     * of many regions do not all add up; 0 = off).  The count is checked only where it
+     * moves a region whose error exceeds unc_tau_thr |val| (default 1e-6). */
+    double unc_thr, unc_tau_thr;
 } g3l_options;
 int g3l_get_options(g3l_ctx *ctx, g3l_options *opt);
 int g3l_set_options(g3l_ctx *ctx, const g3l_options *opt);
@@ -273,6 +282,8 @@ typedef struct g3l_stats {
     double select_ms;         /* selection + scan kernels */
     uint64_t h2d_bytes, d2h_bytes; /* bytes copied in / out by the call */
     uint64_t escalated_full;  /* of escalated: whole-rule re-evaluations (selection, polish) */
+    uint64_t thr_checks;      /* mixed precision: threshold decisions re-taken after FP64
+                                 re-evaluation (unc_thr) */
 } g3l_stats;
 int g3l_get_stats(g3l_ctx *ctx, g3l_stats *st);
 

@@ -188,3 +188,34 @@ def test_mixed_matches_fp64_at_other_tolerances(rect, rtol):
         b = c.eval(specs, G.MIXED)
         assert np.array_equal(a["neval"], b["neval"])
         assert _rel(b["val"], a["val"]).max() < TERM_RTOL
+
+
+def _region_set(c, index, dim):
+    p = c.debug_pool(index)
+    n = p["n"]
+    cen = p["centers"][:dim * n].reshape(dim, n).T
+    lev = p["levels"][:dim * n].reshape(dim, n).T
+    return {tuple(cen[j]) + tuple(lev[j]) for j in range(n)}
+
+
+def test_gladwell_count_near_its_threshold_follows_fp64(rect):
+    """A 3-halo term whose value nearly cancels (V = 2 against an error of 110 in round
+    16, rtol 1e-3): the Gladwell count -- how many regions leave the error within
+    rtol |V| -- sits within the FP32 noise of the sums it compares.  The mixed form
+    re-takes that decision after FP64 re-evaluation (unc_thr), so it cuts the same
+    regions as the FP64 form; unguarded, it cut one region more in round 16 and ended
+    7.3e-5 away (the same evaluation count: the budget cap evens the total out)."""
+    T, _ = rect
+    c = G.Context(T, clamp_k=True)
+    c.set_hod(0, W.hod_sweep(64, seed=12345)[46])
+    th = (0.00014545, 0.00046177496601754924, 0.0006786865952253847)
+    spec = (G.NNMAP, 3, 0, 0, th, 1e-3, 1_000_000)
+    a = c.eval([spec], G.FP64)
+    sa = _region_set(c, 0, 7)
+    b = c.eval([spec], G.MIXED)
+    sb = _region_set(c, 0, 7)
+    assert c.stats()["thr_checks"] > 0
+    c.close()
+    assert a["neval"][0] == b["neval"][0]
+    assert sa == sb, (len(sa - sb), len(sb - sa))
+    assert _rel(b["val"], a["val"])[0] < 1e-5
