@@ -49,6 +49,7 @@ constexpr int PC_CAP_SMALL = 512, PC_CAP_LARGE = 2048;
 constexpr int PC_CAP_TINY = 64;
 constexpr int PC_MAX_ROUNDS = 4096;
 constexpr size_t pc_smem(int cap) { return sizeof(double) * 4 * (cap + 2 * cap); }
+constexpr size_t nbar_smem(int cap) { return pc_smem(cap) + sizeof(int) * cap; }
 
 // QUADPACK qk15 nodes and weights (the reference's rule15gauss, src/hcubature.cpp:626-660)
 __constant__ double cXgk[8] = {0.991455371120812639206854697526329, 0.949107912342758524526189684047851,
@@ -365,6 +366,161 @@ __device__ PcOut gk_integrate(double lo, double hi, double *sm, const Eval &ev)
     return o;
 }
 
+// The same refinement with the live regions in plain arrays instead of a heap, for
+// integrals whose result needs agree with the reference's to ~1e-12 rather than in the
+// last bit (n_bar): each round the whole block sorts the live regions by error
+// (bitonic, descending) and thread 0 walks that order with the reference's Gladwell
+// rule (pop the largest errors until the rest is within tolerance), so the regions cut
+// are the heap's; only the order among exactly equal errors and the summation order of
+// the totals differ.  Shared memory: pc_smem(CAP) plus CAP ints.
+template <int CAP, class Eval>
+__device__ PcOut gk_integrate_sorted(double lo, double hi, double *sm, const Eval &ev)
+{
+    constexpr int PC_BATCH = 2 * CAP;
+    double *lc = sm, *lh = sm + CAP, *lv = sm + 2 * CAP, *le = sm + 3 * CAP;
+    double *bc = sm + 4 * CAP, *bh = bc + PC_BATCH, *bv = bh + PC_BATCH, *be = bv + PC_BATCH;
+    int *ord = (int *)(be + PC_BATCH);
+    __shared__ int s_nb, s_done, s_n, s_K, s_status, s_rounds;
+    __shared__ double s_red[2][32];
+    __shared__ unsigned long long s_neval;
+    const int tid = threadIdx.x, nth = blockDim.x;
+    if (tid == 0) {
+        bc[0] = 0.5 * (lo + hi);
+        bh[0] = 0.5 * (hi - lo);
+        s_nb = 1;
+        s_done = 0;
+        s_n = 0;
+        s_status = 0;
+        s_rounds = 0;
+        s_neval = 15;
+    }
+    __syncthreads();
+    // deterministic block sums of val and err over the live regions
+    auto totals = [&](int n, double &V, double &E) {
+        double v = 0, e = 0;
+        for (int i = tid; i < n; i += nth) {
+            v += lv[i];
+            e += le[i];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            v += __shfl_down_sync(0xffffffffu, v, o);
+            e += __shfl_down_sync(0xffffffffu, e, o);
+        }
+        if ((tid & 31) == 0) {
+            s_red[0][tid >> 5] = v;
+            s_red[1][tid >> 5] = e;
+        }
+        __syncthreads();
+        V = 0;
+        E = 0;
+        for (int w = 0; w < nth / 32; ++w) {
+            V += s_red[0][w];
+            E += s_red[1][w];
+        }
+        __syncthreads();
+    };
+    while (true) {
+        ev(s_nb, bc, bh, bv, be);
+        __syncthreads();
+        // the batch joins the live regions
+        const int n0 = s_n, nb = s_nb;
+        for (int b = tid; b < nb; b += nth) {
+            lc[n0 + b] = bc[b];
+            lh[n0 + b] = bh[b];
+            lv[n0 + b] = bv[b];
+            le[n0 + b] = be[b];
+        }
+        const int n = n0 + nb;
+        __syncthreads();
+        if (tid == 0) s_n = n;  // every thread has read n0 (barrier above)
+        double hv, he;
+        totals(n, hv, he);
+        if (converged(he, hv)) break;
+        // largest errors first
+        int P2 = 1;
+        while (P2 < n) P2 <<= 1;
+        for (int i = tid; i < P2; i += nth) ord[i] = i;
+        __syncthreads();
+        for (int k = 2; k <= P2; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int t = tid; t < P2; t += nth) {
+                    const int u = t ^ j;
+                    if (u > t) {
+                        const int a = ord[t], b = ord[u];
+                        const double ka = a < n ? le[a] : -1.0, kb = b < n ? le[b] : -1.0;
+                        // descending overall: the first half of each k-block descending
+                        const bool desc = (t & k) == 0;
+                        if (desc ? (ka < kb || (ka == kb && a > b)) : (ka > kb || (ka == kb && a < b))) {
+                            ord[t] = b;
+                            ord[u] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        if (tid == 0) {
+            int K = 0;
+            if (++s_rounds > PC_MAX_ROUNDS) {
+                s_status = G3L_ERR_ROUNDS;
+                s_done = 1;
+            } else {
+                double eErr = he;
+                const double eVal = hv;
+                do {
+                    if (n + K + 1 > CAP) {  // live regions and children after this pop
+                        s_status = G3L_ERR_POOL;
+                        s_done = 1;
+                        break;
+                    }
+                    eErr -= le[ord[K]];
+                    ++K;
+                    if (converged(eErr, eVal)) break;
+                } while (K < n);
+            }
+            s_K = K;
+        }
+        __syncthreads();
+        if (s_done) break;
+        const int K = s_K;
+        // children of the popped regions (cut, src/hcubature.cpp:206-218)
+        for (int k = tid; k < K; k += nth) {
+            const int r = ord[k];
+            const double h2 = lh[r] * 0.5;
+            bc[2 * k] = lc[r] - h2;
+            bh[2 * k] = h2;
+            bc[2 * k + 1] = lc[r] + h2;
+            bh[2 * k + 1] = h2;
+        }
+        // the rest stays live (gathered through the batch's value arrays)
+        const int m = n - K;
+        for (int k = tid; k < m; k += nth) {
+            const int r = ord[K + k];
+            bv[k] = lc[r];
+            bv[CAP + k] = lh[r];
+            be[k] = lv[r];
+            be[CAP + k] = le[r];
+        }
+        __syncthreads();
+        for (int k = tid; k < m; k += nth) {
+            lc[k] = bv[k];
+            lh[k] = bv[CAP + k];
+            lv[k] = be[k];
+            le[k] = be[CAP + k];
+        }
+        if (tid == 0) {
+            s_n = m;
+            s_nb = 2 * K;
+            s_neval += 30ull * (unsigned long long)K;
+        }
+        __syncthreads();
+    }
+    double V, E;
+    totals(s_n, V, E);
+    PcOut o{V, E, s_neval, s_status, s_rounds};
+    __syncthreads();
+    return o;
+}
+
 // The batch of one precompute integral: one region per half-warp, one point per lane.
 struct PcEval {
     const PkDev &P;
@@ -559,7 +715,7 @@ __global__ void __launch_bounds__(NBAR_THREADS) k_nbar(NbarArgs A, const NbarTas
     for (int tj = blockIdx.x; tj < ntask; tj += gridDim.x) {
         const int ti = idx ? idx[tj] : tj;
         const NbarTask t = tasks[ti];
-        const PcOut o = gk_integrate<CAP>(t.lo, t.hi, sm, NbarEval{A, t});
+        const PcOut o = gk_integrate_sorted<CAP>(t.lo, t.hi, sm, NbarEval{A, t});
         if (threadIdx.x == 0) out[ti] = o;
     }
 }
@@ -779,9 +935,9 @@ int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const dou
     const double lo = std::log10(B.mmin), hi = std::log10(B.mmax_integral());
     const double ln10 = std::log(10.0);
     PC_CK(cudaFuncSetAttribute(k_nbar<kNbarCapSmall>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)pc_smem(kNbarCapSmall)));
+                               (int)nbar_smem(kNbarCapSmall)));
     PC_CK(cudaFuncSetAttribute(k_nbar<PC_CAP_LARGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)pc_smem(PC_CAP_LARGE)));
+                               (int)nbar_smem(PC_CAP_LARGE)));
     std::vector<NbarTask> tasks;
     std::vector<PcOut> res;
     std::vector<int> big;
@@ -842,7 +998,7 @@ int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const dou
         PC_CK(cudaMemcpyAsync(W.hods, hods + (size_t)6 * h0, sizeof(double) * 6 * nk,
                               cudaMemcpyHostToDevice, s));
         PC_CK(cudaMemsetAsync(A.st, 0, sizeof(unsigned) * E, s));
-        k_nbar<kNbarCapSmall><<<std::min(ntask, nsm * 2), NBAR_THREADS, pc_smem(kNbarCapSmall), s>>>(
+        k_nbar<kNbarCapSmall><<<std::min(ntask, nsm * 2), NBAR_THREADS, nbar_smem(kNbarCapSmall), s>>>(
             A, (const NbarTask *)W.tasks, nullptr, ntask, (PcOut *)W.out);
         PC_CK(cudaGetLastError());
         res.resize(ntask);
@@ -854,7 +1010,7 @@ int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const dou
         if (!big.empty()) {  // the rest with the larger heap, from their root regions
             const int nb = (int)big.size();
             PC_CK(cudaMemcpyAsync(W.idx, big.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
-            k_nbar<PC_CAP_LARGE><<<std::min(nb, nsm), NBAR_THREADS, pc_smem(PC_CAP_LARGE), s>>>(
+            k_nbar<PC_CAP_LARGE><<<std::min(nb, nsm), NBAR_THREADS, nbar_smem(PC_CAP_LARGE), s>>>(
                 A, (const NbarTask *)W.tasks, (const int *)W.idx, nb, (PcOut *)W.out);
             PC_CK(cudaGetLastError());
             PC_CK(cudaMemcpyAsync(res.data(), W.out, sizeof(PcOut) * ntask, cudaMemcpyDeviceToHost,
