@@ -34,7 +34,7 @@ int n_bar(const Binning &B, const double *hmf, const double hod[6], double *out)
 struct NbarDevice {
     void *tasks = nullptr, *out = nullptr, *idx = nullptr, *cache = nullptr;
     double *hods = nullptr;
-    size_t ntask_cap = 0, nhod_cap = 0, cache_entries = 0;
+    size_t ntask_cap = 0, nhod_cap = 0;
 };
 void free_nbar_device(NbarDevice &W);
 // n_bar(z_i) of nh HOD vectors (hods: [nh][6] on the host) on the current device from its

@@ -567,14 +567,17 @@ __global__ void __launch_bounds__(PC_THREADS) k_pc_integrate(const PkDev *__rest
 // each z bin one adaptive Gauss-Kronrod integral at rtol 1e-4
 // (src/generalFunctions.cu:149-245, src/hcubature.cpp:620-765).
 //
-// The mass factors (m, N_c + N_s, mass bin) do not depend on z, and every z bin bisects
-// the same interval, so most 15-point blocks recur across the z bins of one HOD vector
-// (a 64 x 128 table set evaluates ~1.5M points per vector at ~30k distinct abscissae).
-// A block's factors are kept in a device hash table keyed by the region (centre and
-// half-width bits) and the HOD vector: the first half-warp to claim a key computes and
-// publishes them, later ones read them; a half-warp that meets a key being filled
-// computes its block itself (no waiting).  Every value is computed by the same
-// expression either way, so the result does not depend on who computed it.
+// The mass factors (m, N_c + N_s, mass bin) do not depend on z, and every region of
+// every z bin is a node of the same bisection tree of [log10 mmin, log10 mmax'): depth
+// d and index k, with half-width hw0 2^-d (exact) and the centre the cut arithmetic
+// c -+ h/2 produces along the path from the root.  k_nbar_factors evaluates the factors
+// of all 15 abscissae of every node down to depth NBAR_DEPTH, for every HOD vector of
+// the call, spread over the whole device and reproducing that arithmetic bit for bit;
+// the integrals then read them by node index and evaluate only deeper regions
+// themselves.  Either way a factor is the same expression of the same abscissa.
+constexpr int NBAR_DEPTH = 12;
+constexpr int NBAR_NODES = (2 << NBAR_DEPTH) - 1;  // depths 0..NBAR_DEPTH
+
 struct NbarTask {
     double lo, hi;
     int z_ix, hod;
@@ -585,23 +588,13 @@ struct NbarArgs {
     const double *hods;  // [hod][6] f, alpha, Mth, sigma, M', beta
     int Nm;
     double mmin, ln_mratio;  // mass bin = round(log(m / mmin) Nm / ln_mratio)
-    // block-factor table: state (0 empty, 1 being filled, 2 published), key, factors
-    unsigned *st;
-    unsigned long long *kc, *kh;
-    int *kg;
+    double lo, hi;           // integration range in log10 m
+    // factors of node n of HOD h at abscissa i: [(h * NBAR_NODES + n) * 15 + i]
     double *fm, *fS;
     int *fmix;
-    unsigned mask;  // entries - 1 (a power of two)
 };
 
-constexpr size_t kNbarEntryBytes = 4 + 8 + 8 + 4 + 15 * (8 + 8 + 4);
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p)
-{
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
+constexpr size_t kNbarNodeBytes = 15 * (8 + 8 + 4);
 
 // N_c + N_s (src/HOD.cu:35-76; erf taken once, the same argument in both) and the
 // nearest mass bin (src/NNMap_Model.cu:556) at x = log10 m
@@ -617,39 +610,38 @@ __device__ __forceinline__ void nbar_factors(const NbarArgs &A, const double *h,
     mix = min(max(mix, 0), A.Nm - 1);  // in range for every abscissa of the interval
 }
 
-// Find the region's block in the table (lane 0 of a half-warp).  mode 0: published,
-// read it at `slot`; 1: claimed, fill `slot`; 2: compute only.
-__device__ void nbar_probe(const NbarArgs &A, double c, double hw, int hod, int &mode, int &slot)
+// centre and half-width of node n (heap numbering: root 0, children 2n+1 and 2n+2 the
+// lower and upper half), by the cut arithmetic of the integrators (src/hcubature.cpp:
+// 206-218): h2 = hw / 2, children c - h2 and c + h2
+__device__ __forceinline__ void nbar_node(double lo, double hi, int n, double &c, double &hw)
 {
-    const unsigned long long kc = (unsigned long long)__double_as_longlong(c);
-    const unsigned long long kh = (unsigned long long)__double_as_longlong(hw);
-    unsigned long long x = kc * 0x9E3779B97F4A7C15ull;
-    x ^= (kh + 0x632BE59BD9B4E019ull) * 0xC2B2AE3D27D4EB4Full;
-    x ^= (unsigned long long)(hod + 1) * 0x165667B19E3779F9ull;
-    x ^= x >> 29;
-    unsigned idx = (unsigned)x & A.mask;
-    mode = 2;
-    slot = 0;
-    for (int probe = 0; probe < 16; ++probe, idx = (idx + 1) & A.mask) {
-        unsigned s = ld_acquire_u32(A.st + idx);
-        if (s == 0) {
-            s = atomicCAS(A.st + idx, 0u, 1u);
-            if (s == 0) {
-                A.kc[idx] = kc;
-                A.kh[idx] = kh;
-                A.kg[idx] = hod;
-                mode = 1;
-                slot = (int)idx;
-                return;
-            }
-            if (s == 2) s = ld_acquire_u32(A.st + idx);
-        }
-        if (s == 1) return;  // being filled: compute this block here
-        if (__ldcg(A.kc + idx) == kc && __ldcg(A.kh + idx) == kh && __ldcg(A.kg + idx) == hod) {
-            mode = 0;
-            slot = (int)idx;
-            return;
-        }
+    c = 0.5 * (lo + hi);
+    hw = 0.5 * (hi - lo);
+    int d = 31 - __clz(n + 1);  // depth
+    for (int l = d - 1; l >= 0; --l) {
+        const double h2 = hw * 0.5;
+        c = (((n + 1) >> l) & 1) ? c + h2 : c - h2;
+        hw = h2;
+    }
+}
+
+// one thread per (HOD, node, abscissa)
+__global__ void __launch_bounds__(256) k_nbar_factors(NbarArgs A, int nh)
+{
+    const long long total = (long long)nh * NBAR_NODES * 15;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % 15);
+        const long long hn = t / 15;
+        const int n = (int)(hn % NBAR_NODES), h = (int)(hn / NBAR_NODES);
+        double c, hw;
+        nbar_node(A.lo, A.hi, n, c, hw);
+        double m, S;
+        int mix;
+        nbar_factors(A, A.hods + 6 * h, gk_point(c, hw, i), m, S, mix);
+        A.fm[t] = m;
+        A.fS[t] = S;
+        A.fmix[t] = mix;
     }
 }
 
@@ -657,6 +649,7 @@ __device__ void nbar_probe(const NbarArgs &A, double c, double hw, int hod, int 
 struct NbarEval {
     const NbarArgs &A;
     const NbarTask &t;
+    double hw0;  // root half-width
     __device__ void operator()(int nb, const double *bc, const double *bh, double *bv,
                                double *be) const
     {
@@ -667,34 +660,26 @@ struct NbarEval {
         for (int r0 = 2 * warp; r0 < nb; r0 += 2 * nwarps) {
             const int r = r0 + half;
             const bool live = r < nb;
-            const double c = live ? bc[r] : 0.0, hw = live ? bh[r] : 0.0;
-            int mode = 2, slot = 0;
-            if (live && hl == 0) nbar_probe(A, c, hw, t.hod, mode, slot);
-            __syncwarp();  // orders lane 0's acquire before the other lanes' reads
-            mode = __shfl_sync(0xffffffffu, mode, 0, 16);
-            slot = __shfl_sync(0xffffffffu, slot, 0, 16);
             double f = 0;
+            const double c = live ? bc[r] : 0.0, hw = live ? bh[r] : 1.0;
             if (live && hl < 15) {
+                // node of the region: depth from the exact half-width, index from the
+                // centre (within a few ulp of lo + (2k + 1) hw)
+                const int d = ilogb(hw0) - ilogb(hw);
                 double m, S;
                 int mix;
-                const size_t k = (size_t)slot * 15 + hl;
-                if (mode == 0) {
-                    m = __ldcg(A.fm + k);
-                    S = __ldcg(A.fS + k);
-                    mix = __ldcg(A.fmix + k);
+                if (d >= 0 && d <= NBAR_DEPTH) {
+                    const long long k = (long long)floor((c - A.lo) / (2.0 * hw));
+                    const long long n = (1ll << d) - 1 + k;
+                    const size_t q = ((size_t)t.hod * NBAR_NODES + n) * 15 + hl;
+                    m = A.fm[q];
+                    S = A.fS[q];
+                    mix = A.fmix[q];
                 } else {
                     nbar_factors(A, h, gk_point(c, hw, hl), m, S, mix);
-                    if (mode == 1) {
-                        A.fm[k] = m;
-                        A.fS[k] = S;
-                        A.fmix[k] = mix;
-                    }
                 }
                 f = m * row[mix] * S;  // src/generalFunctions.cu:233-245
             }
-            if (mode == 1) __threadfence();
-            __syncwarp();
-            if (live && hl == 0 && mode == 1) atomicExch(A.st + slot, 2u);  // publish
             double vk[15];
 #pragma unroll
             for (int q = 0; q < 15; ++q) vk[q] = __shfl_sync(0xffffffffu, f, q, 16);
@@ -715,7 +700,7 @@ __global__ void __launch_bounds__(NBAR_THREADS) k_nbar(NbarArgs A, const NbarTas
     for (int tj = blockIdx.x; tj < ntask; tj += gridDim.x) {
         const int ti = idx ? idx[tj] : tj;
         const NbarTask t = tasks[ti];
-        const PcOut o = gk_integrate_sorted<CAP>(t.lo, t.hi, sm, NbarEval{A, t});
+        const PcOut o = gk_integrate_sorted<CAP>(t.lo, t.hi, sm, NbarEval{A, t, 0.5 * (t.hi - t.lo)});
         if (threadIdx.x == 0) out[ti] = o;
     }
 }
@@ -923,7 +908,7 @@ void free_nbar_device(NbarDevice &W)
 }
 
 namespace {
-constexpr int kNbarChunk = 256;          // HOD vectors per launch
+constexpr int kNbarChunk = 64;  // HOD vectors per launch (157 MB of factor tables)
 constexpr int kNbarCapSmall = 1024;      // live regions of the first pass
 }  // namespace
 
@@ -951,9 +936,6 @@ int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const dou
                 const int z_ix = (int)std::round((z - B.zmin) * B.Nz / (B.zmax - B.zmin));
                 tasks[(size_t)k * Nz + i] = NbarTask{lo, hi, z_ix, k};
             }
-        // ~2000 distinct blocks per vector: a table at most half full
-        size_t entries = 8192;
-        while (entries < (size_t)nk * 8192) entries <<= 1;
         if ((size_t)ntask > W.ntask_cap) {
             for (void **p : {&W.tasks, &W.out, &W.idx})
                 if (*p) cudaFree(*p), *p = nullptr;
@@ -963,41 +945,38 @@ int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const dou
             PC_CK(cudaMalloc(&W.idx, sizeof(int) * ntask));
             W.ntask_cap = (size_t)ntask;
         }
-        if ((size_t)nk > W.nhod_cap) {
+        if ((size_t)nk > W.nhod_cap) {  // HOD vectors and their factor tables
             if (W.hods) cudaFree(W.hods);
+            if (W.cache) cudaFree(W.cache);
             W.hods = nullptr;
+            W.cache = nullptr;
             W.nhod_cap = 0;
             PC_CK(cudaMalloc((void **)&W.hods, sizeof(double) * 6 * nk));
+            PC_CK(cudaMalloc(&W.cache, (size_t)nk * NBAR_NODES * kNbarNodeBytes));
             W.nhod_cap = (size_t)nk;
         }
-        if (entries > W.cache_entries) {
-            if (W.cache) cudaFree(W.cache);
-            W.cache = nullptr;
-            W.cache_entries = 0;
-            PC_CK(cudaMalloc(&W.cache, entries * kNbarEntryBytes));
-            W.cache_entries = entries;
-        }
-        const size_t E = W.cache_entries;
-        char *cb = (char *)W.cache;
+        const size_t E = (size_t)W.nhod_cap * NBAR_NODES * 15;
         NbarArgs A{};
         A.hmf = d_hmf;
         A.hods = W.hods;
         A.Nm = B.Nm;
         A.mmin = B.mmin;
         A.ln_mratio = std::log(B.mmax / B.mmin);
-        A.kc = (unsigned long long *)cb;
-        A.kh = A.kc + E;
-        A.fm = (double *)(A.kh + E);
-        A.fS = A.fm + 15 * E;
-        A.st = (unsigned *)(A.fS + 15 * E);
-        A.kg = (int *)(A.st + E);
-        A.fmix = A.kg + E;
-        A.mask = (unsigned)(E - 1);
+        A.lo = lo;
+        A.hi = hi;
+        A.fm = (double *)W.cache;
+        A.fS = A.fm + E;
+        A.fmix = (int *)(A.fS + E);
         PC_CK(cudaMemcpyAsync(W.tasks, tasks.data(), sizeof(NbarTask) * ntask,
                               cudaMemcpyHostToDevice, s));
         PC_CK(cudaMemcpyAsync(W.hods, hods + (size_t)6 * h0, sizeof(double) * 6 * nk,
                               cudaMemcpyHostToDevice, s));
-        PC_CK(cudaMemsetAsync(A.st, 0, sizeof(unsigned) * E, s));
+        {
+            const long long nthr = (long long)nk * NBAR_NODES * 15;
+            const int grid = (int)std::min<long long>((nthr + 255) / 256, (long long)nsm * 16);
+            k_nbar_factors<<<grid, 256, 0, s>>>(A, nk);
+            PC_CK(cudaGetLastError());
+        }
         k_nbar<kNbarCapSmall><<<std::min(ntask, nsm * 2), NBAR_THREADS, nbar_smem(kNbarCapSmall), s>>>(
             A, (const NbarTask *)W.tasks, nullptr, ntask, (PcOut *)W.out);
         PC_CK(cudaGetLastError());
