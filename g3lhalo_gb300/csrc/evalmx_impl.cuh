@@ -476,39 +476,9 @@ struct ModelF {
         return u_nfw32(kx * r, fac, T.small_arg, small);
     }
 
-    // u_NFW at k3 = |l1 + l2| / w with one halo mass (the 2- and 3-halo terms): it does
-    // not depend on the other mass dimensions, so the points that differ only there share
-    // it.  Function f uses mass dimension u3_mass(f) and ignores the dimensions in
-    // u3_drop(f) (3-bit variant fields of the point code); evaluated once per distinct
-    // projection of the rule's points (at most rule_points(5) = 93) by u3() with the
-    // expressions of point().
-    static constexpr int NU3 = TERM == 1 ? 0 : (TERM == 2 ? 2 : 1);
-    __host__ __device__ static constexpr int u3_mass(int f)
-    {
-        return TERM == 2 ? 3 + f : (KIND == 0 ? 5 : 4);
-    }
-    __host__ __device__ static constexpr uint32_t u3_drop(int f)
-    {
-        return TERM == 2 ? (7u << (3 * (4 - f)))
-                         : (KIND == 0 ? ((7u << 9) | (7u << 12)) : ((7u << 9) | (7u << 15)));
-    }
-    __device__ static float u3(const DevTables &T, int f, const SlotF *const *s, int &small)
-    {
-        const SlotF &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
-        const SlotF &M = *s[u3_mass(f)];
-        const float l1 = L1.f[0], l2 = L2.f[0];
-        const float dl = l1 - l2;
-        const float l3 = sqrtf(fmaf(dl, dl, 2.f * l1 * l2 * PH.f[1]));
-        const float k3 = l3 * Z.f[1];
-        const float r = cbrtf(M.f[0] * Z.f[2]);
-        const float c = __ldg(T.f_conc + Z.i1 * T.Nm + M.i1);
-        return u_nfw32(k3 * r, c, T.small_arg, small);
-    }
-
-    // uc: the cached (l, m, z) u_NFW of the point; u3c: its cached k3 u_NFW (u3())
     __device__ static float point(const DevTables &T, const IntDesc &d, const SlotF *const *s,
                                   const Child &C, int ch, int sdim, uint32_t vv, unsigned &ties,
-                                  int &small, const float *uc, const float *u3c)
+                                  int &small, const float *uc)
     {
         const SlotF &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
         const float l1 = L1.f[0], l2 = L2.f[0], cphi = PH.f[0];
@@ -539,8 +509,11 @@ struct ModelF {
                 const int kx3 = kidx_k3(T, d, C, ch, sdim, vv, zr, k3, false, ties);
                 const float P1 = plin32(T, zr, kx1, k1), P2 = plin32(T, zr, kx2, k2);
                 const float P3 = plin32(T, zr, kx3, k3);
-                const float u3_1 = u3c[0];
-                const float u3_2 = u3c[1];
+                const float ra = cbrtf(M1.f[0] * k200), rb = cbrtf(M2.f[0] * k200);
+                const float ca = __ldg(T.f_conc + zt * Nm + M1.i1);
+                const float cb = __ldg(T.f_conc + zt * Nm + M2.i1);
+                const float u3_1 = u_nfw32(k3 * ra, ca, sa, small);
+                const float u3_2 = u_nfw32(k3 * rb, cb, sa, small);
                 const float u1_1 = uc[0];
                 const float u2_1 = uc[1];
                 const float u1_2 = uc[2];
@@ -558,7 +531,7 @@ struct ModelF {
             } else {
                 const SlotF &M1 = *s[3], &M2 = *s[4], &M3 = *s[5];
                 const float m1 = M1.f[0], m2 = M2.f[0], m3 = M3.f[0];
-                const float u3 = u3c[0];
+                const float u3 = u_nfw32(k3 * cbrtf(m3 * k200), __ldg(T.f_conc + zt * Nm + M3.i1), sa, small);
                 const float u1 = UC ? uc[0] : u_nfw32(k1 * cbrtf(m1 * k200), f1 * __ldg(T.f_conc + zt * Nm + M1.i1), sa, small);
                 const float u2 = UC ? uc[1] : u_nfw32(k2 * cbrtf(m2 * k200), f2 * __ldg(T.f_conc + zt * Nm + M2.i1), sa, small);
                 const float G1 = M1.f[1] + M1.f[2] * u1, G2 = M2.f[3] + M2.f[4] * u2;
@@ -588,10 +561,13 @@ struct ModelF {
                 const int kx3 = kidx_k3(T, d, C, ch, sdim, vv, zr, k3, false, ties);
                 const float P1 = plin32(T, zr, kx1, k1), P2 = plin32(T, zr, kx2, k2);
                 const float P3 = plin32(T, zr, kx3, k3);
+                const float ra = cbrtf(M1.f[0] * k200), rb = cbrtf(M2.f[0] * k200);
+                const float ca = __ldg(T.f_conc + zt * Nm + M1.i1);
+                const float cb = __ldg(T.f_conc + zt * Nm + M2.i1);
                 const float u2_1 = uc[0];
-                const float u3_2 = u3c[1];
+                const float u3_2 = u_nfw32(k3 * rb, cb, sa, small);
                 const float u1_2f = uc[1];
-                const float u3_1 = u3c[0];
+                const float u3_1 = u_nfw32(k3 * ra, ca, sa, small);
                 const float u2_2 = uc[2];
                 const float u1_1f = uc[3];
                 const float G2 = M2.f[1] + M2.f[2] * u1_2f, G1 = M1.f[1] + M1.f[2] * u1_1f;
@@ -609,7 +585,7 @@ struct ModelF {
                 const float ca = __ldg(T.f_conc + zt * Nm + M1.i1);
                 const float cb = __ldg(T.f_conc + zt * Nm + M2.i1);
                 const float u2_1 = UC ? uc[0] : u_nfw32(k2 * ra, ca, sa, small);
-                const float u3_2 = u3c[0];
+                const float u3_2 = u_nfw32(k3 * rb, cb, sa, small);
                 const float G = M3.f[1] + M3.f[2] * (UC ? uc[1] : u_nfw32(k1 * rb, f * cb, sa, small));
                 const float Bi = bi32(T, d, C, ch, sdim, vv, zr, k1, k2, k3, cphi, L1, L2, ties);
                 const float HB = (__ldg(T.f_hmf + zr * Nm + M1.i0) * m1 * m1) *
@@ -677,58 +653,12 @@ __device__ __forceinline__ df hw_sum(df a)
 // integral (default 0: always); the selection kernel has it re-taken in FP64 if the
 // region is cut.  The error estimate's bound (unc) decides selection boundaries.
 
-// Projections of the rule's points for the k3 u_NFW cache (ModelF::u3): u3rep[f][p] is
-// the projection of point p (its variant code without the dimensions u3_drop(f)),
-// numbered in the order of first occurrence; u3list[f][j] is the first point of
-// projection j and u3n[f] their count.  Block-cooperative (every thread of the block
-// calls it; it synchronises); sdesc must hold the point codes; tmp: 2 NP bytes.
-constexpr int U3_MAX = rule_points(5);  // projections onto the five dimensions kept
-
-template <int KIND, int TERM>
-__device__ inline void u3_tables(const uint32_t *sdesc, uint8_t *u3rep, uint8_t *u3list, int *u3n,
-                                 uint8_t *tmp)
-{
-    constexpr int NP = rule_points(TERM + 4);
-    for (int f = 0; f < ModelF<KIND, TERM>::NU3; ++f) {
-        const uint32_t keep = ~ModelF<KIND, TERM>::u3_drop(f);
-        uint8_t *first = tmp, *cidx = tmp + NP;
-        for (int p = threadIdx.x; p < NP; p += blockDim.x) {
-            const uint32_t key = sdesc[p] & keep;
-            int q = 0;
-            while (q < p && (sdesc[q] & keep) != key) ++q;
-            first[p] = (uint8_t)q;
-        }
-        __syncthreads();
-        if (threadIdx.x < 32) {  // number the projections in point order
-            const int lane = threadIdx.x;
-            int base = 0;
-            for (int c = 0; c < NP; c += 32) {
-                const int q = c + lane;
-                const bool on = q < NP && first[q] == q;
-                const unsigned b = __ballot_sync(0xffffffffu, on);
-                const int idx = base + __popc(b & ((1u << lane) - 1u));
-                if (on && idx < U3_MAX) {
-                    cidx[q] = (uint8_t)idx;
-                    u3list[f * U3_MAX + idx] = (uint8_t)q;
-                }
-                base += __popc(b);
-            }
-            if (lane == 0) u3n[f] = base < U3_MAX ? base : U3_MAX;
-        }
-        __syncthreads();
-        for (int p = threadIdx.x; p < NP; p += blockDim.x) u3rep[f * NP + p] = cidx[first[p]];
-        __syncthreads();
-    }
-}
-
 template <int KIND, int TERM>
 __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, double Vcur,
                            const Pool &P, BatchHdr *H, long long pslot, long long qslot, bool cut,
                            SlotF *slots, float *vals, Child &C, const uint32_t *sdesc,
                            unsigned &ties, int &small, const uint8_t *ucidx,
-                           const uint16_t *ucl, const int *ucn, float *ucache,
-                           const uint8_t *u3rep, const uint8_t *u3list, const int *u3n,
-                           float *u3cache)
+                           const uint16_t *ucl, const int *ucn, float *ucache)
 {
     constexpr int DIM = TERM + 4;
     constexpr int NP = rule_points(DIM);
@@ -794,22 +724,6 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
             ModelF<KIND, TERM>::ucached(T, d, f, sl(dl, vl), sl(dm, vm), sl(DIM - 1, vz), small);
     }
     __syncwarp();
-    // u_NFW at k3 of each projection the points share (2- and 3-halo terms), per child
-    constexpr int NU3 = ModelF<KIND, TERM>::NU3;
-    for (int t = lane; NU3 > 0 && t < nchild * NU3 * U3_MAX; t += 32) {
-        const int ch = t / (NU3 * U3_MAX), r = t - ch * NU3 * U3_MAX;
-        const int f = r / U3_MAX, j = r - f * U3_MAX;
-        if (j >= u3n[f]) continue;
-        const uint32_t vv = sdesc[u3list[f * U3_MAX + j]];
-        const SlotF *sp[DIM];
-#pragma unroll
-        for (int dd = 0; dd < DIM; ++dd) {
-            const int v = (vv >> (3 * dd)) & 7;
-            sp[dd] = (ch && dd == sdim) ? &slots[DIM * NVAR + v] : &slots[dd * NVAR + v];
-        }
-        u3cache[(ch * NU3 + f) * U3_MAX + j] = ModelF<KIND, TERM>::u3(T, f, sp, small);
-    }
-    __syncwarp();
     // points
     for (int p = lane; p < nchild * NP; p += 32) {
         const int ch = p >= NP ? 1 : 0;
@@ -826,11 +740,7 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
 #pragma unroll
             for (int f = 0; f < NF; ++f) uc[f] = ucache[(ch * NF + f) * UC_MAX + ucidx[f * NP + pp]];
         }
-        float u3v[NU3 > 0 ? NU3 : 1] = {};
-#pragma unroll
-        for (int f = 0; f < NU3; ++f)
-            u3v[f] = u3cache[(ch * NU3 + f) * U3_MAX + u3rep[f * NP + pp]];
-        vals[p] = ModelF<KIND, TERM>::point(T, d, sp, C, ch, sdim, vv, ties, small, uc, u3v);
+        vals[p] = ModelF<KIND, TERM>::point(T, d, sp, C, ch, sdim, vv, ties, small, uc);
         if (H->dbg) H->dbg[p] = (double)vals[p];
     }
     __syncwarp();
@@ -988,16 +898,10 @@ __global__ void __launch_bounds__(128, MINB) k_evalmx(DevTables T, const IntDesc
     __shared__ int ucn[NF];
     __shared__ float ucache[WPB][2 * NF * UC_MAX];
     __shared__ uint8_t ucmap[NF * 343];
-    constexpr int NU3 = ModelF<KIND, TERM>::NU3 > 0 ? ModelF<KIND, TERM>::NU3 : 1;
-    __shared__ uint8_t u3rep[NU3 * NP];           // projection of each point, per function
-    __shared__ uint8_t u3list[NU3 * U3_MAX];      // first point of each projection
-    __shared__ int u3n[NU3];
-    __shared__ float u3cache[WPB][2 * NU3 * U3_MAX];
     if (ModelF<KIND, TERM>::UC) ucache_tables<KIND, TERM>(ucidx, ucl, ucn, ucmap);
     const int g = KIND * 3 + TERM - 1;
     for (int p = threadIdx.x; p < NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
     __syncthreads();
-    u3_tables<KIND, TERM>(sdesc, u3rep, u3list, u3n, ucmap);  // ucmap is free again
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gb = H->gbeg[g], ge = H->gbeg[g + 1];
     if (gb >= ge) return;
@@ -1021,7 +925,7 @@ __global__ void __launch_bounds__(128, MINB) k_evalmx(DevTables T, const IntDesc
         const long long qslot = cut ? d.base + (S[i].nR - S[i].K) + j : -1;
         warp_itemF<KIND, TERM>(T, d, i, S[i].val, P, H, pslot, qslot, cut, sslot[wib],
                                svals[wib], schild[wib], sdesc, ties, small, ucidx, ucl, ucn,
-                               ucache[wib], u3rep, u3list, u3n, u3cache[wib]);
+                               ucache[wib]);
     }
     // warp-aggregated diagnostics
     unsigned tw = __reduce_add_sync(0xffffffffu, ties);
