@@ -535,8 +535,8 @@ int build_graph_ws(g3l_ctx *c, Workspace &W, int precision, int gmask, bool init
         int st = add_reevals(prev);
         if (st) return st;
     }
-    // the groups' rule kernels touch disjoint integrals: side by side, so that one
-    // kernel's tail overlaps the next group's work
+    // the groups' rule kernels in a chain (side-by-side branches measured slower: each
+    // kernel fills the device, and concurrent ones contend for it)
     for (int grp = 0; grp < NGROUPS; ++grp) {
         if (!(gmask & (1 << grp))) continue;
         void *fn = eval_fn(c, precision, grp);
@@ -544,6 +544,7 @@ int build_graph_ws(g3l_ctx *c, Workspace &W, int precision, int gmask, bool init
         cudaGraphNode_t n_ev;
         int st = add_kernel(body, &n_ev, &prev, 1, fn, eval_grid(c, fn), 128, args);
         if (st) return st;
+        prev = n_ev;
     }
     cudaGraphExec_t ex;
     G3L_CK(cudaGraphInstantiate(&ex, g, 0));

@@ -645,6 +645,49 @@ __global__ void __launch_bounds__(256) k_nbar_factors(NbarArgs A, int nh)
     }
 }
 
+// The 15-point Gauss-Kronrod value and QUADPACK error of rule_gk15, formed across the
+// 16 lanes of a half-warp (lane i holds the value at abscissa i of gk_point's order;
+// lane 15 holds nothing) instead of by one lane: the same sums in another order.
+// Valid in lane 0 of the half-warp.
+__device__ __forceinline__ void rule_gk15_hw(double f, int hl, double hw, double &val, double &err)
+{
+    // abscissa i: 0 centre, then pairs (2j+1, 2j+2): Gauss-Kronrod pair j (Kronrod-only
+    // nodes for j = 0, 2, 4, 6 of cXgk; Gauss nodes for odd j)
+    double wk = 0, wg = 0;
+    if (hl == 0) {
+        wk = cWgk[7];
+        wg = cWg[3];
+    } else if (hl < 7) {  // pairs j = 0..2: Gauss nodes cXgk[2j+1]
+        const int j = (hl - 1) >> 1;
+        wk = cWgk[2 * j + 1];
+        wg = cWg[j];
+    } else if (hl < 15) {  // pairs j = 3..6: Kronrod nodes cXgk[2(j-3)]
+        const int j = (hl - 1) >> 1;
+        wk = cWgk[2 * (j - 3)];
+    }
+    double rk = wk * f, rg = wg * f, ra = wk * fabs(f);
+    for (int o = 8; o > 0; o >>= 1) {
+        rk += __shfl_xor_sync(0xffffffffu, rk, o, 16);
+        rg += __shfl_xor_sync(0xffffffffu, rg, o, 16);
+        ra += __shfl_xor_sync(0xffffffffu, ra, o, 16);
+    }
+    const double mean = rk * 0.5;
+    double rs = wk * fabs(f - mean);
+    for (int o = 8; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o, 16);
+    val = rk * hw;
+    double e = fabs(rk - rg) * hw;
+    const double rabs = ra * hw, rasc = rs * hw;
+    if (rasc != 0 && e != 0) {
+        const double scale = pow((200 * e / rasc), 1.5);
+        e = (scale < 1) ? rasc * scale : rasc;
+    }
+    if (rabs > DBL_MIN / (50 * DBL_EPSILON)) {
+        const double min_err = 50 * DBL_EPSILON * rabs;
+        if (min_err > e) e = min_err;
+    }
+    err = e;
+}
+
 // The batch of one n_bar integral: one region per half-warp, one point per lane.
 struct NbarEval {
     const NbarArgs &A;
@@ -680,10 +723,12 @@ struct NbarEval {
                 }
                 f = m * row[mix] * S;  // src/generalFunctions.cu:233-245
             }
-            double vk[15];
-#pragma unroll
-            for (int q = 0; q < 15; ++q) vk[q] = __shfl_sync(0xffffffffu, f, q, 16);
-            if (live && hl == 0) rule_gk15(vk, hw, bv[r], be[r]);
+            double v, e;
+            rule_gk15_hw(f, hl, hw, v, e);
+            if (live && hl == 0) {
+                bv[r] = v;
+                be[r] = e;
+            }
         }
     }
 };
