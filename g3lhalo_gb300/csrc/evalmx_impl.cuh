@@ -157,8 +157,27 @@ __device__ __forceinline__ void fg_large(float x, float &f, float &g, float &fm)
     g = t * __fdividef(c, d);
 }
 
+// The FP64 form of u_nfw32 for a1 = kr / c below the small-argument threshold, where the
+// Si/Ci differences cancel.  Kept out of line: it is rare, and inlined in every call
+// site it would crowd the instruction cache of the rule kernels.
+static __device__ __noinline__ float u_nfw_small64(float kr, float c)
+{
+    const double cd = (double)c;
+    const double a1d = (double)kr / cd;
+    const double a2d = a1d * (1 + cd);
+    double si1, ci1, si2, ci2;
+    sici64(a1d, si1, ci1);
+    sici64(a2d, si2, ci2);
+    double s1, c1;
+    sincos(a1d, &s1, &c1);
+    double num = s1 * (si2 - si1) + c1 * (ci2 - ci1) - sin(a1d * cd) / a2d;
+    return (float)(num / (log(1. + cd) - cd / (1. + cd)));
+}
+
 // NFW profile u(k, m) from kr = k r_200 and c = f conc; a1 = kr / c, a2 = a1 (1 + c),
 // a1 c = kr.  Returns the FP32 value; lanes with a1 < small_arg take the FP64 form.
+// The Si/Ci parts of a1 and a2 (a1 < a2) come from one loop body, small-argument form
+// below 4 and auxiliary functions f, g above, so the code holds each form once.
 __device__ __forceinline__ float u_nfw32(float kr, float c, float small_arg, int &small_hits)
 {
     if (!(kr > 0.f)) return 1.f;  // k -> 0 limit of the profile
@@ -169,39 +188,49 @@ __device__ __forceinline__ float u_nfw32(float kr, float c, float small_arg, int
     const float F = lnopc - __fdividef(c, opc);
     if (a1 < small_arg) {
         ++small_hits;
-        const double cd = (double)c;
-        const double a1d = (double)kr / cd;
-        const double a2d = a1d * (1 + cd);
-        double si1, ci1, si2, ci2;
-        sici64(a1d, si1, ci1);
-        sici64(a2d, si2, ci2);
-        double s1, c1;
-        sincos(a1d, &s1, &c1);
-        double num = s1 * (si2 - si1) + c1 * (ci2 - ci1) - sin(a1d * cd) / a2d;
-        return (float)(num / (log(1. + cd) - cd / (1. + cd)));
+        return u_nfw_small64(kr, c);
     }
     float s1, c1, sk, ck;
     sincosf(a1, &s1, &c1);
     sincosf(kr, &sk, &ck);
+    // (a, b, e) of a1 and of a2: small form (Si, Ci polynomial, 0) below 4, else
+    // (f, g, f - 1/x)
+    float a1a = 0.f, a1b = 0.f, a2a = 0.f, a2b = 0.f, a2e = 0.f;
+#pragma unroll 1
+    for (int q = 0; q < 2; ++q) {
+        const float x = q ? a2 : a1;
+        float a, b, e;
+        if (x < 4.f) {
+            a = si_small(x);
+            b = ci_small_poly(x);
+            e = 0.f;
+        } else {
+            fg_large(x, a, b, e);
+        }
+        if (q == 0) {
+            a1a = a;
+            a1b = b;
+        } else {
+            a2a = a;
+            a2b = b;
+            a2e = e;
+        }
+    }
     float N;
     if (a2 < 4.f) {
-        const float dS = si_small(a2) - si_small(a1);
-        const float dC = lnopc + (ci_small_poly(a2) - ci_small_poly(a1));
+        const float dS = a2a - a1a;
+        const float dC = lnopc + (a2b - a1b);
         N = s1 * dS + c1 * dC - __fdividef(sk, a2);
     } else if (a1 >= 4.f) {
-        float f1, g1, fm1, f2, g2, fm2;
-        fg_large(a1, f1, g1, fm1);
-        fg_large(a2, f2, g2, fm2);
-        N = g1 - g2 * ck + fm2 * sk;
+        N = a1b - a2b * ck + a2e * sk;  // g(a1) - g(a2) cos(kr) + (f(a2) - 1/a2) sin(kr)
     } else {
-        float f2, g2, fm2;
-        fg_large(a2, f2, g2, fm2);
+        const float f2 = a2a, g2 = a2b;
         const float s2 = s1 * ck + c1 * sk;  // sin(a1 + a1 c)
         const float c2 = c1 * ck - s1 * sk;
         const float Si2 = HALF_PI_F - f2 * c2 - g2 * s2;
         const float Ci2 = f2 * s2 - g2 * c2;
-        const float Si1 = si_small(a1);
-        const float Ci1 = GAMMA_F + __logf(a1) + ci_small_poly(a1);
+        const float Si1 = a1a;
+        const float Ci1 = GAMMA_F + __logf(a1) + a1b;
         N = s1 * (Si2 - Si1) + c1 * (Ci2 - Ci1) - __fdividef(sk, a2);
     }
     return __fdividef(N, F);
@@ -297,6 +326,59 @@ __device__ __forceinline__ df ln_df(float v)
     return df_add_f(el, logf(m));
 }
 
+// Exact nearest-bin / truncated indices for arguments within IDX_TOL of a rounding
+// boundary: the tie table for the dyadic centre values (v == 0), else the reference's FP64
+// expression (src/NNMap_Model.cu:555-556, 796-799).  Out of line, like the k indices
+// below: they are rare, and their FP64 code would otherwise crowd the rule kernels'
+// instruction cache.  Return 1 when the FP64 expression was evaluated (counted).
+static __device__ __noinline__ int m_index_exact(const DevTables &T, double x64, int v, int &ir, int &it)
+{
+    if (v == 0 && tie_lookup(T.tie_m_bits, T.tie_m_round, T.tie_m_trunc, T.n_tie_m, x64, ir, it))
+        return 0;
+    double m = pow(10.0, x64);
+    double ar = log(m / T.mmin) * T.Nm / T.ln_mratio;
+    ir = min(max((int)round(ar), 0), T.Nm - 1);
+    it = min(max((int)ar, 0), T.Nm - 1);
+    return 1;
+}
+
+static __device__ __noinline__ int z_index_exact(const DevTables &T, double x64, int v, int &ir, int &it)
+{
+    if (v == 0 && tie_lookup(T.tie_z_bits, T.tie_z_round, T.tie_z_trunc, T.n_tie_z, x64, ir, it))
+        return 0;
+    double zr = (x64 - T.zmin) * T.Nz / (T.zmax - T.zmin);
+    ir = min(max((int)round(zr), 0), T.Nz - 1);
+    it = min(max((int)zr, 0), T.Nz - 1);
+    return 1;
+}
+
+// the k index of k = 10^x / w(z), by the reference's expression
+static __device__ __noinline__ int kidx_l_exact(const DevTables &T, double x, int zr)
+{
+    const double l = pow(10.0, x);
+    return kix_exact64(T, l / T.w[zr]);
+}
+
+// the k index of k3 from the FP64 coordinates of l1, l2 and phi: |l1 + l2| / w
+// (src/NNMap_Model.cu:814-817), or the bispectrum's k3 from k1 = l1 / w, k2 = l2 / w
+// (src/generalFunctions.cu:99)
+static __device__ __noinline__ int kidx_k3_exact(const DevTables &T, double x1, double x2, double xphi,
+                                          int zr, bool from_k)
+{
+    const double cph = cos(xphi);
+    double p1 = pow(10.0, x1), p2 = pow(10.0, x2);
+    const double wz = T.w[zr];
+    if (from_k) {
+        p1 = p1 / wz;
+        p2 = p2 / wz;
+    }
+    double q = __dadd_rn(__dadd_rn(__dmul_rn(p1, p1), __dmul_rn(p2, p2)),
+                         __dmul_rn(__dmul_rn(__dmul_rn(2.0, p1), p2), cph));
+    q = sqrt(q);
+    if (!from_k) q = q / wz;
+    return kix_exact64(T, q);
+}
+
 // ------------------------------------------------------------------ per-term models
 struct Child {
     double c64[MAX_DIM + 1];  // FP64 centres: dims of child 0, then child 1's split dim
@@ -339,17 +421,8 @@ struct ModelF {
         } else if (dim < 3 + TERM) {  // halo mass (log10 m)
             int ir, it;
             df a = df_mul(df_add(x, df_neg({T.m_x02.x, T.m_x02.y})), {T.m_s2.x, T.m_s2.y});
-            if (idx_df(a, T.Nm, IDX_TOL, ir, it)) {
-                double x64 = coord64(d, C, slotdim, dim, v);
-                if (!(v == 0 && tie_lookup(T.tie_m_bits, T.tie_m_round, T.tie_m_trunc, T.n_tie_m,
-                                           x64, ir, it))) {
-                    double m = pow(10.0, x64);
-                    double ar = log(m / T.mmin) * T.Nm / T.ln_mratio;
-                    ir = min(max((int)round(ar), 0), T.Nm - 1);
-                    it = min(max((int)ar, 0), T.Nm - 1);
-                    ++ties;
-                }
-            }
+            if (idx_df(a, T.Nm, IDX_TOL, ir, it))
+                ties += m_index_exact(T, coord64(d, C, slotdim, dim, v), v, ir, it);
             S.i0 = ir;
             S.i1 = it;
             S.f[0] = exp10f(x.hi - 12.f) * fmaf(2.302585093f, x.lo, 1.f);  // m / 1e12
@@ -377,16 +450,8 @@ struct ModelF {
         } else {  // z
             int ir, it;
             df a = df_mul(df_add(x, df_neg({T.z_02.x, T.z_02.y})), {T.z_s2.x, T.z_s2.y});
-            if (idx_df(a, T.Nz, IDX_TOL, ir, it)) {
-                double x64 = coord64(d, C, slotdim, dim, v);
-                if (!(v == 0 && tie_lookup(T.tie_z_bits, T.tie_z_round, T.tie_z_trunc, T.n_tie_z,
-                                           x64, ir, it))) {
-                    double zr = (x64 - T.zmin) * T.Nz / (T.zmax - T.zmin);
-                    ir = min(max((int)round(zr), 0), T.Nz - 1);
-                    it = min(max((int)zr, 0), T.Nz - 1);
-                    ++ties;
-                }
-            }
+            if (idx_df(a, T.Nz, IDX_TOL, ir, it))
+                ties += z_index_exact(T, coord64(d, C, slotdim, dim, v), v, ir, it);
             S.i0 = ir;
             S.i1 = it;
             const float opz = 1.f + (x.hi + x.lo);
@@ -423,8 +488,7 @@ struct ModelF {
         int ix = round_df(a, IDX_TOL, near);
         if (!near) return ix;
         ++ties;
-        const double l = pow(10.0, px64(d, C, ch, sdim, dl, vv));
-        return kix_exact64(T, l / T.w[zr]);
+        return kidx_l_exact(T, px64(d, C, ch, sdim, dl, vv), zr);
     }
 
     // k index of k3 (|l1 + l2| / w, or from k1, k2 in the bispectrum), exact on a boundary
@@ -438,19 +502,8 @@ struct ModelF {
         int ix = round_df(a, K3_TOL, near);
         if (!near) return ix;
         ++ties;
-        const double x1 = px64(d, C, ch, sdim, 0, vv), x2 = px64(d, C, ch, sdim, 1, vv);
-        const double cph = cos(px64(d, C, ch, sdim, 2, vv));
-        double p1 = pow(10.0, x1), p2 = pow(10.0, x2);
-        const double wz = T.w[zr];
-        if (from_k) {  // src/generalFunctions.cu:99 with k = l / w
-            p1 = p1 / wz;
-            p2 = p2 / wz;
-        }
-        double q = __dadd_rn(__dadd_rn(__dmul_rn(p1, p1), __dmul_rn(p2, p2)),
-                             __dmul_rn(__dmul_rn(__dmul_rn(2.0, p1), p2), cph));
-        q = sqrt(q);
-        if (!from_k) q = q / wz;  // src/NNMap_Model.cu:814-817
-        return kix_exact64(T, q);
+        return kidx_k3_exact(T, px64(d, C, ch, sdim, 0, vv), px64(d, C, ch, sdim, 1, vv),
+                             px64(d, C, ch, sdim, 2, vv), zr, from_k);
     }
 
     // u_NFW calls that depend on one l, one mass and z only: evaluated once per distinct

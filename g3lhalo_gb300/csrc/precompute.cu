@@ -447,7 +447,10 @@ __device__ PcOut gk_integrate_sorted(double lo, double hi, double *sm, const Eva
                     const int u = t ^ j;
                     if (u > t) {
                         const int a = ord[t], b = ord[u];
-                        const double ka = a < n ? le[a] : -1.0, kb = b < n ? le[b] : -1.0;
+                        // errors are >= 0: their bit patterns order as integers (integer
+                        // compares; FP64 ones run at 1/64 of the FP32 rate)
+                        const long long ka = a < n ? __double_as_longlong(le[a]) : -1ll;
+                        const long long kb = b < n ? __double_as_longlong(le[b]) : -1ll;
                         // descending overall: the first half of each k-block descending
                         const bool desc = (t & k) == 0;
                         if (desc ? (ka < kb || (ka == kb && a > b)) : (ka > kb || (ka == kb && a < b))) {
@@ -589,6 +592,7 @@ struct NbarArgs {
     int Nm;
     double mmin, ln_mratio;  // mass bin = round(log(m / mmin) Nm / ln_mratio)
     double lo, hi;           // integration range in log10 m
+    double inv_hw0;          // 1 / root half-width
     // factors of node n of HOD h at abscissa i: [(h * NBAR_NODES + n) * 15 + i]
     double *fm, *fS;
     int *fmix;
@@ -706,13 +710,15 @@ struct NbarEval {
             double f = 0;
             const double c = live ? bc[r] : 0.0, hw = live ? bh[r] : 1.0;
             if (live && hl < 15) {
-                // node of the region: depth from the exact half-width, index from the
-                // centre (within a few ulp of lo + (2k + 1) hw)
-                const int d = ilogb(hw0) - ilogb(hw);
+                // node of the region: depth from the exponent of the exact half-width
+                // hw0 2^-d, index from the centre (within a few ulp of lo + (2k + 1) hw):
+                // k = floor((c - lo) / (2 hw)) with 1 / (2 hw) = 2^(d-1) / hw0
+                const int d = (int)((__double_as_longlong(hw0) >> 52) & 0x7ff) -
+                              (int)((__double_as_longlong(hw) >> 52) & 0x7ff);
                 double m, S;
                 int mix;
                 if (d >= 0 && d <= NBAR_DEPTH) {
-                    const long long k = (long long)floor((c - A.lo) / (2.0 * hw));
+                    const long long k = (long long)floor((c - A.lo) * ldexp(A.inv_hw0, d - 1));
                     const long long n = (1ll << d) - 1 + k;
                     const size_t q = ((size_t)t.hod * NBAR_NODES + n) * 15 + hl;
                     m = A.fm[q];
@@ -1009,6 +1015,7 @@ int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const dou
         A.ln_mratio = std::log(B.mmax / B.mmin);
         A.lo = lo;
         A.hi = hi;
+        A.inv_hw0 = 1.0 / (0.5 * (hi - lo));
         A.fm = (double *)W.cache;
         A.fS = A.fm + E;
         A.fmix = (int *)(A.fS + E);
