@@ -177,8 +177,10 @@ static __device__ __noinline__ float u_nfw_small64(float kr, float c)
 // NFW profile u(k, m) from kr = k r_200 and c = f conc; a1 = kr / c, a2 = a1 (1 + c),
 // a1 c = kr.  Returns the FP32 value; lanes with a1 < small_arg take the FP64 form.
 // The Si/Ci parts of a1 and a2 (a1 < a2) come from one loop body, small-argument form
-// below 4 and auxiliary functions f, g above, so the code holds each form once.
-__device__ __forceinline__ float u_nfw32(float kr, float c, float small_arg, int &small_hits)
+// below 4 and auxiliary functions f, g above, so the code holds each form once; and the
+// function is one out-of-line copy for all its call sites.  The rule kernels are bound by
+// instruction fetch, not by the call: measured 5-15% faster than inlined.
+static __device__ __noinline__ float u_nfw32(float kr, float c, float small_arg, int &small_hits)
 {
     if (!(kr > 0.f)) return 1.f;  // k -> 0 limit of the profile
     const float opc = 1.f + c;
@@ -562,11 +564,8 @@ struct ModelF {
                 const int kx3 = kidx_k3(T, d, C, ch, sdim, vv, zr, k3, false, ties);
                 const float P1 = plin32(T, zr, kx1, k1), P2 = plin32(T, zr, kx2, k2);
                 const float P3 = plin32(T, zr, kx3, k3);
-                const float ra = cbrtf(M1.f[0] * k200), rb = cbrtf(M2.f[0] * k200);
-                const float ca = __ldg(T.f_conc + zt * Nm + M1.i1);
-                const float cb = __ldg(T.f_conc + zt * Nm + M2.i1);
-                const float u3_1 = u_nfw32(k3 * ra, ca, sa, small);
-                const float u3_2 = u_nfw32(k3 * rb, cb, sa, small);
+                float u3_1, u3_2;
+                u3_pair(T, M1, M2, k3, k200, zt, small, u3_1, u3_2);
                 const float u1_1 = uc[0];
                 const float u2_1 = uc[1];
                 const float u1_2 = uc[2];
@@ -614,13 +613,10 @@ struct ModelF {
                 const int kx3 = kidx_k3(T, d, C, ch, sdim, vv, zr, k3, false, ties);
                 const float P1 = plin32(T, zr, kx1, k1), P2 = plin32(T, zr, kx2, k2);
                 const float P3 = plin32(T, zr, kx3, k3);
-                const float ra = cbrtf(M1.f[0] * k200), rb = cbrtf(M2.f[0] * k200);
-                const float ca = __ldg(T.f_conc + zt * Nm + M1.i1);
-                const float cb = __ldg(T.f_conc + zt * Nm + M2.i1);
+                float u3_1, u3_2;
+                u3_pair(T, M1, M2, k3, k200, zt, small, u3_1, u3_2);
                 const float u2_1 = uc[0];
-                const float u3_2 = u_nfw32(k3 * rb, cb, sa, small);
                 const float u1_2f = uc[1];
-                const float u3_1 = u_nfw32(k3 * ra, ca, sa, small);
                 const float u2_2 = uc[2];
                 const float u1_1f = uc[3];
                 const float G2 = M2.f[1] + M2.f[2] * u1_2f, G1 = M1.f[1] + M1.f[2] * u1_1f;
@@ -649,6 +645,25 @@ struct ModelF {
                 return A12 * U3 * Z.f[0] * HB * u2_1 * u3_2 * G * Bi;
             }
         }
+    }
+
+    // u_NFW(k3 r_200(m_a), c(m_a)) for the two masses of a 2-halo point, through one call
+    // site (a single copy of u_nfw32 in the kernel's hot loop)
+    __device__ static void u3_pair(const DevTables &T, const SlotF &M1, const SlotF &M2,
+                                   float k3, float k200, int zt, int &small, float &u1, float &u2)
+    {
+        float u[2];
+#pragma unroll 1
+        for (int q = 0; q < 2; ++q) {
+            const SlotF &M = q ? M2 : M1;
+            const float r = cbrtf(M.f[0] * k200);
+            const float c = __ldg(T.f_conc + zt * T.Nm + M.i1);
+            const float v = u_nfw32(k3 * r, c, T.small_arg, small);
+            if (q == 0) u[0] = v;
+            else u[1] = v;
+        }
+        u1 = u[0];
+        u2 = u[1];
     }
 
     // tree-level bispectrum (src/generalFunctions.cu:94-147), scaled by the P_lin scale^2;
