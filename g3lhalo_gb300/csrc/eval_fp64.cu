@@ -70,9 +70,24 @@ struct Model64 {
         return u_nfw64(k, r, c, fs == 0 ? 1.0 : (fs == 1 ? T.hod[6 * d.hod1] : T.hod[6 * d.hod2]));
     }
 
-    // uc: the cached u_NFW values of this point (ucache_fun order), or null
+    // u_NFW(k3, mass u3_mass(f)) of the 2- and 3-halo terms, with the expressions of
+    // point(): shared by the points with the same projection (u3_drop)
+    __device__ static double u3(const DevTables &T, int f, const Slot64 *const *s)
+    {
+        const Slot64 &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
+        const Slot64 &M = *s[u3_mass(KIND, TERM, f)];
+        const double l1 = L1.a[0], l2 = L2.a[0], cphi = PH.a[0];
+        const double w_ = __ldg(T.w + Z.i0);
+        const double l3 = sqrt(l1 * l1 + l2 * l2 + 2 * l1 * l2 * cphi);
+        const double k3 = l3 / w_;
+        const double rhot = __ldg(T.rho_bar + Z.i1);
+        return u_nfw64(k3, r200_64(M.a[0], rhot), __ldg(T.conc + Z.i1 * T.Nm + M.i1), 1);
+    }
+
+    // uc: the cached u_NFW values of this point (ucache_fun order), or null; u3c: its
+    // cached u_NFW at k3 (u3()), or null
     __device__ static double point(const DevTables &T, const IntDesc &d, const Slot64 *const *s,
-                                   const double *uc = nullptr)
+                                   const double *uc = nullptr, const double *u3c = nullptr)
     {
         const Slot64 &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
         const double l1 = L1.a[0], l2 = L2.a[0], cphi = PH.a[0], z = Z.a[0];
@@ -114,8 +129,8 @@ struct Model64 {
                 const double ra = r200_64(m1, rhot), rb = r200_64(m2, rhot);
                 const double ca = __ldg(T.conc + z_it * Nm + M1.i1);
                 const double cb = __ldg(T.conc + z_it * Nm + M2.i1);
-                const double u3_1 = u_nfw64(k3, ra, ca, 1);
-                const double u3_2 = u_nfw64(k3, rb, cb, 1);
+                const double u3_1 = u3c ? u3c[0] : u_nfw64(k3, ra, ca, 1);
+                const double u3_2 = u3c ? u3c[1] : u_nfw64(k3, rb, cb, 1);
                 const double u1_1 = uc ? uc[0] : u_nfw64(k1, ra, ca, f1);
                 const double u2_1 = uc ? uc[1] : u_nfw64(k2, ra, ca, f2);
                 const double u1_2 = uc ? uc[2] : u_nfw64(k1, rb, cb, f1);
@@ -139,7 +154,8 @@ struct Model64 {
                 // src/NNMap_Model.cu:1003-1037
                 const Slot64 &M1 = *s[3], &M2 = *s[4], &M3 = *s[5];
                 const double m1 = M1.a[0], m2 = M2.a[0], m3 = M3.a[0];
-                const double u3 = u_nfw64(k3, r200_64(m3, rhot), __ldg(T.conc + z_it * Nm + M3.i1), 1);
+                const double u3 = u3c ? u3c[0]
+                                      : u_nfw64(k3, r200_64(m3, rhot), __ldg(T.conc + z_it * Nm + M3.i1), 1);
                 const double u1 = uc ? uc[0] : u_nfw64(k1, r200_64(m1, rhot), __ldg(T.conc + z_it * Nm + M1.i1), f1);
                 const double u2 = uc ? uc[1] : u_nfw64(k2, r200_64(m2, rhot), __ldg(T.conc + z_it * Nm + M2.i1), f2);
                 const double Gg1 = M1.a[1] + M1.a[2] * u1;  // hod1 at m1
@@ -180,9 +196,9 @@ struct Model64 {
                 const double ca = __ldg(T.conc + z_it * Nm + M1.i1);
                 const double cb = __ldg(T.conc + z_it * Nm + M2.i1);
                 const double u2_1 = uc ? uc[0] : u_nfw64(k2, ra, ca, 1);
-                const double u3_2 = u_nfw64(k3, rb, cb, 1);
+                const double u3_2 = u3c ? u3c[1] : u_nfw64(k3, rb, cb, 1);
                 const double u1_2f = uc ? uc[1] : u_nfw64(k1, rb, cb, f);
-                const double u3_1 = u_nfw64(k3, ra, ca, 1);
+                const double u3_1 = u3c ? u3c[0] : u_nfw64(k3, ra, ca, 1);
                 const double u2_2 = uc ? uc[2] : u_nfw64(k2, rb, cb, 1);
                 const double u1_1f = uc ? uc[3] : u_nfw64(k1, ra, ca, f);
                 double Bgdd = 1. / nbar / rho / rho * __ldg(T.hmf + z_ix * Nm + M1.i0) *
@@ -205,7 +221,8 @@ struct Model64 {
                               __ldg(T.hmf + z_ix * Nm + M2.i0) * __ldg(T.hmf + z_ix * Nm + M3.i0) *
                               __ldg(T.b_h + z_ix * Nm + M1.i0) * __ldg(T.b_h + z_ix * Nm + M2.i0) *
                               __ldg(T.b_h + z_ix * Nm + M3.i0) * m1 * m2 *
-                              (uc ? uc[0] : u_nfw64(k2, ra, ca, 1)) * u_nfw64(k3, rb, cb, 1) *
+                              (uc ? uc[0] : u_nfw64(k2, ra, ca, 1)) *
+                              (u3c ? u3c[0] : u_nfw64(k3, rb, cb, 1)) *
                               (M3.a[1] + M3.a[2] * (uc ? uc[1] : u_nfw64(k1, rb, cb, f))) *
                               bi_lin64(T, k1, k2, cphi, z_ix);
                 double bgkk = Bgdd / __ldg(T.dwdz + z_ix) * gz * gz * __ldg(T.p1 + z_ix) / w_ / w_ *
@@ -423,6 +440,10 @@ struct Reeval {
     {
         return vals(P) + (long long)P.rcap * 256;
     }
+    __device__ static double *u3v(const Pool &P)  // [rcap][U3_NF_MAX][U3_MAX]
+    {
+        return ucv(P) + (long long)P.rcap * UC_NF_MAX * UC_MAX;
+    }
     __device__ static int count(const Pool &P, const BatchHdr *H)
     {
         const int cap = H->esc_cap[G];
@@ -472,19 +493,45 @@ __global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *_
 {
     using R = Reeval<KIND, TERM>;
     constexpr int NF = ucache_nf(TERM);
+    constexpr int NU3 = u3_nfun(TERM) > 0 ? u3_nfun(TERM) : 1;
     __shared__ uint8_t ucidx[NF * R::NP];
     __shared__ uint16_t ucl[NF * UC_MAX];
     __shared__ int ucn[NF];
     __shared__ uint8_t ucmap[NF * 343];
+    __shared__ uint32_t sdesc[R::NP];
+    __shared__ uint8_t u3rep[NU3 * R::NP];
+    __shared__ uint8_t u3list[NU3 * U3_MAX];
     const int m = R::count(P, H);
     if (m == 0 || !R::UCACHE) return;
     ucache_tables<KIND, TERM>(ucidx, ucl, ucn, ucmap);
+    for (int p = threadIdx.x; p < R::NP; p += blockDim.x) sdesc[p] = point_variants(R::DIM, p);
+    __syncthreads();
+    u3_tables<KIND, TERM>(sdesc, u3rep, u3list, ucmap);  // ucmap is free again
     const int2 *Q = P.esc + H->esc_beg[R::G];
     const Slot64 *SL = R::slots(P);
     double *UC = R::ucv(P);
-    const long long tot = (long long)m * NF * UC_MAX;
+    double *U3C = R::u3v(P);
+    const long long tot1 = (long long)m * NF * UC_MAX;
+    // the k3 u_NFW of each projection (2- and 3-halo terms): after the (l, m, z) ones
+    const long long tot = tot1 + (long long)m * u3_nfun(TERM) * U3_MAX;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
          t += (long long)gridDim.x * blockDim.x) {
+        if (t >= tot1) {
+            const long long t2 = t - tot1;
+            const int k = (int)(t2 / (u3_nfun(TERM) * U3_MAX));
+            const int r = (int)(t2 - (long long)k * u3_nfun(TERM) * U3_MAX);
+            const int f = r / U3_MAX, j = r - f * U3_MAX;
+            const int pr = u3list[f * U3_MAX + j];  // every projection index is used (93)
+            const int2 ent = Q[k];
+            if (!(ent.y >> 30) && pr >= R::NAX) continue;  // split only: axis points
+            const uint32_t vv = sdesc[pr];
+            const Slot64 *base = SL + (long long)k * R::NS;
+            const Slot64 *sp[R::DIM];
+#pragma unroll
+            for (int dd = 0; dd < R::DIM; ++dd) sp[dd] = base + dd * NVAR + ((vv >> (3 * dd)) & 7);
+            U3C[((long long)k * U3_NF_MAX + f) * U3_MAX + j] = Model64<KIND, TERM>::u3(T, f, sp);
+            continue;
+        }
         const int k = (int)(t / (NF * UC_MAX)), r = (int)(t - (long long)k * NF * UC_MAX);
         const int f = r / UC_MAX, j = r - f * UC_MAX;
         if (j >= ucn[f]) continue;
@@ -507,16 +554,21 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
     using R = Reeval<KIND, TERM>;
     constexpr int DIM = R::DIM;
     constexpr int NF = ucache_nf(TERM);
+    constexpr int NU3 = u3_nfun(TERM);
     __shared__ uint32_t sdesc[R::NP];
     __shared__ uint8_t ucidx[NF * R::NP];
     __shared__ uint16_t ucl[NF * UC_MAX];
     __shared__ int ucn[NF];
     __shared__ uint8_t ucmap[NF * 343];
+    __shared__ uint8_t u3rep[(NU3 > 0 ? NU3 : 1) * R::NP];
+    __shared__ uint8_t u3list[(NU3 > 0 ? NU3 : 1) * U3_MAX];
     const int m = R::count(P, H);
     if (m == 0) return;
     for (int p = threadIdx.x; p < R::NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
     if (R::UCACHE) ucache_tables<KIND, TERM>(ucidx, ucl, ucn, ucmap);
     __syncthreads();
+    if (R::UCACHE) u3_tables<KIND, TERM>(sdesc, u3rep, u3list, ucmap);
+    const double *U3C = R::u3v(P);
     const int2 *Q = P.esc + H->esc_beg[R::G];
     const Slot64 *SL = R::slots(P);
     double *VL = R::vals(P);
@@ -539,7 +591,14 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
             for (int f = 0; f < NF; ++f)
                 uc[f] = UC[((long long)k * UC_NF_MAX + f) * UC_MAX + ucidx[f * R::NP + p]];
         }
-        VL[(long long)k * R::NPAD + p] = Model64<KIND, TERM>::point(T, d, sp, R::UCACHE ? uc : nullptr);
+        double u3c[NU3 > 0 ? NU3 : 1];
+        if (R::UCACHE) {
+#pragma unroll
+            for (int f = 0; f < NU3; ++f)
+                u3c[f] = U3C[((long long)k * U3_NF_MAX + f) * U3_MAX + u3rep[f * R::NP + p]];
+        }
+        VL[(long long)k * R::NPAD + p] = Model64<KIND, TERM>::point(
+            T, d, sp, R::UCACHE ? uc : nullptr, (R::UCACHE && NU3 > 0) ? u3c : nullptr);
     }
 }
 

@@ -121,12 +121,31 @@ struct Pool {
     int rcap;
 };
 
+// u_NFW at k3 = |l1 + l2| / w with one halo mass (2- and 3-halo terms) does not depend
+// on the other mass dimensions, so the rule points that differ only there share it:
+// function f (u3_nfun(term) of them) uses mass dimension u3_mass(kind, term, f) and
+// ignores the variant fields u3_drop(kind, term, f) of the point code.  Dropping one of 6
+// or two of 7 dimensions leaves U3_MAX = rule_points(5) = 93 distinct projections.
+constexpr int U3_MAX = 93;
+constexpr int U3_NF_MAX = 2;
+__host__ __device__ constexpr int u3_nfun(int term) { return term == 1 ? 0 : (term == 2 ? 2 : 1); }
+__host__ __device__ constexpr int u3_mass(int kind, int term, int f)
+{
+    return term == 2 ? 3 + f : (kind == 0 ? 5 : 4);
+}
+__host__ __device__ constexpr uint32_t u3_drop(int kind, int term, int f)
+{
+    return term == 2 ? (7u << (3 * (4 - f)))
+                     : (kind == 0 ? ((7u << 9) | (7u << 12)) : ((7u << 9) | (7u << 15)));
+}
+
 // Bytes of re-evaluation scratch per group for rcap entries (any term).
 constexpr long long reeval_slot_bytes = 56;  // sizeof(Slot64)
 __host__ __device__ constexpr long long reeval_scratch_group_bytes(int rcap)
 {
     return ((long long)rcap * MAX_DIM * NVAR * reeval_slot_bytes + 255) / 256 * 256 +
-           (long long)rcap * 256 * 8 + (long long)rcap * UC_NF_MAX * UC_MAX * 8;
+           (long long)rcap * 256 * 8 + (long long)rcap * UC_NF_MAX * UC_MAX * 8 +
+           (long long)rcap * U3_NF_MAX * U3_MAX * 8;
 }
 
 // Per-call header kept in device memory so one instantiated graph serves any batch.
@@ -293,6 +312,46 @@ __device__ inline void ucache_tables(uint8_t *ucidx, uint16_t *ucl, int *ucn, ui
         ucidx[t] = map[f * 343 + (k & 7) + 7 * (((k >> 3) & 7) + 7 * (k >> 6))];
     }
     __syncthreads();
+}
+
+// Projection tables of the k3 u_NFW (u3_drop): u3rep[f][p] is the projection of point p,
+// numbered in order of first occurrence, u3list[f][j] the first point of projection j.
+// Block-cooperative (every thread calls it; it synchronises); sdesc holds the point
+// codes (point_variants); tmp: 2 NP bytes of shared scratch.
+template <int KIND, int TERM>
+__device__ inline void u3_tables(const uint32_t *sdesc, uint8_t *u3rep, uint8_t *u3list,
+                                 uint8_t *tmp)
+{
+    constexpr int NP = rule_points(TERM + 4);
+    for (int f = 0; f < u3_nfun(TERM); ++f) {
+        const uint32_t keep = ~u3_drop(KIND, TERM, f);
+        uint8_t *first = tmp, *cidx = tmp + NP;
+        for (int p = threadIdx.x; p < NP; p += blockDim.x) {
+            const uint32_t key = sdesc[p] & keep;
+            int q = 0;
+            while (q < p && (sdesc[q] & keep) != key) ++q;
+            first[p] = (uint8_t)q;
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {  // number the projections in point order
+            const int lane = threadIdx.x;
+            int base = 0;
+            for (int c = 0; c < NP; c += 32) {
+                const int q = c + lane;
+                const bool on = q < NP && first[q] == q;
+                const unsigned b = __ballot_sync(0xffffffffu, on);
+                const int idx = base + __popc(b & ((1u << lane) - 1u));
+                if (on && idx < U3_MAX) {
+                    cidx[q] = (uint8_t)idx;
+                    u3list[f * U3_MAX + idx] = (uint8_t)q;
+                }
+                base += __popc(b);
+            }
+        }
+        __syncthreads();
+        for (int p = threadIdx.x; p < NP; p += blockDim.x) u3rep[f * NP + p] = cidx[first[p]];
+        __syncthreads();
+    }
 }
 
 }  // namespace g3l
