@@ -47,27 +47,25 @@ sys.path.insert(0, ROOT)
 METRIC = "NNMap evals/s (220 triplets,1h+2h+3h,rtol 1e-4) mixed vs FP64; p50/p99 ms"
 MAX_EVAL = 1_000_000
 RTOL = 1e-4
-# FP32 operations per integrand point of the NNMap 2-halo rule, counted by ncu
-# (thread-level fadd + fmul + 2 ffma over every launch of an evaluation, divided by its
-# points).  Algorithmic count: the integrand with its u_NFW calls de-duplicated within
-# a point, as the kernel evaluated it before sharing u_NFW across the points of a rule
-# (3.434e11 over 2.2005e8 points of the benchmark).  Executed count of the current
-# kernel, which evaluates the (l, m, z) u_NFW once per rule: 8.728e9 over 2 x 4,802,568
-# points of a 24-triplet, maxEval 2e5 case.  DRAM traffic per launch (read + write): the
-# mean over all 58 launches of two evaluations of the benchmark (one-pass capture).
+# FP32 operations per integrand point of the NNMap 2-halo rule (algorithmic): the
+# integrand with its u_NFW calls de-duplicated within a point, counted by ncu as thread-
+# level fadd + fmul + 2 ffma on the kernel version that evaluated every u_NFW per point
+# (3.434e11 over 2.2005e8 points of the benchmark).  DRAM traffic per launch (read +
+# write): three launches of the kernel on the 110-triplet case (7.3 MB per ms of kernel
+# time), scaled by duration to the benchmark's mean launch (18.55 ms / 28 launches);
+# profiles/k_evalmx_nnmap2h.md.
 FLOPS_PER_POINT = {"nnmap_2h": 1561.0}
-EXECUTED_FLOPS_PER_POINT = {"nnmap_2h": 909.0}
-DRAM_BYTES_PER_LAUNCH = {"nnmap_2h": 5.04e6}
-# Pipe utilisation (% of peak while the SMs are active) of the dominant kernels.  The
-# FP32 rule kernel: fma, alu, issue and warps active time-weighted over all launches of
-# the full workload (one-pass captures), xu and fp64 from one `ncu --set full` launch of
-# the small case; the others from one `--set full` launch each (the commands and the
-# captures are summarised in profiles/k_evalmx_nnmap2h.md, profiles/k_re_points_nnmap3h.md
-# and profiles/k_pc_integrate_precompute.md).
+DRAM_BYTES_PER_LAUNCH = {"nnmap_2h": 4.9e6}
+# Pipe utilisation (% of peak while the SMs are active) of the dominant kernels, from one
+# `ncu --set full` capture of three launches each (profiles/k_evalmx_nnmap2h.md,
+# profiles/k_re_points_nnmap3h.md, profiles/k_nbar_densities.md,
+# profiles/k_pc_integrate_precompute.md).
 PIPES_NCU = {
-    "k_evalmx<NNMap,2h> (FP32 rule)": {"fma": 25.6, "alu": 22.8, "xu_mufu": 4.0, "fp64": 2.6,
-                                       "issue_active": 45.4, "warps_active": 47.0},
-    "k_re_points<NNMap,3h> (FP64 re-evaluation)": {"fp64": 67.3},
+    "k_evalmx<NNMap,2h> (FP32 rule)": {"fma": 36.3, "alu": 35.3, "xu_mufu": 7.9, "fp64": 8.6,
+                                       "issue_active": 66.8, "warps_active": 34.1},
+    "k_re_ucache<NNMap,2h> (FP64 re-evaluation, u_NFW)": {"fp64": 72.4},
+    "k_re_points<NNMap,3h> (FP64 re-evaluation, points)": {"fp64": 49.8},
+    "k_nbar (n_bar integrals)": {"fp64": 65.1},
     "k_pc_integrate (table precompute)": {"fp64": 79.2, "fma": 0.5, "xu_mufu": 0.1},
 }
 
@@ -613,11 +611,9 @@ def main():
             ach = pts_g * fpp / (ms_g * 1e-3) / 1e12
             out["roofline"] = {"bound": "fp32", "achieved": ach, "peak": p32, "unit": "TFLOP/s",
                                "frac": ach / p32, "traffic": DRAM_BYTES_PER_LAUNCH["nnmap_2h"],
-                               "traffic_unit": "bytes per launch (ncu dram read+write)",
+                               "traffic_unit": "bytes per launch (ncu dram read+write, 110-triplet "
+                                               "case scaled by duration)",
                                "flops_per_point": fpp,
-                               "executed_flops_per_point": EXECUTED_FLOPS_PER_POINT["nnmap_2h"],
-                               "executed_tflops": pts_g * EXECUTED_FLOPS_PER_POINT["nnmap_2h"] /
-                                                  (ms_g * 1e-3) / 1e12,
                                "peak_source": "measured FP32 FMA rate of this device "
                                               "(g3l_measure_peaks, CUDA events); the measured-peaks "
                                               "file holds only HBM and bf16 figures",
