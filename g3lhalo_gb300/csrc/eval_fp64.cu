@@ -39,14 +39,19 @@ struct Model64 {
             m_index(T, x, m, S.i0, S.i1, ties);
             const double *h1 = T.hod + 6 * d.hod1;
             const double *h2 = T.hod + 6 * d.hod2;
-            S.a[1] = ncen64(h1, m);
-            S.a[2] = nsat64(h1, m);
+            occupations64(h1, m, S.a[1], S.a[2]);
             if (KIND == 0) {
-                S.a[3] = ncen64(h2, m);
-                S.a[4] = nsat64(h2, m);
+                // the second population's occupations: the same values as the first's when
+                // the slots are the same
+                if (d.same) {
+                    S.a[3] = S.a[1];
+                    S.a[4] = S.a[2];
+                } else {
+                    occupations64(h2, m, S.a[3], S.a[4]);
+                }
                 // rescaling s of the hod1 slot at this mass's rounded bin
                 // (src/NNMap_Model.cu:563,808)
-                S.a[5] = nsatnsat64(h1, h2, d.same, T.A, T.eps, m,
+                S.a[5] = nsatnsat64(S.a[2], S.a[4], d.same, T.A, T.eps, m,
                                     __ldg(T.scale + (size_t)d.hod1 * T.Nm + S.i0));
             }
         } else {  // z

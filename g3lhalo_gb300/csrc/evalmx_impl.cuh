@@ -431,17 +431,28 @@ struct ModelF {
             // occupations (src/HOD.cu:35-76) from log10 m; hodp = {f, alpha, log10 Mth (df),
             // ln10 / (sigma 1.414213562), log10 M' (df), beta}.  erfc keeps 1 + erf accurate
             // far below the threshold mass.
-            const float *h1 = T.f_hodp + 8 * d.hod1;
+            // one loop body for the populations (NNMap: hod1 and hod2; the same values
+            // when they are one slot), so the erfc and exp10 code is held once
             const float xm = x.hi + x.lo;
-            const float e1 = erfcf(-((x.hi - h1[2]) + (x.lo - h1[3])) * h1[4]);
-            S.f[1] = 0.5f * h1[1] * e1;
-            S.f[2] = 0.5f * e1 * exp10f(h1[7] * ((x.hi - h1[5]) + (x.lo - h1[6])));
+            const int npop = (KIND == 0 && !d.same) ? 2 : 1;
+#pragma unroll 1
+            for (int q = 0; q < npop; ++q) {
+                const float *h = T.f_hodp + 8 * (q ? d.hod2 : d.hod1);
+                const float e = erfcf(-((x.hi - h[2]) + (x.lo - h[3])) * h[4]);
+                const float nc = 0.5f * h[1] * e;
+                const float ns = 0.5f * e * exp10f(h[7] * ((x.hi - h[5]) + (x.lo - h[6])));
+                if (q == 0) {
+                    S.f[1] = nc;
+                    S.f[2] = ns;
+                } else {
+                    S.f[3] = nc;
+                    S.f[4] = ns;
+                }
+            }
             if (KIND == 0) {
-                const float *h2 = T.f_hodp + 8 * d.hod2;
-                const float e2 = erfcf(-((x.hi - h2[2]) + (x.lo - h2[3])) * h2[4]);
-                S.f[3] = 0.5f * h2[1] * e2;
-                S.f[4] = 0.5f * e2 * exp10f(h2[7] * ((x.hi - h2[5]) + (x.lo - h2[6])));
-                if (d.same) {  // (N_s + s^2 - 1) N_s, s^2 - 1 per slot and mass bin
+                if (d.same) {
+                    S.f[3] = S.f[1];
+                    S.f[4] = S.f[2];  // (N_s + s^2 - 1) N_s, s^2 - 1 per slot and mass bin
                     S.f[5] = (S.f[2] + __ldg(T.f_scale + d.hod1 * T.Nm + ir)) * S.f[2];
                 } else {
                     float n12 = S.f[2] * S.f[4];
@@ -559,10 +570,9 @@ struct ModelF {
                 return A12 * U3 * Z.f[0] * (H * M.f[0] * M.f[0]) * u3 * Ggg;
             } else if (TERM == 2) {
                 const SlotF &M1 = *s[3], &M2 = *s[4];
-                const int kx1 = kidx_l(T, d, C, ch, sdim, vv, 0, L1, zr, ties);
-                const int kx2 = kidx_l(T, d, C, ch, sdim, vv, 1, L2, zr, ties);
                 const int kx3 = kidx_k3(T, d, C, ch, sdim, vv, zr, k3, false, ties);
-                const float P1 = plin32(T, zr, kx1, k1), P2 = plin32(T, zr, kx2, k2);
+                float P1, P2;
+                plin_l12(T, d, C, ch, sdim, vv, L1, L2, zr, k1, k2, ties, P1, P2);
                 const float P3 = plin32(T, zr, kx3, k3);
                 float u3_1, u3_2;
                 u3_pair(T, M1, M2, k3, k200, zt, small, u3_1, u3_2);
@@ -608,10 +618,9 @@ struct ModelF {
                 return A12 * U3 * Z.f[0] * (__ldg(T.f_hmf + zr * Nm + M.i0) * m * m * m) * G * u2 * u3;
             } else if (TERM == 2) {
                 const SlotF &M1 = *s[3], &M2 = *s[4];
-                const int kx1 = kidx_l(T, d, C, ch, sdim, vv, 0, L1, zr, ties);
-                const int kx2 = kidx_l(T, d, C, ch, sdim, vv, 1, L2, zr, ties);
                 const int kx3 = kidx_k3(T, d, C, ch, sdim, vv, zr, k3, false, ties);
-                const float P1 = plin32(T, zr, kx1, k1), P2 = plin32(T, zr, kx2, k2);
+                float P1, P2;
+                plin_l12(T, d, C, ch, sdim, vv, L1, L2, zr, k1, k2, ties, P1, P2);
                 const float P3 = plin32(T, zr, kx3, k3);
                 float u3_1, u3_2;
                 u3_pair(T, M1, M2, k3, k200, zt, small, u3_1, u3_2);
@@ -647,6 +656,25 @@ struct ModelF {
         }
     }
 
+    // P_lin at k1 = l1 / w and k2 = l2 / w with their exact-on-a-boundary indices, through
+    // one copy of the index code
+    __device__ static void plin_l12(const DevTables &T, const IntDesc &d, const Child &C, int ch,
+                                    int sdim, uint32_t vv, const SlotF &L1, const SlotF &L2,
+                                    int zr, float k1, float k2, unsigned &ties, float &P1,
+                                    float &P2)
+    {
+        float P[2];
+#pragma unroll 1
+        for (int q = 0; q < 2; ++q) {
+            const int kx = kidx_l(T, d, C, ch, sdim, vv, q, q ? L2 : L1, zr, ties);
+            const float v = plin32(T, zr, kx, q ? k2 : k1);
+            if (q == 0) P[0] = v;
+            else P[1] = v;
+        }
+        P1 = P[0];
+        P2 = P[1];
+    }
+
     // u_NFW(k3 r_200(m_a), c(m_a)) for the two masses of a 2-halo point, through one call
     // site (a single copy of u_nfw32 in the kernel's hot loop)
     __device__ static void u3_pair(const DevTables &T, const SlotF &M1, const SlotF &M2,
@@ -675,10 +703,9 @@ struct ModelF {
     {
         const float c13 = -(k1 + k2 * cphi) / k3;
         const float c23 = -(k2 + k1 * cphi) / k3;
-        const int kx1 = kidx_l(T, d, C, ch, sdim, vv, 0, L1, zr, ties);
-        const int kx2 = kidx_l(T, d, C, ch, sdim, vv, 1, L2, zr, ties);
         const int kx3 = kidx_k3(T, d, C, ch, sdim, vv, zr, k3, true, ties);
-        const float P1 = plin32(T, zr, kx1, k1), P2 = plin32(T, zr, kx2, k2);
+        float P1, P2;
+        plin_l12(T, d, C, ch, sdim, vv, L1, L2, zr, k1, k2, ties, P1, P2);
         const float P3 = plin32(T, zr, kx3, k3);
         const float F12 = 0.7143f + 0.2857f * cphi * cphi + 0.5f * cphi * (k1 / k2 + 1.f);
         const float F13 = 0.7143f + 0.2857f * c13 * c13 + 0.5f * c13 * (k1 / k3 + 1.f);

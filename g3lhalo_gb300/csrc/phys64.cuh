@@ -129,22 +129,22 @@ __device__ __forceinline__ double aperture64(double eta)
 }
 
 // hod = {f, alpha, Mth, sigma, M', beta}
-__device__ __forceinline__ double nsat64(const double *h, double m)
+// N_c and N_s of one HOD at mass m from one evaluation of their common factor
+// 1 + erf(ln(m/Mth) / (sigma sqrt 2)) (the reference evaluates it in each, src/HOD.cu:35-76;
+// the same expression, so the same values)
+__device__ __forceinline__ void occupations64(const double *h, double m, double &nc, double &ns)
 {
-    return 0.5 * (1 + erf(log(m / h[2]) / h[3] / 1.414213562)) * pow(m / h[4], h[5]);
+    const double e1 = 1 + erf(log(m / h[2]) / h[3] / 1.414213562);
+    nc = 0.5 * h[1] * e1;
+    ns = 0.5 * e1 * pow(m / h[4], h[5]);
 }
-__device__ __forceinline__ double ncen64(const double *h, double m)
-{
-    return 0.5 * h[1] * (1 + erf(log(m / h[2]) / h[3] / 1.414213562));
-}
+// NsatNsat from the two satellite occupations Ns1 (hod1) and Ns2 (hod2) at m, the
+// reference's expression (src/HOD.cu:78-94) with its nsat calls' values passed in;
 // scale1: satellite-variance rescaling (1 = none); the reference reads scale1 only
-// (src/HOD.cu:78-94)
-__device__ __forceinline__ double nsatnsat64(const double *h1, const double *h2, int same,
-                                             double A, double eps, double m, double scale1)
+__device__ __forceinline__ double nsatnsat64(double Ns1, double Ns2, int same, double A,
+                                             double eps, double m, double scale1)
 {
-    double Ns1 = nsat64(h1, m);
     if (same) return (Ns1 + scale1 * scale1 - 1) * Ns1;
-    double Ns2 = nsat64(h2, m);
     double result = Ns1 * Ns2 + A * pow(m, eps) * sqrt(Ns1 * Ns2);
     if (result < 0) return 0;
     return result;
