@@ -972,8 +972,8 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
     __syncwarp();
 }
 
-// MINB: the blocks per SM the register budget is cut for (4: 128 registers per thread,
-// 6: 80, 8: 64); the autotuner picks it per kind x term.
+// MINB: the blocks per SM the register budget is cut for (6: 80 registers per thread,
+// 7: 72, 8: 64); the autotuner picks it per kind x term.
 template <int KIND, int TERM, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_evalmx(DevTables T, const IntDesc *__restrict__ D,
                                                 IntState *__restrict__ S, Pool P, BatchHdr *H,

@@ -1269,8 +1269,8 @@ try {
     c->opt.unc_thr = 0.1;
     c->opt.unc_tau_thr = 1e-6;
     // register-budget variant of the rule kernels per kind x term (autotuned default:
-    // 6 blocks per SM for the 1- and 2-halo terms, 8 for the 3-halo terms)
-    for (int g = 0; g < NGROUPS; ++g) c->opt.evalmx_variant[g] = g % 3 == 2 ? 2 : 1;
+    // 8 blocks per SM for the 1-halo terms, 6 for the 2- and 3-halo terms)
+    for (int g = 0; g < NGROUPS; ++g) c->opt.evalmx_variant[g] = g % 3 == 0 ? 2 : 1;
 
     DevTables &T = c->T;
     T.Nz = t->Nz;

@@ -228,8 +228,8 @@ typedef struct g3l_options {
      * (split decisions use unc_eps_rel). */
     double unc_eps_sel;
     /* Register budget of the mixed-precision rule kernel per kind x term
-     * (kind * 3 + term - 1): 0, 1, 2 = 4, 6, 8 blocks per SM (128, 80, 64 registers
-     * per thread).  Set by g3l_autotune; default 1 for the 1- and 2-halo terms, 2 for the
+     * (kind * 3 + term - 1): 0, 1, 2 = 7, 6, 8 blocks per SM (72, 80, 64 registers
+     * per thread).  Set by g3l_autotune; default 2 for the 1-halo terms, 1 for the 2- and
      * 3-halo terms. */
     int evalmx_variant[6];
     /* Deadline of a g3l_eval / g3l_eval_terms / g3l_eval_static call in milliseconds,
