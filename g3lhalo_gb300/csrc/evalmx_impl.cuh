@@ -165,11 +165,9 @@ static __device__ __noinline__ float u_nfw_small64(float kr, float c)
     const double cd = (double)c;
     const double a1d = (double)kr / cd;
     const double a2d = a1d * (1 + cd);
-    double si1, ci1, si2, ci2;
-    sici64(a1d, si1, ci1);
+    double si1, ci1, si2, ci2, s1, c1;
+    sici64_sc(a1d, si1, ci1, s1, c1);
     sici64(a2d, si2, ci2);
-    double s1, c1;
-    sincos(a1d, &s1, &c1);
     double num = s1 * (si2 - si1) + c1 * (ci2 - ci1) - sin(a1d * cd) / a2d;
     return (float)(num / (log(1. + cd) - cd / (1. + cd)));
 }

@@ -17,7 +17,9 @@
 
 namespace g3l {
 
-__device__ __forceinline__ void sici64(double x, double &si, double &ci)
+// Si(x), Ci(x); sx, cx receive sin(x), cos(x) (the large-argument branch needs them; the
+// small one computes them for the caller, so that u_NFW evaluates them once)
+__device__ __forceinline__ void sici64_sc(double x, double &si, double &ci, double &sx, double &cx)
 {
     double x2 = x * x;
     double x4 = x2 * x2;
@@ -43,6 +45,7 @@ __device__ __forceinline__ void sici64(double x, double &si, double &ci)
             1.38536352772778619e-12 * x10 + 1.89106054713059759e-15 * x12 +
             1.39759616731376855e-18 * x14;
         ci = 0.5772156649 + log(x) + x2 * a / b;
+        sincos(x, &sx, &cx);
     } else {
         // f = (1/x) A(t)/B(t), g = t C(t)/D(t) with t = 1/x^2: the reference's explicit
         // powers of 1/x (src/generalFunctions.cu:65-81) in Horner form, one division for t
@@ -96,7 +99,15 @@ __device__ __forceinline__ void sici64(double x, double &si, double &ci)
         const double g = C / Dd * t;
         si = 0.5 * 3.14159265358979323846 - f * cos_x - g * sin_x;
         ci = f * sin_x - g * cos_x;
+        sx = sin_x;
+        cx = cos_x;
     }
+}
+
+__device__ __forceinline__ void sici64(double x, double &si, double &ci)
+{
+    double sx, cx;
+    sici64_sc(x, si, ci, sx, cx);
 }
 
 // NFW Fourier profile given k, r_200 and the tabulated concentration (truncated indices
@@ -106,11 +117,9 @@ __device__ __forceinline__ double u_nfw64(double k, double r200, double conc, do
     double c = f * conc;
     double arg1 = k * r200 / c;
     double arg2 = arg1 * (1 + c);
-    double si1, ci1, si2, ci2;
-    sici64(arg1, si1, ci1);
+    double si1, ci1, si2, ci2, s1, c1;
+    sici64_sc(arg1, si1, ci1, s1, c1);  // s1, c1 = sin(arg1), cos(arg1)
     sici64(arg2, si2, ci2);
-    double s1, c1;
-    sincos(arg1, &s1, &c1);
     double term1 = s1 * (si2 - si1);
     double term2 = c1 * (ci2 - ci1);
     double term3 = -sin(arg1 * c) / arg2;
