@@ -580,6 +580,12 @@ __global__ void __launch_bounds__(PC_THREADS) k_pc_integrate(const PkDev *__rest
 // themselves.  Either way a factor is the same expression of the same abscissa.
 constexpr int NBAR_DEPTH = 12;
 constexpr int NBAR_NODES = (2 << NBAR_DEPTH) - 1;  // depths 0..NBAR_DEPTH
+// Below depth NBAR_DEPTH the refinement follows the mass-bin edges (the nearest-bin
+// lookup makes n(m, z) jump there; elsewhere the integrand is smooth): at every depth the
+// two children of the node that contains an edge.  k_nbar_deep evaluates those, for the
+// Nm - 1 edges and depths NBAR_DEPTH + 1 .. NBAR_DEEP, by the same path arithmetic.
+constexpr int NBAR_DEEP = 44;
+constexpr int NBAR_NDEEP = NBAR_DEEP - NBAR_DEPTH;
 
 struct NbarTask {
     double lo, hi;
@@ -596,9 +602,18 @@ struct NbarArgs {
     // factors of node n of HOD h at abscissa i: [(h * NBAR_NODES + n) * 15 + i]
     double *fm, *fS;
     int *fmix;
+    // deep nodes: edge e (e + 1 = the index whose bin starts there) at x = xm0 + (e + 0.5) dx,
+    // depth NBAR_DEPTH + 1 + dd, side s: entry q = ((h * ne + e) * NBAR_NDEEP + dd) * 2 + s,
+    // its node index at that depth dkey[q], factors [q * 15 + i]
+    double xm0, dx, inv_dx;
+    int ne;
+    long long *dkey;
+    double *dm, *dS;
+    int *dmix;
 };
 
 constexpr size_t kNbarNodeBytes = 15 * (8 + 8 + 4);
+constexpr size_t kNbarDeepBytes = 8 + kNbarNodeBytes;  // key + factors
 
 // N_c + N_s (src/HOD.cu:35-76; erf taken once, the same argument in both) and the
 // nearest mass bin (src/NNMap_Model.cu:556) at x = log10 m
@@ -692,6 +707,44 @@ __device__ __forceinline__ void rule_gk15_hw(double f, int hl, double hw, double
     err = e;
 }
 
+// one thread per (HOD, edge, depth, side, abscissa): walk from the root towards the edge
+// (upper half when the edge is at or above the centre), then take the child on side s
+__global__ void __launch_bounds__(256) k_nbar_deep(NbarArgs A, int nh)
+{
+    const long long total = (long long)nh * A.ne * NBAR_NDEEP * 2 * 15;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % 15);
+        const long long q = t / 15;
+        const int side = (int)(q & 1);
+        const int dd = (int)((q >> 1) % NBAR_NDEEP);
+        const long long he = (q >> 1) / NBAR_NDEEP;
+        const int e = (int)(he % A.ne), h = (int)(he / A.ne);
+        const double xe = A.xm0 + (e + 0.5) * A.dx;
+        const int d = NBAR_DEPTH + 1 + dd;
+        double c = 0.5 * (A.lo + A.hi), hw = 0.5 * (A.hi - A.lo);
+        long long k = 0;
+        for (int l = 1; l < d; ++l) {  // to the depth-(d-1) node containing the edge
+            const double h2 = hw * 0.5;
+            const bool up = xe >= c;
+            c = up ? c + h2 : c - h2;
+            hw = h2;
+            k = 2 * k + (up ? 1 : 0);
+        }
+        const double h2 = hw * 0.5;
+        c = side ? c + h2 : c - h2;
+        hw = h2;
+        k = 2 * k + side;
+        double m, S;
+        int mix;
+        nbar_factors(A, A.hods + 6 * h, gk_point(c, hw, i), m, S, mix);
+        A.dm[t] = m;
+        A.dS[t] = S;
+        A.dmix[t] = mix;
+        if (i == 0) A.dkey[q] = k;
+    }
+}
+
 // The batch of one n_bar integral: one region per half-warp, one point per lane.
 struct NbarEval {
     const NbarArgs &A;
@@ -717,6 +770,7 @@ struct NbarEval {
                               (int)((__double_as_longlong(hw) >> 52) & 0x7ff);
                 double m, S;
                 int mix;
+                bool have = false;
                 if (d >= 0 && d <= NBAR_DEPTH) {
                     const long long k = (long long)floor((c - A.lo) * ldexp(A.inv_hw0, d - 1));
                     const long long n = (1ll << d) - 1 + k;
@@ -724,9 +778,24 @@ struct NbarEval {
                     m = A.fm[q];
                     S = A.fS[q];
                     mix = A.fmix[q];
-                } else {
-                    nbar_factors(A, h, gk_point(c, hw, hl), m, S, mix);
+                    have = true;
+                } else if (d > NBAR_DEPTH && d <= NBAR_DEEP) {
+                    // a node on the path to the nearest mass-bin edge, if it is one
+                    const long long k = (long long)floor((c - A.lo) * ldexp(A.inv_hw0, d - 1));
+                    const int e = (int)floor((c - A.xm0) * A.inv_dx);
+                    if (e >= 0 && e < A.ne) {
+                        const long long q =
+                            (((long long)t.hod * A.ne + e) * NBAR_NDEEP + (d - NBAR_DEPTH - 1)) * 2 +
+                            (k & 1);
+                        if (A.dkey[q] == k) {
+                            m = A.dm[q * 15 + hl];
+                            S = A.dS[q * 15 + hl];
+                            mix = A.dmix[q * 15 + hl];
+                            have = true;
+                        }
+                    }
                 }
+                if (!have) nbar_factors(A, h, gk_point(c, hw, hl), m, S, mix);
                 f = m * row[mix] * S;  // src/generalFunctions.cu:233-245
             }
             double v, e;
@@ -1003,7 +1072,10 @@ int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const dou
             W.cache = nullptr;
             W.nhod_cap = 0;
             PC_CK(cudaMalloc((void **)&W.hods, sizeof(double) * 6 * nk));
-            PC_CK(cudaMalloc(&W.cache, (size_t)nk * NBAR_NODES * kNbarNodeBytes));
+            PC_CK(cudaMalloc(&W.cache, (size_t)nk * (NBAR_NODES * kNbarNodeBytes +
+                                                     (size_t)(B.Nm - 1) * NBAR_NDEEP * 2 *
+                                                         kNbarDeepBytes) +
+                                   8));  // + alignment of the deep keys
             W.nhod_cap = (size_t)nk;
         }
         const size_t E = (size_t)W.nhod_cap * NBAR_NODES * 15;
@@ -1019,6 +1091,16 @@ int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const dou
         A.fm = (double *)W.cache;
         A.fS = A.fm + E;
         A.fmix = (int *)(A.fS + E);
+        // deep nodes along the mass-bin edges
+        A.xm0 = std::log10(B.mmin);
+        A.dx = std::log(B.mmax / B.mmin) / (std::log(10.0) * B.Nm);
+        A.inv_dx = 1 / A.dx;
+        A.ne = B.Nm - 1;
+        const size_t E2 = (size_t)W.nhod_cap * A.ne * NBAR_NDEEP * 2;
+        A.dkey = (long long *)(A.fmix + E + (E & 1));  // 8-byte aligned
+        A.dm = (double *)(A.dkey + E2);
+        A.dS = A.dm + E2 * 15;
+        A.dmix = (int *)(A.dS + E2 * 15);
         PC_CK(cudaMemcpyAsync(W.tasks, tasks.data(), sizeof(NbarTask) * ntask,
                               cudaMemcpyHostToDevice, s));
         PC_CK(cudaMemcpyAsync(W.hods, hods + (size_t)6 * h0, sizeof(double) * 6 * nk,
@@ -1027,6 +1109,10 @@ int n_bar_device(NbarDevice &W, const Binning &B, const double *d_hmf, const dou
             const long long nthr = (long long)nk * NBAR_NODES * 15;
             const int grid = (int)std::min<long long>((nthr + 255) / 256, (long long)nsm * 16);
             k_nbar_factors<<<grid, 256, 0, s>>>(A, nk);
+            PC_CK(cudaGetLastError());
+            const long long nthr2 = (long long)nk * A.ne * NBAR_NDEEP * 2 * 15;
+            const int grid2 = (int)std::min<long long>((nthr2 + 255) / 256, (long long)nsm * 16);
+            if (nthr2 > 0) k_nbar_deep<<<grid2, 256, 0, s>>>(A, nk);
             PC_CK(cudaGetLastError());
         }
         k_nbar<kNbarCapSmall><<<std::min(ntask, nsm * 2), NBAR_THREADS, nbar_smem(kNbarCapSmall), s>>>(
