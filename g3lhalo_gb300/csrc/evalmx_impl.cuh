@@ -540,27 +540,9 @@ struct ModelF {
         return u_nfw32(kx * r, fac, T.small_arg, small);
     }
 
-    // u_NFW at k3 = |l1 + l2| / w with the mass of dimension u3_mass(f) (2- and 3-halo
-    // terms), with the expressions of point(): shared by the points whose coordinates
-    // differ only in the other mass dimensions (u3_drop), so evaluated once per projection
-    static constexpr int NU3 = u3_nfun(TERM);
-    __device__ static float u3(const DevTables &T, int f, const SlotF *const *s, int &small)
-    {
-        const SlotF &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
-        const SlotF &M = *s[u3_mass(KIND, TERM, f)];
-        const float l1 = L1.f[0], l2 = L2.f[0];
-        const float dl = l1 - l2;
-        const float l3 = sqrtf(fmaf(dl, dl, 2.f * l1 * l2 * PH.f[1]));
-        const float k3 = l3 * Z.f[1];
-        const float r = cbrtf(M.f[0] * Z.f[2]);
-        const float c = __ldg(T.f_conc + Z.i1 * T.Nm + M.i1);
-        return u_nfw32(k3 * r, c, T.small_arg, small);
-    }
-
-    // uc: the cached (l, m, z) u_NFW of the point; u3c: its cached k3 u_NFW (u3())
     __device__ static float point(const DevTables &T, const IntDesc &d, const SlotF *const *s,
                                   const Child &C, int ch, int sdim, uint32_t vv, unsigned &ties,
-                                  int &small, const float *uc, const float *u3c)
+                                  int &small, const float *uc)
     {
         const SlotF &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
         const float l1 = L1.f[0], l2 = L2.f[0], cphi = PH.f[0];
@@ -590,7 +572,8 @@ struct ModelF {
                 float P1, P2;
                 plin_l12(T, d, C, ch, sdim, vv, L1, L2, zr, k1, k2, ties, P1, P2);
                 const float P3 = plin32(T, zr, kx3, k3);
-                const float u3_1 = u3c[0], u3_2 = u3c[1];
+                float u3_1, u3_2;
+                u3_pair(T, M1, M2, k3, k200, zt, small, u3_1, u3_2);
                 const float u1_1 = uc[0];
                 const float u2_1 = uc[1];
                 const float u1_2 = uc[2];
@@ -608,7 +591,7 @@ struct ModelF {
             } else {
                 const SlotF &M1 = *s[3], &M2 = *s[4], &M3 = *s[5];
                 const float m1 = M1.f[0], m2 = M2.f[0], m3 = M3.f[0];
-                const float u3 = u3c[0];
+                const float u3 = u_nfw32(k3 * cbrtf(m3 * k200), __ldg(T.f_conc + zt * Nm + M3.i1), sa, small);
                 const float u1 = UC ? uc[0] : u_nfw32(k1 * cbrtf(m1 * k200), f1 * __ldg(T.f_conc + zt * Nm + M1.i1), sa, small);
                 const float u2 = UC ? uc[1] : u_nfw32(k2 * cbrtf(m2 * k200), f2 * __ldg(T.f_conc + zt * Nm + M2.i1), sa, small);
                 const float G1 = M1.f[1] + M1.f[2] * u1, G2 = M2.f[3] + M2.f[4] * u2;
@@ -637,7 +620,8 @@ struct ModelF {
                 float P1, P2;
                 plin_l12(T, d, C, ch, sdim, vv, L1, L2, zr, k1, k2, ties, P1, P2);
                 const float P3 = plin32(T, zr, kx3, k3);
-                const float u3_1 = u3c[0], u3_2 = u3c[1];
+                float u3_1, u3_2;
+                u3_pair(T, M1, M2, k3, k200, zt, small, u3_1, u3_2);
                 const float u2_1 = uc[0];
                 const float u1_2f = uc[1];
                 const float u2_2 = uc[2];
@@ -657,7 +641,7 @@ struct ModelF {
                 const float ca = __ldg(T.f_conc + zt * Nm + M1.i1);
                 const float cb = __ldg(T.f_conc + zt * Nm + M2.i1);
                 const float u2_1 = UC ? uc[0] : u_nfw32(k2 * ra, ca, sa, small);
-                const float u3_2 = u3c[0];
+                const float u3_2 = u_nfw32(k3 * rb, cb, sa, small);
                 const float G = M3.f[1] + M3.f[2] * (UC ? uc[1] : u_nfw32(k1 * rb, f * cb, sa, small));
                 const float Bi = bi32(T, d, C, ch, sdim, vv, zr, k1, k2, k3, cphi, L1, L2, ties);
                 const float HB = (__ldg(T.f_hmf + zr * Nm + M1.i0) * m1 * m1) *
@@ -687,6 +671,25 @@ struct ModelF {
         }
         P1 = P[0];
         P2 = P[1];
+    }
+
+    // u_NFW(k3 r_200(m_a), c(m_a)) for the two masses of a 2-halo point, through one call
+    // site (a single copy of u_nfw32 in the kernel's hot loop)
+    __device__ static void u3_pair(const DevTables &T, const SlotF &M1, const SlotF &M2,
+                                   float k3, float k200, int zt, int &small, float &u1, float &u2)
+    {
+        float u[2];
+#pragma unroll 1
+        for (int q = 0; q < 2; ++q) {
+            const SlotF &M = q ? M2 : M1;
+            const float r = cbrtf(M.f[0] * k200);
+            const float c = __ldg(T.f_conc + zt * T.Nm + M.i1);
+            const float v = u_nfw32(k3 * r, c, T.small_arg, small);
+            if (q == 0) u[0] = v;
+            else u[1] = v;
+        }
+        u1 = u[0];
+        u2 = u[1];
     }
 
     // tree-level bispectrum (src/generalFunctions.cu:94-147), scaled by the P_lin scale^2;
@@ -748,8 +751,7 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
                            const Pool &P, BatchHdr *H, long long pslot, long long qslot, bool cut,
                            SlotF *slots, float *vals, Child &C, const uint32_t *sdesc,
                            unsigned &ties, int &small, const uint8_t *ucidx,
-                           const uint16_t *ucl, const int *ucn, float *ucache,
-                           const uint8_t *u3rep, const uint8_t *u3list, float *u3cache)
+                           const uint16_t *ucl, const int *ucn, float *ucache)
 {
     constexpr int DIM = TERM + 4;
     constexpr int NP = rule_points(DIM);
@@ -817,20 +819,6 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
         ucache[(ch * NF + f) * UC_MAX + j] =
             ModelF<KIND, TERM>::ucached(T, d, f, sl(dl, vl), sl(dm, vm), sl(DIM - 1, vz), small);
     }
-    // u_NFW at k3 of each projection of the rule's points (2- and 3-halo terms), per child
-    constexpr int NU3 = ModelF<KIND, TERM>::NU3;
-    for (int t = lane; NU3 > 0 && t < nchild * NU3 * U3_MAX; t += 32) {
-        const int ch = t / (NU3 * U3_MAX), r = t - ch * NU3 * U3_MAX;
-        const int f = r / U3_MAX, j = r - f * U3_MAX;
-        const uint32_t vv = sdesc[u3list[f * U3_MAX + j]];  // every projection index is used
-        const SlotF *sp[DIM];
-#pragma unroll
-        for (int dd = 0; dd < DIM; ++dd) {
-            const int v = (vv >> (3 * dd)) & 7;
-            sp[dd] = (ch && dd == sdim) ? &slots[DIM * NVAR + v] : &slots[dd * NVAR + v];
-        }
-        u3cache[(ch * U3_NF_MAX + f) * U3_MAX + j] = ModelF<KIND, TERM>::u3(T, f, sp, small);
-    }
     __syncwarp();
     if (ModelF<KIND, TERM>::UC && nchild == 2) {
         for (int t = lane; t < NF * UC_MAX; t += 32) {
@@ -857,11 +845,7 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
 #pragma unroll
             for (int f = 0; f < NF; ++f) uc[f] = ucache[(ch * NF + f) * UC_MAX + ucidx[f * NP + pp]];
         }
-        float u3v[NU3 > 0 ? NU3 : 1];
-#pragma unroll
-        for (int f = 0; f < NU3; ++f)
-            u3v[f] = u3cache[(ch * U3_NF_MAX + f) * U3_MAX + u3rep[f * NP + pp]];
-        vals[p] = ModelF<KIND, TERM>::point(T, d, sp, C, ch, sdim, vv, ties, small, uc, u3v);
+        vals[p] = ModelF<KIND, TERM>::point(T, d, sp, C, ch, sdim, vv, ties, small, uc);
         if (H->dbg) H->dbg[p] = (double)vals[p];
     }
     __syncwarp();
@@ -1019,15 +1003,10 @@ __global__ void __launch_bounds__(128, MINB) k_evalmx(DevTables T, const IntDesc
     __shared__ int ucn[NF];
     __shared__ float ucache[WPB][2 * NF * UC_MAX];
     __shared__ uint8_t ucmap[NF * 343];
-    constexpr int NU3 = ModelF<KIND, TERM>::NU3 > 0 ? ModelF<KIND, TERM>::NU3 : 1;
-    __shared__ uint8_t u3rep[NU3 * NP];       // projection of each point, per function
-    __shared__ uint8_t u3list[NU3 * U3_MAX];  // first point of each projection
-    __shared__ float u3cache[WPB][2 * U3_NF_MAX * U3_MAX];
     if (ModelF<KIND, TERM>::UC) ucache_tables<KIND, TERM>(ucidx, ucl, ucn, ucmap);
     const int g = KIND * 3 + TERM - 1;
     for (int p = threadIdx.x; p < NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
     __syncthreads();
-    u3_tables<KIND, TERM>(sdesc, u3rep, u3list, ucmap);  // ucmap is free again
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gb = H->gbeg[g], ge = H->gbeg[g + 1];
     if (gb >= ge) return;
@@ -1051,7 +1030,7 @@ __global__ void __launch_bounds__(128, MINB) k_evalmx(DevTables T, const IntDesc
         const long long qslot = cut ? d.base + (S[i].nR - S[i].K) + j : -1;
         warp_itemF<KIND, TERM>(T, d, i, S[i].val, P, H, pslot, qslot, cut, sslot[wib],
                                svals[wib], schild[wib], sdesc, ties, small, ucidx, ucl, ucn,
-                               ucache[wib], u3rep, u3list, u3cache[wib]);
+                               ucache[wib]);
     }
     // warp-aggregated diagnostics
     unsigned tw = __reduce_add_sync(0xffffffffu, ties);
