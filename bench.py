@@ -61,11 +61,11 @@ DRAM_BYTES_PER_LAUNCH = {"nnmap_2h": 4.9e6}
 # profiles/k_re_points_nnmap3h.md, profiles/k_nbar_densities.md,
 # profiles/k_pc_integrate_precompute.md).
 PIPES_NCU = {
-    "k_evalmx<NNMap,2h> (FP32 rule)": {"fma": 36.3, "alu": 35.3, "xu_mufu": 7.9, "fp64": 8.6,
-                                       "issue_active": 66.8, "warps_active": 34.1},
-    "k_re_ucache<NNMap,2h> (FP64 re-evaluation, u_NFW)": {"fp64": 72.4},
-    "k_re_points<NNMap,3h> (FP64 re-evaluation, points)": {"fp64": 49.8},
-    "k_nbar (n_bar integrals)": {"fp64": 65.1},
+    "k_evalmx<NNMap,2h> (FP32 rule)": {"fma": 35.2, "alu": 38.1, "xu_mufu": 7.7, "fp64": 8.9,
+                                       "issue_active": 68.2, "warps_active": 33.6},
+    "k_re_ucache<NNMap,2h> (FP64 re-evaluation, u_NFW)": {"fp64": 72.6},
+    "k_re_points<NNMap,3h> (FP64 re-evaluation, points)": {"fp64": 49.6},
+    "k_nbar (n_bar integrals)": {"fp64": 57.7},
     "k_pc_integrate (table precompute)": {"fp64": 79.2, "fma": 0.5, "xu_mufu": 0.1},
 }
 
