@@ -89,10 +89,25 @@ struct Model64 {
         return u_nfw64(k3, r200_64(M.a[0], rhot), __ldg(T.conc + Z.i1 * T.Nm + M.i1), 1);
     }
 
+    // auxiliary function a (aux_dims) with the expressions of point(): the aperture filter
+    // of l3; P_lin at k1, k2, k3 (2-halo); the tree-level bispectrum (3-halo)
+    __device__ static double aux(const DevTables &T, const IntDesc &d, int a, const Slot64 *const *s)
+    {
+        const Slot64 &L1 = *s[0], &L2 = *s[1], &PH = *s[2];
+        const double l1 = L1.a[0], l2 = L2.a[0], cphi = PH.a[0];
+        const double l3 = sqrt(l1 * l1 + l2 * l2 + 2 * l1 * l2 * cphi);
+        if (a == 0) return aperture64(d.theta[2] * l3);
+        const int z_ix = s[DIM - 1]->i0;
+        const double w_ = __ldg(T.w + z_ix);
+        if (TERM == 3) return bi_lin64(T, l1 / w_, l2 / w_, cphi, z_ix);
+        return plin64(T, z_ix, (a == 1 ? l1 : (a == 2 ? l2 : l3)) / w_);
+    }
+
     // uc: the cached u_NFW values of this point (ucache_fun order), or null; u3c: its
-    // cached u_NFW at k3 (u3()), or null
+    // cached u_NFW at k3 (u3()), or null; ax: its cached auxiliary values (aux()), or null
     __device__ static double point(const DevTables &T, const IntDesc &d, const Slot64 *const *s,
-                                   const double *uc = nullptr, const double *u3c = nullptr)
+                                   const double *uc = nullptr, const double *u3c = nullptr,
+                                   const double *ax = nullptr)
     {
         const Slot64 &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
         const double l1 = L1.a[0], l2 = L2.a[0], cphi = PH.a[0], z = Z.a[0];
@@ -105,7 +120,7 @@ struct Model64 {
         const double rho = __ldg(T.rho_bar + z_ix);
         const double rhot = __ldg(T.rho_bar + z_it);
         const double f1 = T.hod[6 * d.hod1];
-        const double U3 = aperture64(d.theta[2] * l3);
+        const double U3 = ax ? ax[0] : aperture64(d.theta[2] * l3);
         if (KIND == 0) {
             const double nbar1 = __ldg(T.nbar + d.hod1 * T.Nz + z_ix);
             const double nbar2 = __ldg(T.nbar + d.hod2 * T.Nz + z_ix);
@@ -128,9 +143,9 @@ struct Model64 {
                 // src/NNMap_Model.cu:787-856
                 const Slot64 &M1 = *s[3], &M2 = *s[4];
                 const double m1 = M1.a[0], m2 = M2.a[0];
-                const double Pk1 = plin64(T, z_ix, k1);
-                const double Pk2 = plin64(T, z_ix, k2);
-                const double Pk3 = plin64(T, z_ix, k3);
+                const double Pk1 = ax ? ax[1] : plin64(T, z_ix, k1);
+                const double Pk2 = ax ? ax[2] : plin64(T, z_ix, k2);
+                const double Pk3 = ax ? ax[3] : plin64(T, z_ix, k3);
                 const double ra = r200_64(m1, rhot), rb = r200_64(m2, rhot);
                 const double ca = __ldg(T.conc + z_it * Nm + M1.i1);
                 const double cb = __ldg(T.conc + z_it * Nm + M2.i1);
@@ -167,7 +182,7 @@ struct Model64 {
                 const double Gg2 = M2.a[3] + M2.a[4] * u2;  // hod2 at m2
                 double Bggd = 1. / nbar1 / nbar2 / rho * __ldg(T.hmf + z_ix * Nm + M1.i0) *
                               __ldg(T.hmf + z_ix * Nm + M2.i0) * __ldg(T.hmf + z_ix * Nm + M3.i0) *
-                              m3 * u3 * Gg1 * Gg2 * bi_lin64(T, k1, k2, cphi, z_ix) *
+                              m3 * u3 * Gg1 * Gg2 * (ax ? ax[1] : bi_lin64(T, k1, k2, cphi, z_ix)) *
                               __ldg(T.b_h + z_ix * Nm + M1.i0) * __ldg(T.b_h + z_ix * Nm + M2.i0) *
                               __ldg(T.b_h + z_ix * Nm + M3.i0);
                 double bggk = Bggd / __ldg(T.dwdz + z_ix) * __ldg(T.g + z_ix) * __ldg(T.p1 + z_ix) *
@@ -194,9 +209,9 @@ struct Model64 {
                 // src/NMapMap_Model.cu:402-468
                 const Slot64 &M1 = *s[3], &M2 = *s[4];
                 const double m1 = M1.a[0], m2 = M2.a[0];
-                const double Pk1 = plin64(T, z_ix, k1);
-                const double Pk2 = plin64(T, z_ix, k2);
-                const double Pk3 = plin64(T, z_ix, k3);
+                const double Pk1 = ax ? ax[1] : plin64(T, z_ix, k1);
+                const double Pk2 = ax ? ax[2] : plin64(T, z_ix, k2);
+                const double Pk3 = ax ? ax[3] : plin64(T, z_ix, k3);
                 const double ra = r200_64(m1, rhot), rb = r200_64(m2, rhot);
                 const double ca = __ldg(T.conc + z_it * Nm + M1.i1);
                 const double cb = __ldg(T.conc + z_it * Nm + M2.i1);
@@ -229,7 +244,7 @@ struct Model64 {
                               (uc ? uc[0] : u_nfw64(k2, ra, ca, 1)) *
                               (u3c ? u3c[0] : u_nfw64(k3, rb, cb, 1)) *
                               (M3.a[1] + M3.a[2] * (uc ? uc[1] : u_nfw64(k1, rb, cb, f))) *
-                              bi_lin64(T, k1, k2, cphi, z_ix);
+                              (ax ? ax[1] : bi_lin64(T, k1, k2, cphi, z_ix));
                 double bgkk = Bgdd / __ldg(T.dwdz + z_ix) * gz * gz * __ldg(T.p1 + z_ix) / w_ / w_ *
                               (1. + z) * (1. + z);
                 return l1 * l2 * m1 * m2 * m3 * l1 * l2 * L1.a[1] * L2.a[1] * U3 * bgkk / nbar;
@@ -449,6 +464,13 @@ struct Reeval {
     {
         return ucv(P) + (long long)P.rcap * UC_NF_MAX * UC_MAX;
     }
+    __device__ static double *auxv(const Pool &P)  // [rcap][AUX_MAX]
+    {
+        return u3v(P) + (long long)P.rcap * U3_NF_MAX * U3_MAX;
+    }
+    // auxiliary values per entry (124 for the 2-halo terms)
+    static constexpr int NAUX = aux_off(TERM, aux_nfun(TERM) - 1) + aux_count(TERM, aux_nfun(TERM) - 1);
+    static_assert(NAUX <= AUX_MAX, "auxiliary projections exceed AUX_MAX");
     __device__ static int count(const Pool &P, const BatchHdr *H)
     {
         const int cap = H->esc_cap[G];
@@ -456,6 +478,56 @@ struct Reeval {
         return n < P.rcap ? n : P.rcap;
     }
 };
+
+// Point tables of a group's re-evaluation passes: the point codes, the (l, m, z)
+// combinations of the cached u_NFW (ucache_tables) and the projections of the k3 u_NFW
+// (u3_tables) and of the auxiliary functions (aux_tables).  The same for every launch, so
+// k_re_tables builds them once per context into P.retab and each block copies them to
+// shared memory (building them per block cost more than the cached work saves).
+template <int KIND, int TERM>
+struct ReTab {
+    static constexpr int DIM = TERM + 4, NP = rule_points(DIM), NF = ucache_nf(TERM);
+    static constexpr int NU3 = u3_nfun(TERM) > 0 ? u3_nfun(TERM) : 1, NA = aux_nfun(TERM);
+    uint32_t sdesc[NP];
+    int ucn[NF];
+    uint16_t ucl[NF * UC_MAX];
+    uint8_t ucidx[NF * NP];
+    uint8_t u3rep[NU3 * NP];
+    uint8_t u3list[NU3 * U3_MAX];
+    uint8_t auxrep[NA * NP];
+    uint8_t auxlist[AUX_MAX];
+};
+
+template <int KIND, int TERM>
+__global__ void __launch_bounds__(128) k_re_tables(unsigned char *out)
+{
+    using RT = ReTab<KIND, TERM>;
+    static_assert(sizeof(RT) <= RETAB_BYTES && sizeof(RT) % 4 == 0, "re-evaluation table size");
+    __shared__ __align__(16) unsigned char buf[sizeof(RT)];
+    __shared__ uint8_t map[RT::NF * 343];
+    RT &t = *reinterpret_cast<RT *>(buf);
+    ucache_tables<KIND, TERM>(t.ucidx, t.ucl, t.ucn, map);
+    for (int p = threadIdx.x; p < RT::NP; p += blockDim.x) t.sdesc[p] = point_variants(RT::DIM, p);
+    __syncthreads();
+    u3_tables<KIND, TERM>(t.sdesc, t.u3rep, t.u3list, map);  // map is free again
+    aux_tables<TERM>(t.sdesc, t.auxrep, t.auxlist, map);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(out + (KIND * 3 + TERM - 1) * RETAB_BYTES);
+    for (int i = threadIdx.x; i < (int)(sizeof(RT) / 4); i += blockDim.x)
+        dst[i] = reinterpret_cast<const uint32_t *>(buf)[i];
+}
+
+// copy group (KIND, TERM)'s tables to shared memory buf (every thread calls it)
+template <int KIND, int TERM>
+__device__ inline const ReTab<KIND, TERM> &load_retab(const Pool &P, unsigned char *buf)
+{
+    using RT = ReTab<KIND, TERM>;
+    const uint32_t *src =
+        reinterpret_cast<const uint32_t *>(P.retab + (KIND * 3 + TERM - 1) * RETAB_BYTES);
+    for (int i = threadIdx.x; i < (int)(sizeof(RT) / 4); i += blockDim.x)
+        reinterpret_cast<uint32_t *>(buf)[i] = __ldg(src + i);
+    __syncthreads();
+    return *reinterpret_cast<const RT *>(buf);
+}
 
 template <int KIND, int TERM>
 __global__ void __launch_bounds__(128) k_re_fill(DevTables T, const IntDesc *__restrict__ D,
@@ -498,29 +570,42 @@ __global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *_
 {
     using R = Reeval<KIND, TERM>;
     constexpr int NF = ucache_nf(TERM);
-    constexpr int NU3 = u3_nfun(TERM) > 0 ? u3_nfun(TERM) : 1;
-    __shared__ uint8_t ucidx[NF * R::NP];
-    __shared__ uint16_t ucl[NF * UC_MAX];
-    __shared__ int ucn[NF];
-    __shared__ uint8_t ucmap[NF * 343];
-    __shared__ uint32_t sdesc[R::NP];
-    __shared__ uint8_t u3rep[NU3 * R::NP];
-    __shared__ uint8_t u3list[NU3 * U3_MAX];
+    __shared__ __align__(16) unsigned char tbuf[sizeof(ReTab<KIND, TERM>)];
     const int m = R::count(P, H);
     if (m == 0 || !R::UCACHE) return;
-    ucache_tables<KIND, TERM>(ucidx, ucl, ucn, ucmap);
-    for (int p = threadIdx.x; p < R::NP; p += blockDim.x) sdesc[p] = point_variants(R::DIM, p);
-    __syncthreads();
-    u3_tables<KIND, TERM>(sdesc, u3rep, u3list, ucmap);  // ucmap is free again
+    const ReTab<KIND, TERM> &tb = load_retab<KIND, TERM>(P, tbuf);
+    const uint32_t *sdesc = tb.sdesc;
+    const uint16_t *ucl = tb.ucl;
+    const int *ucn = tb.ucn;
+    const uint8_t *u3list = tb.u3list, *auxlist = tb.auxlist;
     const int2 *Q = P.esc + H->esc_beg[R::G];
     const Slot64 *SL = R::slots(P);
     double *UC = R::ucv(P);
     double *U3C = R::u3v(P);
+    double *AX = R::auxv(P);
     const long long tot1 = (long long)m * NF * UC_MAX;
     // the k3 u_NFW of each projection (2- and 3-halo terms): after the (l, m, z) ones
-    const long long tot = tot1 + (long long)m * u3_nfun(TERM) * U3_MAX;
+    const long long tot2 = tot1 + (long long)m * u3_nfun(TERM) * U3_MAX;
+    // the auxiliary functions of each projection: last
+    const long long tot = tot2 + (long long)m * R::NAUX;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
          t += (long long)gridDim.x * blockDim.x) {
+        if (t >= tot2) {
+            const long long t3 = t - tot2;
+            const int k = (int)(t3 / R::NAUX), r = (int)(t3 - (long long)k * R::NAUX);
+            int a = 0;
+            while (a + 1 < aux_nfun(TERM) && r >= aux_off(TERM, a + 1)) ++a;
+            const int pr = auxlist[r];
+            const int2 ent = Q[k];
+            if (!(ent.y >> 30) && pr >= R::NAX) continue;  // split only: axis points
+            const uint32_t vv = sdesc[pr];
+            const Slot64 *base = SL + (long long)k * R::NS;
+            const Slot64 *sp[R::DIM];
+#pragma unroll
+            for (int dd = 0; dd < R::DIM; ++dd) sp[dd] = base + dd * NVAR + ((vv >> (3 * dd)) & 7);
+            AX[(long long)k * AUX_MAX + r] = Model64<KIND, TERM>::aux(T, D[ent.x], a, sp);
+            continue;
+        }
         if (t >= tot1) {
             const long long t2 = t - tot1;
             const int k = (int)(t2 / (u3_nfun(TERM) * U3_MAX));
@@ -560,20 +645,15 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
     constexpr int DIM = R::DIM;
     constexpr int NF = ucache_nf(TERM);
     constexpr int NU3 = u3_nfun(TERM);
-    __shared__ uint32_t sdesc[R::NP];
-    __shared__ uint8_t ucidx[NF * R::NP];
-    __shared__ uint16_t ucl[NF * UC_MAX];
-    __shared__ int ucn[NF];
-    __shared__ uint8_t ucmap[NF * 343];
-    __shared__ uint8_t u3rep[(NU3 > 0 ? NU3 : 1) * R::NP];
-    __shared__ uint8_t u3list[(NU3 > 0 ? NU3 : 1) * U3_MAX];
+    constexpr int NA = aux_nfun(TERM);
+    __shared__ __align__(16) unsigned char tbuf[sizeof(ReTab<KIND, TERM>)];
     const int m = R::count(P, H);
     if (m == 0) return;
-    for (int p = threadIdx.x; p < R::NP; p += blockDim.x) sdesc[p] = point_variants(DIM, p);
-    if (R::UCACHE) ucache_tables<KIND, TERM>(ucidx, ucl, ucn, ucmap);
-    __syncthreads();
-    if (R::UCACHE) u3_tables<KIND, TERM>(sdesc, u3rep, u3list, ucmap);
+    const ReTab<KIND, TERM> &tb = load_retab<KIND, TERM>(P, tbuf);
+    const uint32_t *sdesc = tb.sdesc;
+    const uint8_t *ucidx = tb.ucidx, *u3rep = tb.u3rep, *auxrep = tb.auxrep;
     const double *U3C = R::u3v(P);
+    const double *AX = R::auxv(P);
     const int2 *Q = P.esc + H->esc_beg[R::G];
     const Slot64 *SL = R::slots(P);
     double *VL = R::vals(P);
@@ -602,8 +682,15 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
             for (int f = 0; f < NU3; ++f)
                 u3c[f] = U3C[((long long)k * U3_NF_MAX + f) * U3_MAX + u3rep[f * R::NP + p]];
         }
+        double ax[NA];
+        if (R::UCACHE) {
+#pragma unroll
+            for (int a = 0; a < NA; ++a)
+                ax[a] = AX[(long long)k * AUX_MAX + aux_off(TERM, a) + auxrep[a * R::NP + p]];
+        }
         VL[(long long)k * R::NPAD + p] = Model64<KIND, TERM>::point(
-            T, d, sp, R::UCACHE ? uc : nullptr, (R::UCACHE && NU3 > 0) ? u3c : nullptr);
+            T, d, sp, R::UCACHE ? uc : nullptr, (R::UCACHE && NU3 > 0) ? u3c : nullptr,
+            R::UCACHE ? ax : nullptr);
     }
 }
 
@@ -748,13 +835,27 @@ __global__ void __launch_bounds__(128) k_reeval64(DevTables T, const IntDesc *__
     template __global__ void k_re_points<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,   \
                                                 BatchHdr *, const long long *);                  \
     template __global__ void k_re_combine<K, Tm>(DevTables, const IntDesc *, IntState *, Pool,  \
-                                                 BatchHdr *, const long long *);
+                                                 BatchHdr *, const long long *);                 \
+    template __global__ void k_re_tables<K, Tm>(unsigned char *);
 G3L_INST64(0, 1)
 G3L_INST64(0, 2)
 G3L_INST64(0, 3)
 G3L_INST64(1, 1)
 G3L_INST64(1, 2)
 G3L_INST64(1, 3)
+
+// Build the re-evaluation point tables of every group into out (NGROUPS * RETAB_BYTES
+// bytes of device memory), on stream s.
+cudaError_t build_reeval_tables(unsigned char *out, cudaStream_t s)
+{
+    k_re_tables<0, 1><<<1, 128, 0, s>>>(out);
+    k_re_tables<0, 2><<<1, 128, 0, s>>>(out);
+    k_re_tables<0, 3><<<1, 128, 0, s>>>(out);
+    k_re_tables<1, 1><<<1, 128, 0, s>>>(out);
+    k_re_tables<1, 2><<<1, 128, 0, s>>>(out);
+    k_re_tables<1, 3><<<1, 128, 0, s>>>(out);
+    return cudaGetLastError();
+}
 
 // re-evaluation kernels of a group: 0 = fill, 1 = cached u_NFW, 2 = points, 3 = combine,
 // 4 = batched tail

@@ -119,7 +119,11 @@ struct Pool {
     unsigned char *rscr;
     long long rscr_group;   // bytes per group
     int rcap;
+    // the point tables of the re-evaluation passes, RETAB_BYTES per group (built once per
+    // context by k_re_tables)
+    const unsigned char *retab;
 };
+constexpr int RETAB_BYTES = 4096;
 
 // u_NFW at k3 = |l1 + l2| / w with one halo mass (2- and 3-halo terms) does not depend
 // on the other mass dimensions, so the rule points that differ only there share it:
@@ -139,13 +143,45 @@ __host__ __device__ constexpr uint32_t u3_drop(int kind, int term, int f)
                      : (kind == 0 ? ((7u << 9) | (7u << 12)) : ((7u << 9) | (7u << 15)));
 }
 
+// Other quantities of a point that depend on a few of its dimensions only, cached per
+// projection in the FP64 re-evaluation (function a of a term keeps the dimensions
+// aux_dims(term, a), a bit per dimension): the aperture filter of l3 (l1, l2, phi) for
+// every term; P_lin at k1 (l1, z), k2 (l2, z) and k3 (l1, l2, phi, z) for the 2-halo
+// terms; the tree-level bispectrum (l1, l2, phi, z) for the 3-halo terms.  A projection
+// onto k dimensions has rule_points(k) members (33, 17 or 57); function a's values are
+// at [aux_off(term, a), + rule_points(k)) of the entry's AUX_MAX.
+constexpr int AUX_MAX = 128;
+__host__ __device__ constexpr int aux_nfun(int term) { return term == 1 ? 1 : (term == 2 ? 4 : 2); }
+__host__ __device__ constexpr uint32_t aux_dims(int term, int a)
+{
+    return a == 0 ? 7u
+                  : (term == 2 ? (a == 1 ? (1u | (1u << 5)) : a == 2 ? (2u | (1u << 5)) : (7u | (1u << 5)))
+                               : (7u | (1u << 6)));
+}
+__host__ __device__ constexpr int aux_nkept(int term, int a)
+{
+    return a == 0 ? 3 : (term == 2 ? (a == 3 ? 4 : 2) : 4);
+}
+__host__ __device__ constexpr int aux_count(int term, int a) { return rule_points(aux_nkept(term, a)); }
+__host__ __device__ constexpr int aux_off(int term, int a)
+{
+    return a == 0 ? 0 : aux_off(term, a - 1) + aux_count(term, a - 1);
+}
+__host__ __device__ constexpr uint32_t aux_keep(int term, int a)
+{
+    uint32_t k = 0;
+    for (int d = 0; d < MAX_DIM; ++d)
+        if ((aux_dims(term, a) >> d) & 1u) k |= 7u << (3 * d);
+    return k;
+}
+
 // Bytes of re-evaluation scratch per group for rcap entries (any term).
 constexpr long long reeval_slot_bytes = 56;  // sizeof(Slot64)
 __host__ __device__ constexpr long long reeval_scratch_group_bytes(int rcap)
 {
     return ((long long)rcap * MAX_DIM * NVAR * reeval_slot_bytes + 255) / 256 * 256 +
            (long long)rcap * 256 * 8 + (long long)rcap * UC_NF_MAX * UC_MAX * 8 +
-           (long long)rcap * U3_NF_MAX * U3_MAX * 8;
+           (long long)rcap * U3_NF_MAX * U3_MAX * 8 + (long long)rcap * AUX_MAX * 8;
 }
 
 // Per-call header kept in device memory so one instantiated graph serves any batch.
@@ -314,44 +350,62 @@ __device__ inline void ucache_tables(uint8_t *ucidx, uint16_t *ucl, int *ucn, ui
     __syncthreads();
 }
 
-// Projection tables of the k3 u_NFW (u3_drop): u3rep[f][p] is the projection of point p,
-// numbered in order of first occurrence, u3list[f][j] the first point of projection j.
-// Block-cooperative (every thread calls it; it synchronises); sdesc holds the point
-// codes (point_variants); tmp: 2 NP bytes of shared scratch.
+// Projection tables: rep[p] is the projection of point p (its code & keep), numbered in
+// order of first occurrence, list[j] the first point of projection j (at most maxn of
+// them).  Block-cooperative (every thread calls it; it synchronises); sdesc holds the
+// point codes (point_variants); tmp: 2 np bytes of shared scratch.
+__device__ inline void proj_tables(const uint32_t *sdesc, int np, uint32_t keep, uint8_t *rep,
+                                   uint8_t *list, int maxn, uint8_t *tmp)
+{
+    uint8_t *first = tmp, *cidx = tmp + np;
+    for (int p = threadIdx.x; p < np; p += blockDim.x) {
+        const uint32_t key = sdesc[p] & keep;
+        int q = 0;
+        while (q < p && (sdesc[q] & keep) != key) ++q;
+        first[p] = (uint8_t)q;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {  // number the projections in point order
+        const int lane = threadIdx.x;
+        int base = 0;
+        for (int c = 0; c < np; c += 32) {
+            const int q = c + lane;
+            const bool on = q < np && first[q] == q;
+            const unsigned b = __ballot_sync(0xffffffffu, on);
+            const int idx = base + __popc(b & ((1u << lane) - 1u));
+            if (on && idx < maxn) {
+                cidx[q] = (uint8_t)idx;
+                list[idx] = (uint8_t)q;
+            }
+            base += __popc(b);
+        }
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < np; p += blockDim.x) rep[p] = cidx[first[p]];
+    __syncthreads();
+}
+
+// Projection tables of the k3 u_NFW (u3_drop), per function f: u3rep[f][NP], u3list[f][U3_MAX]
 template <int KIND, int TERM>
 __device__ inline void u3_tables(const uint32_t *sdesc, uint8_t *u3rep, uint8_t *u3list,
                                  uint8_t *tmp)
 {
     constexpr int NP = rule_points(TERM + 4);
-    for (int f = 0; f < u3_nfun(TERM); ++f) {
-        const uint32_t keep = ~u3_drop(KIND, TERM, f);
-        uint8_t *first = tmp, *cidx = tmp + NP;
-        for (int p = threadIdx.x; p < NP; p += blockDim.x) {
-            const uint32_t key = sdesc[p] & keep;
-            int q = 0;
-            while (q < p && (sdesc[q] & keep) != key) ++q;
-            first[p] = (uint8_t)q;
-        }
-        __syncthreads();
-        if (threadIdx.x < 32) {  // number the projections in point order
-            const int lane = threadIdx.x;
-            int base = 0;
-            for (int c = 0; c < NP; c += 32) {
-                const int q = c + lane;
-                const bool on = q < NP && first[q] == q;
-                const unsigned b = __ballot_sync(0xffffffffu, on);
-                const int idx = base + __popc(b & ((1u << lane) - 1u));
-                if (on && idx < U3_MAX) {
-                    cidx[q] = (uint8_t)idx;
-                    u3list[f * U3_MAX + idx] = (uint8_t)q;
-                }
-                base += __popc(b);
-            }
-        }
-        __syncthreads();
-        for (int p = threadIdx.x; p < NP; p += blockDim.x) u3rep[f * NP + p] = cidx[first[p]];
-        __syncthreads();
-    }
+    for (int f = 0; f < u3_nfun(TERM); ++f)
+        proj_tables(sdesc, NP, ~u3_drop(KIND, TERM, f), u3rep + f * NP, u3list + f * U3_MAX,
+                    U3_MAX, tmp);
+}
+
+// Projection tables of the auxiliary caches, per function a: auxrep[a][NP] (index within
+// the function's values), auxlist[aux_off(a) + j] (first point of projection j)
+template <int TERM>
+__device__ inline void aux_tables(const uint32_t *sdesc, uint8_t *auxrep, uint8_t *auxlist,
+                                  uint8_t *tmp)
+{
+    constexpr int NP = rule_points(TERM + 4);
+    for (int a = 0; a < aux_nfun(TERM); ++a)
+        proj_tables(sdesc, NP, aux_keep(TERM, a), auxrep + a * NP, auxlist + aux_off(TERM, a),
+                    aux_count(TERM, a), tmp);
 }
 
 }  // namespace g3l

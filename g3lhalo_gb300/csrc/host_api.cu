@@ -34,6 +34,7 @@ namespace g3l {
 void *eval64_kernel(int kind, int term);
 void *reeval64_kernel(int kind, int term);
 void *reeval_phase_kernel(int kind, int term, int phase);
+cudaError_t build_reeval_tables(unsigned char *out, cudaStream_t s);
 void *round_end_kernel();
 void *evalmx_kernel_k0(int term, int variant);
 void *evalmx_kernel_k1(int term, int variant);
@@ -140,6 +141,7 @@ struct g3l_ctx {
     // in-flight cancel of g3l_eval: a host-mapped word the device loop reads once per
     // round; `running` (under run_mu) tells g3l_eval_cancel whether a call is in flight
     int *cancel_h = nullptr, *cancel_d = nullptr;
+    unsigned char *retab_d = nullptr;  // re-evaluation point tables (NGROUPS * RETAB_BYTES)
     std::mutex run_mu;
     bool running = false;
     host::NbarDevice nbw;  // device buffers of the n_bar integrals (g3l_set_hod)
@@ -333,10 +335,11 @@ void free_workspace(Workspace &W)
 }
 
 // Region pools for `pcap` slots and per-integral arrays for `ncap` integrals.
-int alloc_workspace(Workspace &W, int ncap, size_t pcap)
+int alloc_workspace(Workspace &W, int ncap, size_t pcap, const unsigned char *retab)
 {
     free_workspace(W);
     int st = 0;
+    W.P.retab = retab;
     st |= dalloc(&W.P.center, pcap * MAX_DIM);
     st |= dalloc(&W.P.level, pcap * MAX_DIM);
     st |= dalloc(&W.P.val, pcap);
@@ -380,7 +383,7 @@ int ensure_workspace(g3l_ctx *c, int n, size_t pool)
         cudaGraphDestroy(g.graph);
     }
     c->graphs.clear();
-    return alloc_workspace(W, ncap, pcap);
+    return alloc_workspace(W, ncap, pcap, c->retab_d);
 }
 
 void *eval_fn(const g3l_ctx *c, int precision, int group)
@@ -1017,7 +1020,7 @@ int srv_create(g3l_ctx *c, int precision, int per_group, uint64_t pool_regions, 
     v->chunk = chunk;
     int st = G3L_OK;
     if (cudaStreamCreateWithFlags(&v->s, cudaStreamNonBlocking) != cudaSuccess) st = G3L_ERR_CUDA;
-    if (!st) st = alloc_workspace(v->W, v->n, v->pool);
+    if (!st) st = alloc_workspace(v->W, v->n, v->pool, c->retab_d);
     if (!st) st = dalloc(&v->d_new, (size_t)v->n) | dalloc(&v->d_idx, (size_t)v->n);
     if (!st) st = build_graph_ws(c, v->W, precision, (1 << NGROUPS) - 1, false, v->G);
     if (!st) v->graph_ok = true;
@@ -1233,6 +1236,9 @@ try {
     G3L_CK(cudaHostAlloc((void **)&c->cancel_h, 64, cudaHostAllocMapped));
     *c->cancel_h = 0;
     G3L_CK(cudaHostGetDevicePointer((void **)&c->cancel_d, c->cancel_h, 0));
+    G3L_CK(cudaMalloc((void **)&c->retab_d, (size_t)NGROUPS * RETAB_BYTES));
+    G3L_CK(build_reeval_tables(c->retab_d, c->stream));
+    G3L_CK(cudaStreamSynchronize(c->stream));
     c->B = host::Binning{t->Nz, t->Nm, t->Nk, t->zmin, t->zmax, t->mmin, t->mmax, t->kmin, t->kmax};
     c->Om = t->Om;
     c->OL = t->OL;
@@ -1371,6 +1377,7 @@ void g3l_ctx_destroy(g3l_ctx *c)
     for (void *p : c->allocs) cudaFree(p);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     if (c->cancel_h) cudaFreeHost(c->cancel_h);
+    if (c->retab_d) cudaFree(c->retab_d);
     host::free_nbar_device(c->nbw);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -2287,6 +2294,7 @@ int eval_static_locked(g3l_ctx *c, const g3l_integral *items, int n, int precisi
     a.P.key = (double *)(base + L.key);
     a.P.esc = (int2 *)(base + L.esc);
     a.P.rscr = base + L.rscr;
+    a.P.retab = c->retab_d;
     a.P.rcap = kStaticReevalCap;
     a.P.rscr_group = reeval_scratch_group_bytes(kStaticReevalCap);
     a.P.stride = (long long)pool;
