@@ -671,11 +671,13 @@ __global__ void k_init(const IntDesc *__restrict__ D, IntState *__restrict__ S, 
 }
 
 // end of a mixed-precision round: the FP64 re-evaluation queue has been consumed
-__global__ void k_round_end(BatchHdr *H)
+// End of a re-evaluation stage: count and clear the queues of every group (grp < 0) or
+// of group grp alone (the per-group ends of concurrent branches, hence the atomic count)
+__global__ void k_round_end(BatchHdr *H, int grp)
 {
-    for (int g = 0; g < NGROUPS; ++g) {
+    for (int g = grp < 0 ? 0 : grp; g < (grp < 0 ? NGROUPS : grp + 1); ++g) {
         const int n = H->n_esc[g];
-        H->escalated += (unsigned long long)(n < H->esc_cap[g] ? n : H->esc_cap[g]);
+        atomicAdd(&H->escalated, (unsigned long long)(n < H->esc_cap[g] ? n : H->esc_cap[g]));
         H->n_esc[g] = 0;
     }
 }

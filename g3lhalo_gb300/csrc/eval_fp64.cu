@@ -19,6 +19,25 @@ struct Slot64 {
     int i0, i1;
 };
 
+// coordinate variant v (0 c, 1/2 c -+ r2, 3/4 c -+ r4, 5/6 c -+ r5) of centre c, half-width hw
+__device__ __forceinline__ double variant_x(double c, double hw, int v)
+{
+    double x = c;
+    if (v > 0) {
+        double lam = (v <= 2) ? G3L_LAMBDA2 : (v <= 4 ? G3L_LAMBDA4 : G3L_LAMBDA5);
+        double rr = hw * lam;
+        x = (v & 1) ? c - rr : c + rr;
+    }
+    return x;
+}
+
+// truncated z bin of z = x (the z slot's i1, Model64::fill)
+__device__ __forceinline__ int z_trunc64(const DevTables &T, double x)
+{
+    double zr = (x - T.zmin) * T.Nz / (T.zmax - T.zmin);
+    return min(max((int)zr, 0), T.Nz - 1);
+}
+
 template <int KIND, int TERM>
 struct Model64 {
     static constexpr int DIM = TERM + 4;
@@ -64,20 +83,34 @@ struct Model64 {
 
     // Integrand at one point from its variant slots (kernel_function_* of the reference).
     // cached u_NFW f (ucache_fun) at slots L (l), M (mass), Z (z): the expressions of point()
+    // mz: r_200 and F of the (M, Z) pair (MZ_VALS values, k_re_fill), or null
     __device__ static double ucached(const DevTables &T, const IntDesc &d, int f, const Slot64 &L,
-                                     const Slot64 &M, const Slot64 &Z)
+                                     const Slot64 &M, const Slot64 &Z, const double *mz)
     {
         const double w_ = __ldg(T.w + Z.i0);
         const double k = L.a[0] / w_;
-        const double r = r200_64(M.a[0], __ldg(T.rho_bar + Z.i1));
-        const double c = __ldg(T.conc + Z.i1 * T.Nm + M.i1);
+        const double conc = __ldg(T.conc + Z.i1 * T.Nm + M.i1);
         const int fs = ucache_fun(KIND, TERM, f, 2);
-        return u_nfw64(k, r, c, fs == 0 ? 1.0 : (fs == 1 ? T.hod[6 * d.hod1] : T.hod[6 * d.hod2]));
+        const double c = (fs == 0 ? 1.0 : (fs == 1 ? T.hod[6 * d.hod1] : T.hod[6 * d.hod2])) * conc;
+        if (!mz) return u_nfw64_F(k, r200_64(M.a[0], __ldg(T.rho_bar + Z.i1)), c, nfw_norm64(c));
+        return u_nfw64_F(k, mz[0], c, mz[1 + fs]);
+    }
+
+    // r_200 and F at factors 1, f of hod1, f of hod2 (nf of them) of halo mass slot M at
+    // z bin zt, with the expressions of point(): o[0..nf]
+    __device__ static void mz_values(const DevTables &T, const IntDesc &d, const Slot64 &M, int zt,
+                                     int nf, double *o)
+    {
+        const double conc = __ldg(T.conc + zt * T.Nm + M.i1);
+        o[0] = r200_64(M.a[0], __ldg(T.rho_bar + zt));
+        for (int q = 0; q < nf; ++q)
+            o[1 + q] = nfw_norm64((q == 0 ? 1.0 : (q == 1 ? T.hod[6 * d.hod1] : T.hod[6 * d.hod2])) * conc);
     }
 
     // u_NFW(k3, mass u3_mass(f)) of the 2- and 3-halo terms, with the expressions of
     // point(): shared by the points with the same projection (u3_drop)
-    __device__ static double u3(const DevTables &T, int f, const Slot64 *const *s)
+    // mz: r_200 and F of the (mass, z) pair (k_re_fill), or null
+    __device__ static double u3(const DevTables &T, int f, const Slot64 *const *s, const double *mz)
     {
         const Slot64 &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
         const Slot64 &M = *s[u3_mass(KIND, TERM, f)];
@@ -85,8 +118,9 @@ struct Model64 {
         const double w_ = __ldg(T.w + Z.i0);
         const double l3 = sqrt(l1 * l1 + l2 * l2 + 2 * l1 * l2 * cphi);
         const double k3 = l3 / w_;
-        const double rhot = __ldg(T.rho_bar + Z.i1);
-        return u_nfw64(k3, r200_64(M.a[0], rhot), __ldg(T.conc + Z.i1 * T.Nm + M.i1), 1);
+        const double c = 1.0 * __ldg(T.conc + Z.i1 * T.Nm + M.i1);
+        if (!mz) return u_nfw64_F(k3, r200_64(M.a[0], __ldg(T.rho_bar + Z.i1)), c, nfw_norm64(c));
+        return u_nfw64_F(k3, mz[0], c, mz[1]);
     }
 
     // auxiliary function a (aux_dims) with the expressions of point(): the aperture filter
@@ -104,10 +138,11 @@ struct Model64 {
     }
 
     // uc: the cached u_NFW values of this point (ucache_fun order), or null; u3c: its
-    // cached u_NFW at k3 (u3()), or null; ax: its cached auxiliary values (aux()), or null
+    // cached u_NFW at k3 (u3()), or null; ax: its cached auxiliary values (aux()), or null;
+    // mz: r_200 and F of its (mass, z) pair (1-halo terms), or null
     __device__ static double point(const DevTables &T, const IntDesc &d, const Slot64 *const *s,
                                    const double *uc = nullptr, const double *u3c = nullptr,
-                                   const double *ax = nullptr)
+                                   const double *ax = nullptr, const double *mz = nullptr)
     {
         const Slot64 &L1 = *s[0], &L2 = *s[1], &PH = *s[2], &Z = *s[DIM - 1];
         const double l1 = L1.a[0], l2 = L2.a[0], cphi = PH.a[0], z = Z.a[0];
@@ -129,9 +164,9 @@ struct Model64 {
                 // src/NNMap_Model.cu:544-593
                 const Slot64 &M = *s[3];
                 const double m = M.a[0];
-                const double r2 = r200_64(m, rhot);
+                const double r2 = mz ? mz[0] : r200_64(m, rhot);  // mz[0] is this value
                 const double cc = __ldg(T.conc + z_it * Nm + M.i1);
-                const double u3 = u_nfw64(k3, r2, cc, 1);
+                const double u3 = mz ? u_nfw64_F(k3, mz[0], 1.0 * cc, mz[1]) : u_nfw64(k3, r2, cc, 1);
                 const double u2 = uc ? uc[1] : u_nfw64(k2, r2, cc, f2);
                 const double u1 = uc ? uc[0] : u_nfw64(k1, r2, cc, f1);
                 double Bggd = 1. / nbar1 / nbar2 / rho * __ldg(T.hmf + z_ix * Nm + M.i0) * m * u3;
@@ -197,11 +232,12 @@ struct Model64 {
                 // src/NMapMap_Model.cu:263-301
                 const Slot64 &M = *s[3];
                 const double m = M.a[0];
-                const double r2 = r200_64(m, rhot);
+                const double r2 = mz ? mz[0] : r200_64(m, rhot);  // mz[0] is this value
                 const double cc = __ldg(T.conc + z_it * Nm + M.i1);
                 double Bgdd = 1. / nbar / rho / rho * __ldg(T.hmf + z_ix * Nm + M.i0) * m * m *
                               (M.a[1] + M.a[2] * (uc ? uc[0] : u_nfw64(k1, r2, cc, f))) *
-                              (uc ? uc[1] : u_nfw64(k2, r2, cc, 1)) * u_nfw64(k3, r2, cc, 1);
+                              (uc ? uc[1] : u_nfw64(k2, r2, cc, 1)) *
+                              (mz ? u_nfw64_F(k3, mz[0], 1.0 * cc, mz[1]) : u_nfw64(k3, r2, cc, 1));
                 double bgkk = Bgdd / __ldg(T.dwdz + z_ix) * gz * gz * __ldg(T.p1 + z_ix) / w_ / w_ *
                               (1. + z) * (1. + z);
                 return l1 * l2 * m * l1 * l2 * L1.a[1] * L2.a[1] * U3 * bgkk / nbar;
@@ -447,6 +483,9 @@ struct Reeval {
     // the cached-u_NFW pass (measured faster for every term: it removes 2 of 3 (1h, 3h)
     // or 4 of 6 (2h) FP64 u_NFW evaluations per point)
     static constexpr bool UCACHE = true;
+    // r_200 and F per (mass, z) pair (k_re_fill) for the 1- and 2-halo terms: the 3-halo
+    // terms' 51 pairs cost about what they save
+    static constexpr bool MZ = UCACHE && TERM < 3;
     __device__ static Slot64 *slots(const Pool &P)
     {
         return (Slot64 *)(P.rscr + (long long)G * P.rscr_group);
@@ -467,6 +506,15 @@ struct Reeval {
     __device__ static double *auxv(const Pool &P)  // [rcap][AUX_MAX]
     {
         return u3v(P) + (long long)P.rcap * U3_NF_MAX * U3_MAX;
+    }
+    __device__ static double *mzv(const Pool &P)  // [rcap][3][MZ_PAIRS][MZ_VALS]
+    {
+        return auxv(P) + (long long)P.rcap * AUX_MAX;
+    }
+    __device__ static double *mz(const Pool &P, int k, int mdim, uint32_t vv)
+    {
+        const int vm = (vv >> (3 * mdim)) & 7, vz = (vv >> (3 * (DIM - 1))) & 7;
+        return mzv(P) + (((long long)k * 3 + (mdim - 3)) * MZ_PAIRS + mz_index(vm, vz)) * MZ_VALS;
     }
     // auxiliary values per entry (124 for the 2-halo terms)
     static constexpr int NAUX = aux_off(TERM, aux_nfun(TERM) - 1) + aux_count(TERM, aux_nfun(TERM) - 1);
@@ -540,9 +588,35 @@ __global__ void __launch_bounds__(128) k_re_fill(DevTables T, const IntDesc *__r
     const int2 *Q = P.esc + H->esc_beg[R::G];
     Slot64 *SL = R::slots(P);
     const long long stride = P.stride;
-    const long long tot = (long long)m * R::NS;
+    const long long tot1 = (long long)m * R::NS;
+    // then the (mass, z) pairs' r_200 and F, one thread each (their mass and bin from the
+    // same expressions as the mass slot's)
+    constexpr int NMZ = R::MZ ? TERM * MZ_PAIRS : 0;
+    const long long tot = tot1 + (long long)m * NMZ;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
          t += (long long)gridDim.x * blockDim.x) {
+        if (NMZ > 0 && t >= tot1) {
+            constexpr int NMZ1 = NMZ > 0 ? NMZ : 1;
+            const long long t2 = t - tot1;
+            const int k = (int)(t2 / NMZ1), r = (int)(t2 - (long long)k * NMZ1);
+            const int md = 3 + r / MZ_PAIRS, j = r - (md - 3) * MZ_PAIRS;
+            const int vm = mz_vm_of(j), vz = mz_vz_of(j);
+            const int2 ent = Q[k];
+            if (!(ent.y >> 30) && (vm >= 5 || vz >= 5)) continue;  // split only: no corners
+            const IntDesc &d = D[ent.x];
+            const long long slot = d.base + (ent.y & 0x3FFFFFFF);
+            constexpr int zd = R::DIM - 1;
+            Slot64 M;
+            const double xm = variant_x(P.center[md * stride + slot],
+                                        ldexp(d.hw0[md], -(int)P.level[md * stride + slot]), vm);
+            M.a[0] = pow(10, xm);
+            m_index(T, xm, M.a[0], M.i0, M.i1, nullptr);
+            const int zt = z_trunc64(T, variant_x(P.center[zd * stride + slot],
+                                                  ldexp(d.hw0[zd], -(int)P.level[zd * stride + slot]), vz));
+            Model64<KIND, TERM>::mz_values(T, d, M, zt, KIND == 0 ? 3 : 2,
+                                           R::mzv(P) + (((long long)k * 3 + (md - 3)) * MZ_PAIRS + j) * MZ_VALS);
+            continue;
+        }
         const int k = (int)(t / R::NS), r = (int)(t - (long long)k * R::NS);
         const int dim = r / NVAR, v = r - dim * NVAR;
         const int2 ent = Q[k];
@@ -551,13 +625,7 @@ __global__ void __launch_bounds__(128) k_re_fill(DevTables T, const IntDesc *__r
         const long long slot = d.base + (ent.y & 0x3FFFFFFF);
         const double c = P.center[dim * stride + slot];
         const double hw = ldexp(d.hw0[dim], -(int)P.level[dim * stride + slot]);
-        double x = c;
-        if (v > 0) {
-            double lam = (v <= 2) ? G3L_LAMBDA2 : (v <= 4 ? G3L_LAMBDA4 : G3L_LAMBDA5);
-            double rr = hw * lam;
-            x = (v & 1) ? c - rr : c + rr;
-        }
-        Model64<KIND, TERM>::fill(T, d, dim, x, SL[(long long)k * R::NS + r], &H->ties);
+        Model64<KIND, TERM>::fill(T, d, dim, variant_x(c, hw, v), SL[(long long)k * R::NS + r], &H->ties);
     }
 }
 
@@ -619,7 +687,8 @@ __global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *_
             const Slot64 *sp[R::DIM];
 #pragma unroll
             for (int dd = 0; dd < R::DIM; ++dd) sp[dd] = base + dd * NVAR + ((vv >> (3 * dd)) & 7);
-            U3C[((long long)k * U3_NF_MAX + f) * U3_MAX + j] = Model64<KIND, TERM>::u3(T, f, sp);
+            U3C[((long long)k * U3_NF_MAX + f) * U3_MAX + j] =
+                Model64<KIND, TERM>::u3(T, f, sp, R::MZ ? R::mz(P, k, u3_mass(KIND, TERM, f), vv) : nullptr);
             continue;
         }
         const int k = (int)(t / (NF * UC_MAX)), r = (int)(t - (long long)k * NF * UC_MAX);
@@ -632,7 +701,9 @@ __global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *_
         const Slot64 *base = SL + (long long)k * R::NS;
         const int dl = ucache_fun(KIND, TERM, f, 0), dm = ucache_fun(KIND, TERM, f, 1);
         UC[((long long)k * UC_NF_MAX + f) * UC_MAX + j] = Model64<KIND, TERM>::ucached(
-            T, D[ent.x], f, base[dl * NVAR + vl], base[dm * NVAR + vm], base[(R::DIM - 1) * NVAR + vz]);
+            T, D[ent.x], f, base[dl * NVAR + vl], base[dm * NVAR + vm], base[(R::DIM - 1) * NVAR + vz],
+            R::MZ ? R::mz(P, k, dm, ((uint32_t)vm << (3 * dm)) | ((uint32_t)vz << (3 * (R::DIM - 1))))
+                  : nullptr);
     }
 }
 
@@ -690,7 +761,7 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
         }
         VL[(long long)k * R::NPAD + p] = Model64<KIND, TERM>::point(
             T, d, sp, R::UCACHE ? uc : nullptr, (R::UCACHE && NU3 > 0) ? u3c : nullptr,
-            R::UCACHE ? ax : nullptr);
+            R::UCACHE ? ax : nullptr, (R::MZ && TERM == 1) ? R::mz(P, k, 3, vv) : nullptr);
     }
 }
 

@@ -175,13 +175,47 @@ __host__ __device__ constexpr uint32_t aux_keep(int term, int a)
     return k;
 }
 
+// (mass, z) quantities of the FP64 re-evaluation: r_200 and the NFW normalisation
+// F(c) = ln(1 + c) - c / (1 + c) at c = factor x concentration (factors 1, f of hod1, f of
+// hod2) depend on one halo mass and z only.  Per mass dimension a rule's points take 17
+// (mass variant, z variant) pairs -- the centre, the axis variants of either dimension
+// with the other at the centre, the (+-r4, +-r4) pairs and the (+-r5, +-r5) corners --
+// numbered by mz_index; mz_nz(vm) z variants go with mass variant vm, the i-th being
+// mz_vz(vm, i).  Per entry: [mass dimension][MZ_PAIRS][MZ_VALS] doubles.
+constexpr int MZ_PAIRS = 17;
+constexpr int MZ_VALS = 4;  // r_200, F at factor 1, f of hod1, f of hod2
+__host__ __device__ constexpr int mz_nz(int vm)
+{
+    return vm == 0 ? 5 : (vm <= 2 ? 1 : (vm <= 4 ? 3 : 2));
+}
+__host__ __device__ constexpr int mz_vz(int vm, int i)
+{
+    return vm == 0 ? i : (vm <= 2 ? 0 : (vm <= 4 ? (i == 0 ? 0 : 2 + i) : 5 + i));
+}
+__host__ __device__ constexpr int mz_vm_of(int j)
+{
+    return j < 5 ? 0 : (j < 7 ? j - 4 : (j < 13 ? 3 + (j - 7) / 3 : 5 + (j - 13) / 2));
+}
+__host__ __device__ constexpr int mz_vz_of(int j)
+{
+    return j < 5 ? j : (j < 7 ? 0 : (j < 13 ? ((j - 7) % 3 == 0 ? 0 : 2 + (j - 7) % 3) : 5 + (j - 13) % 2));
+}
+__host__ __device__ constexpr int mz_index(int vm, int vz)
+{
+    return vm == 0 ? vz
+                   : (vm <= 2 ? 4 + vm
+                              : (vm <= 4 ? 7 + 3 * (vm - 3) + (vz == 0 ? 0 : vz - 2)
+                                         : 13 + 2 * (vm - 5) + (vz - 5)));
+}
+
 // Bytes of re-evaluation scratch per group for rcap entries (any term).
 constexpr long long reeval_slot_bytes = 56;  // sizeof(Slot64)
 __host__ __device__ constexpr long long reeval_scratch_group_bytes(int rcap)
 {
     return ((long long)rcap * MAX_DIM * NVAR * reeval_slot_bytes + 255) / 256 * 256 +
            (long long)rcap * 256 * 8 + (long long)rcap * UC_NF_MAX * UC_MAX * 8 +
-           (long long)rcap * U3_NF_MAX * U3_MAX * 8 + (long long)rcap * AUX_MAX * 8;
+           (long long)rcap * U3_NF_MAX * U3_MAX * 8 + (long long)rcap * AUX_MAX * 8 +
+           (long long)rcap * 3 * MZ_PAIRS * MZ_VALS * 8;
 }
 
 // Per-call header kept in device memory so one instantiated graph serves any batch.

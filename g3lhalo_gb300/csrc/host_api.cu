@@ -427,6 +427,8 @@ struct KernelArgs {
     double tau_sel;
     double tau_val;
     int pass0 = 0, pass1 = 1;
+    int all_groups = -1;
+    int grp_id[NGROUPS] = {0, 1, 2, 3, 4, 5};
 };
 
 int add_kernel(cudaGraph_t g, cudaGraphNode_t *node, const cudaGraphNode_t *deps, size_t ndeps,
@@ -483,12 +485,15 @@ int build_graph_ws(g3l_ctx *c, Workspace &W, int precision, int gmask, bool init
     cudaGraphNode_t n_sel, n_scan, prev;
     // mixed: FP64 re-evaluations queued by a selection pass (unsettled splits of the
     // parents about to be cut, ambiguous boundary regions, polish), then the round end
-    // (one branch per group, side by side: each group reads only its own queue)
-    auto add_reevals = [&](cudaGraphNode_t &dep) -> int {
+    // (one branch per group, side by side: each group reads only its own queue).  With
+    // ends != null each group's branch gets its own end node (ends[grp]) and dep is left
+    // as it is: the rule kernel of a group then waits for its own re-evaluations only.
+    auto add_reevals = [&](cudaGraphNode_t &dep, cudaGraphNode_t *ends) -> int {
         cudaGraphNode_t br[2 * NGROUPS];
         int nbr = 0;
         for (int grp = 0; grp < NGROUPS; ++grp) {
             if (!(gmask & (1 << grp))) continue;
+            const int nbr0 = nbr;
             void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
             cudaGraphNode_t chain = dep;
             for (int ph = 0; ph < 4; ++ph) {
@@ -504,8 +509,14 @@ int build_graph_ws(g3l_ctx *c, Workspace &W, int precision, int gmask, bool init
             int st = add_kernel(body, &br[nbr], &dep, 1, fn, reeval_grid(c, fn), 128, args);
             if (st) return st;
             ++nbr;
+            if (ends) {
+                void *eargs[] = {&a.H, &a.grp_id[grp]};
+                st = add_kernel(body, &ends[grp], &br[nbr0], 2, round_end_kernel(), 1, 1, eargs);
+                if (st) return st;
+            }
         }
-        void *args[] = {&a.H};
+        if (ends) return G3L_OK;
+        void *args[] = {&a.H, &a.all_groups};
         cudaGraphNode_t n_end;
         int st = add_kernel(body, &n_end, nbr ? br : &dep, nbr ? nbr : 1, round_end_kernel(), 1,
                             1, args);
@@ -520,7 +531,7 @@ int build_graph_ws(g3l_ctx *c, Workspace &W, int precision, int gmask, bool init
     }
     prev = n_sel;
     if (precision == G3L_MIXED) {
-        int st = add_reevals(prev);
+        int st = add_reevals(prev, nullptr);
         if (st) return st;
         void *args[] = {&a.D, &a.S, &a.P, &a.H, &a.tau_sel, &a.tau_val, &a.pass1};
         cudaGraphNode_t n_sel1;
@@ -534,18 +545,22 @@ int build_graph_ws(g3l_ctx *c, Workspace &W, int precision, int gmask, bool init
         if (st) return st;
     }
     prev = n_scan;
+    cudaGraphNode_t ends[NGROUPS];
     if (precision == G3L_MIXED) {
-        int st = add_reevals(prev);
+        int st = add_reevals(prev, ends);
         if (st) return st;
     }
     // the groups' rule kernels in a chain (side-by-side branches measured slower: each
-    // kernel fills the device, and concurrent ones contend for it)
+    // kernel fills the device, and concurrent ones contend for it); a group's kernel
+    // waits for the previous one and its own re-evaluations, so the other groups'
+    // re-evaluations run beside it
     for (int grp = 0; grp < NGROUPS; ++grp) {
         if (!(gmask & (1 << grp))) continue;
         void *fn = eval_fn(c, precision, grp);
         void *args[] = {&a.T, &a.D, &a.S, &a.P, &a.H, &a.woff};
-        cudaGraphNode_t n_ev;
-        int st = add_kernel(body, &n_ev, &prev, 1, fn, eval_grid(c, fn), 128, args);
+        cudaGraphNode_t n_ev, deps[2] = {prev, ends[grp]};
+        int st = add_kernel(body, &n_ev, deps, precision == G3L_MIXED ? 2 : 1, fn,
+                            eval_grid(c, fn), 128, args);
         if (st) return st;
         prev = n_ev;
     }
@@ -633,7 +648,7 @@ int run_host_loop(g3l_ctx *c, int precision, int gmask, int *launches)
             }
         }
         G3L_CK(cudaEventRecord(c->tev[13], s));
-        void *eargs[] = {&a.H};
+        void *eargs[] = {&a.H, &a.all_groups};
         G3L_CK(cudaLaunchKernel(round_end_kernel(), dim3(1), dim3(1), eargs, 0, s));
         ++*launches;
         G3L_CK(cudaEventSynchronize(c->tev[13]));
@@ -2325,7 +2340,7 @@ int eval_static_locked(g3l_ctx *c, const g3l_integral *items, int n, int precisi
                 ++launches;
             }
         }
-        void *eargs[] = {&a.H};
+        void *eargs[] = {&a.H, &a.all_groups};
         G3L_CK(cudaLaunchKernel(round_end_kernel(), dim3(1), dim3(1), eargs, 0, s));
         ++launches;
         return G3L_OK;

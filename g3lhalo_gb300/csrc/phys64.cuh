@@ -110,11 +110,10 @@ __device__ __forceinline__ void sici64(double x, double &si, double &ci)
     sici64_sc(x, si, ci, sx, cx);
 }
 
-// NFW Fourier profile given k, r_200 and the tabulated concentration (truncated indices
-// are resolved by the caller, as in src/generalFunctions.cu:11-15).
-__device__ __forceinline__ double u_nfw64(double k, double r200, double conc, double f)
+// NFW Fourier profile from k, r_200, c = f x concentration and the normalisation
+// F = ln(1 + c) - c / (1 + c) (callers that share one (mass, z) pair pass F once computed)
+__device__ __forceinline__ double u_nfw64_F(double k, double r200, double c, double F)
 {
-    double c = f * conc;
     double arg1 = k * r200 / c;
     double arg2 = arg1 * (1 + c);
     double si1, ci1, si2, ci2, s1, c1;
@@ -123,8 +122,17 @@ __device__ __forceinline__ double u_nfw64(double k, double r200, double conc, do
     double term1 = s1 * (si2 - si1);
     double term2 = c1 * (ci2 - ci1);
     double term3 = -sin(arg1 * c) / arg2;
-    double F = log(1. + c) - c / (1. + c);
     return (term1 + term2 + term3) / F;
+}
+
+__device__ __forceinline__ double nfw_norm64(double c) { return log(1. + c) - c / (1. + c); }
+
+// NFW Fourier profile given k, r_200 and the tabulated concentration (truncated indices
+// are resolved by the caller, as in src/generalFunctions.cu:11-15).
+__device__ __forceinline__ double u_nfw64(double k, double r200, double conc, double f)
+{
+    const double c = f * conc;
+    return u_nfw64_F(k, r200, c, nfw_norm64(c));
 }
 
 __device__ __forceinline__ double r200_64(double m, double rho)
