@@ -483,9 +483,8 @@ struct Reeval {
     // the cached-u_NFW pass (measured faster for every term: it removes 2 of 3 (1h, 3h)
     // or 4 of 6 (2h) FP64 u_NFW evaluations per point)
     static constexpr bool UCACHE = true;
-    // r_200 and F per (mass, z) pair (k_re_fill) for the 1- and 2-halo terms: the 3-halo
-    // terms' 51 pairs cost about what they save
-    static constexpr bool MZ = UCACHE && TERM < 3;
+    // r_200 and F once per (mass, z) pair (k_re_fill) instead of per u_NFW call
+    static constexpr bool MZ = UCACHE;
     __device__ static Slot64 *slots(const Pool &P)
     {
         return (Slot64 *)(P.rscr + (long long)G * P.rscr_group);
