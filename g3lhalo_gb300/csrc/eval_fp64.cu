@@ -640,6 +640,12 @@ __global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *_
     __shared__ __align__(16) unsigned char tbuf[sizeof(ReTab<KIND, TERM>)];
     const int m = R::count(P, H);
     if (m == 0 || !R::UCACHE) return;
+    const long long tot1 = (long long)m * NF * UC_MAX;
+    // the k3 u_NFW of each projection (2- and 3-halo terms): after the (l, m, z) ones
+    const long long tot2 = tot1 + (long long)m * u3_nfun(TERM) * U3_MAX;
+    // the auxiliary functions of each projection: last
+    const long long tot = tot2 + (long long)m * R::NAUX;
+    if ((long long)blockIdx.x * blockDim.x >= tot) return;  // no work here: skip the tables
     const ReTab<KIND, TERM> &tb = load_retab<KIND, TERM>(P, tbuf);
     const uint32_t *sdesc = tb.sdesc;
     const uint16_t *ucl = tb.ucl;
@@ -650,11 +656,6 @@ __global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *_
     double *UC = R::ucv(P);
     double *U3C = R::u3v(P);
     double *AX = R::auxv(P);
-    const long long tot1 = (long long)m * NF * UC_MAX;
-    // the k3 u_NFW of each projection (2- and 3-halo terms): after the (l, m, z) ones
-    const long long tot2 = tot1 + (long long)m * u3_nfun(TERM) * U3_MAX;
-    // the auxiliary functions of each projection: last
-    const long long tot = tot2 + (long long)m * R::NAUX;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
          t += (long long)gridDim.x * blockDim.x) {
         if (t >= tot2) {
@@ -719,6 +720,8 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
     __shared__ __align__(16) unsigned char tbuf[sizeof(ReTab<KIND, TERM>)];
     const int m = R::count(P, H);
     if (m == 0) return;
+    const long long tot = (long long)m * R::NPAD;
+    if ((long long)blockIdx.x * blockDim.x >= tot) return;  // no work here: skip the tables
     const ReTab<KIND, TERM> &tb = load_retab<KIND, TERM>(P, tbuf);
     const uint32_t *sdesc = tb.sdesc;
     const uint8_t *ucidx = tb.ucidx, *u3rep = tb.u3rep, *auxrep = tb.auxrep;
@@ -728,7 +731,6 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
     const Slot64 *SL = R::slots(P);
     double *VL = R::vals(P);
     const double *UC = R::ucv(P);
-    const long long tot = (long long)m * R::NPAD;
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
          t += (long long)gridDim.x * blockDim.x) {
         const int k = (int)(t / R::NPAD), p = (int)(t - (long long)k * R::NPAD);
