@@ -63,8 +63,8 @@ DRAM_BYTES_PER_LAUNCH = {"nnmap_2h": 4.9e6}
 PIPES_NCU = {
     "k_evalmx<NNMap,2h> (FP32 rule)": {"fma": 35.2, "alu": 38.1, "xu_mufu": 7.7, "fp64": 8.9,
                                        "issue_active": 68.2, "warps_active": 33.6},
-    "k_re_ucache<NNMap,2h> (FP64 re-evaluation, u_NFW)": {"fp64": 72.6},
-    "k_re_points<NNMap,3h> (FP64 re-evaluation, points)": {"fp64": 49.6},
+    "k_re_ucache<NNMap,2h> (FP64 re-evaluation, u_NFW)": {"fp64": 81.0},
+    "k_re_points<NNMap,3h> (FP64 re-evaluation, points)": {"fp64": 46.3},
     "k_nbar (n_bar integrals)": {"fp64": 57.7},
     "k_pc_integrate (table precompute)": {"fp64": 79.2, "fma": 0.5, "xu_mufu": 0.1},
 }
