@@ -17,6 +17,7 @@
 #include <cmath>
 #include <condition_variable>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -78,10 +79,17 @@ int dalloc(T **p, size_t n)
 }
 
 // FP64 re-evaluation entries per group and round that take the device-wide passes
-// (4.8 kB of scratch each): 4 per integral, between 8192 (39 MB per group) and 524288
-// (2.5 GB per group); further entries take the batched kernel.
+// (10.0 kB of scratch each): 4 per integral, between 8192 (82 MB per group) and 524288
+// (5.2 GB per group); further entries take the batched kernel k_reeval64, which
+// evaluates every point on its own.  G3L_REEVAL_CAP=<n> (read when a workspace is
+// allocated) sets the count instead: 0 sends every entry through the batched kernel, so
+// that tests can hold the passes' cached values against it.
 int reeval_cap(int n_integrals)
 {
+    if (const char *e = std::getenv("G3L_REEVAL_CAP")) {
+        const long long v = std::atoll(e);
+        if (v >= 0) return (int)std::min<long long>(v, 524288);
+    }
     return (int)std::min<long long>(std::max<long long>(4ll * n_integrals, 8192), 524288);
 }
 

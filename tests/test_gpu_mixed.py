@@ -54,6 +54,29 @@ def test_mixed_matches_fp64_on_benchmark_triplets(rect, kind):
     assert np.all(_rel(b["result"], a["result"]) < TERM_RTOL)
 
 
+@pytest.mark.parametrize("kind", [G.NNMAP, G.NMAPMAP])
+def test_reevaluation_caches_match_the_batched_kernel(rect, kind, monkeypatch):
+    """The device-wide FP64 re-evaluation passes compute u_NFW, the aperture filter of
+    l3, P_lin, the bispectrum, r_200 and the NFW normalisation once per projection of the
+    rule's points (or per (mass, z) pair) and share them; the batched kernel k_reeval64
+    evaluates every point on its own.  Sending every entry through the batched kernel
+    (G3L_REEVAL_CAP=0, read when a context allocates its workspace) changes no value,
+    error or evaluation count: the cached values are bit-identical."""
+    T, c = rect
+    specs = _bench_specs(kind, step=22)
+    a = c.eval(specs, G.MIXED)
+    esc = c.stats()["escalated"]
+    assert esc > 0
+    monkeypatch.setenv("G3L_REEVAL_CAP", "0")
+    c2 = G.Context(T, clamp_k=True)
+    c2.set_hod(0, W.hod_default())
+    c2.set_hod(1, W.hod_second())
+    b = c2.eval(specs, G.MIXED)
+    assert c2.stats()["escalated"] == esc
+    for k in ("val", "err", "neval", "status"):
+        assert np.array_equal(a[k], b[k]), k
+
+
 def test_mixed_two_populations_and_sweep_hods(rect):
     """Distinct lens populations, and HODs drawn from the fitter's sweep."""
     T, _ = rect
