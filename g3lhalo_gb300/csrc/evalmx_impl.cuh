@@ -809,9 +809,6 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
         if (j >= ucn[f]) continue;
         const uint32_t key = ucl[f * UC_MAX + j];
         const int dl = ModelF<KIND, TERM>::ufun(f, 0), dm = ModelF<KIND, TERM>::ufun(f, 1);
-        // the children differ only in the split dimension: a combination that does not
-        // involve it has child 0's value (copied below)
-        if (ch && dl != sdim && dm != sdim && DIM - 1 != sdim) continue;
         const int vl = key & 7, vm = (key >> 3) & 7, vz = (key >> 6) & 7;
         auto sl = [&](int dim, int v) -> const SlotF & {
             return (ch && dim == sdim) ? slots[DIM * NVAR + v] : slots[dim * NVAR + v];
@@ -820,15 +817,6 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
             ModelF<KIND, TERM>::ucached(T, d, f, sl(dl, vl), sl(dm, vm), sl(DIM - 1, vz), small);
     }
     __syncwarp();
-    if (ModelF<KIND, TERM>::UC && nchild == 2) {
-        for (int t = lane; t < NF * UC_MAX; t += 32) {
-            const int f = t / UC_MAX, j = t - f * UC_MAX;
-            const int dl = ModelF<KIND, TERM>::ufun(f, 0), dm = ModelF<KIND, TERM>::ufun(f, 1);
-            if (j < ucn[f] && dl != sdim && dm != sdim && DIM - 1 != sdim)
-                ucache[(NF + f) * UC_MAX + j] = ucache[f * UC_MAX + j];
-        }
-        __syncwarp();
-    }
     // points
     for (int p = lane; p < nchild * NP; p += 32) {
         const int ch = p >= NP ? 1 : 0;
