@@ -51,18 +51,18 @@ RTOL = 1e-4
 # integrand with its u_NFW calls de-duplicated within a point, counted by ncu as thread-
 # level fadd + fmul + 2 ffma on the kernel version that evaluated every u_NFW per point
 # (3.434e11 over 2.2005e8 points of the benchmark).  DRAM traffic per launch (read +
-# write): three launches of the kernel on the 110-triplet case (7.3 MB per ms of kernel
-# time), scaled by duration to the benchmark's mean launch (18.55 ms / 28 launches);
+# write): three launches of the kernel on the 110-triplet case (7.9 MB per ms of kernel
+# time), scaled by duration to the benchmark's mean launch (17.65 ms / 28 launches);
 # profiles/k_evalmx_nnmap2h.md.
 FLOPS_PER_POINT = {"nnmap_2h": 1561.0}
-DRAM_BYTES_PER_LAUNCH = {"nnmap_2h": 4.9e6}
+DRAM_BYTES_PER_LAUNCH = {"nnmap_2h": 5.0e6}
 # Pipe utilisation (% of peak while the SMs are active) of the dominant kernels, from one
 # `ncu --set full` capture of three launches each (profiles/k_evalmx_nnmap2h.md,
 # profiles/k_re_points_nnmap3h.md, profiles/k_nbar_densities.md,
 # profiles/k_pc_integrate_precompute.md).
 PIPES_NCU = {
-    "k_evalmx<NNMap,2h> (FP32 rule)": {"fma": 35.2, "alu": 38.1, "xu_mufu": 7.7, "fp64": 8.9,
-                                       "issue_active": 68.2, "warps_active": 33.6},
+    "k_evalmx<NNMap,2h> (FP32 rule)": {"fma": 38.7, "alu": 36.6, "xu_mufu": 8.1, "fp64": 9.1,
+                                       "issue_active": 70.5, "warps_active": 33.4},
     "k_re_ucache<NNMap,2h> (FP64 re-evaluation, u_NFW)": {"fp64": 81.0},
     "k_re_points<NNMap,3h> (FP64 re-evaluation, points)": {"fp64": 46.3},
     "k_nbar (n_bar integrals)": {"fp64": 57.7},
