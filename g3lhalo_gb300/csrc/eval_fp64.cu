@@ -480,8 +480,8 @@ struct Reeval {
     static constexpr int NS = DIM * NVAR;
     static constexpr int NPAD = (NP + 31) / 32 * 32;
     static constexpr int G = KIND * 3 + TERM - 1;
-    // the cached-u_NFW pass (measured faster for every term: it removes 2 of 3 (1h, 3h)
-    // or 4 of 6 (2h) FP64 u_NFW evaluations per point)
+    // the pass of cached values (measured faster for every term): the points then
+    // evaluate no FP64 u_NFW of their own except the 1-halo terms' k3 one
     static constexpr bool UCACHE = true;
     // r_200 and F once per (mass, z) pair (k_re_fill) instead of per u_NFW call
     static constexpr bool MZ = UCACHE;
