@@ -38,6 +38,26 @@ __device__ __forceinline__ int z_trunc64(const DevTables &T, double x)
     return min(max((int)zr, 0), T.Nz - 1);
 }
 
+// An FP64 re-take of an unsettled split (a split-only entry) needs the centre and the axis
+// points of the contending dimensions only: cm, the dimensions whose fourth-difference
+// bounds reach the leader's (P.cmask, written by the FP32 rule kernel with the flag).  The
+// others' differences are below the leader's under those bounds, so the FP64 choice among
+// the contenders is the FP64 choice among all dimensions.
+__device__ __forceinline__ unsigned split_cmask(const Pool &P, const IntDesc &d, int2 ent)
+{
+    return (unsigned)P.cmask[d.base + (ent.y & 0x3FFFFFFF)];
+}
+// coordinate variant v of dimension dim (centre, or an axis variant of a contender)
+__device__ __forceinline__ bool split_variant(unsigned cm, int dim, int v)
+{
+    return v == 0 || (v < 5 && ((cm >> dim) & 1u));
+}
+// rule point p (the centre, or an axis point of a contender; nax = 1 + 4 dim)
+__device__ __forceinline__ bool split_point(unsigned cm, int p, int nax)
+{
+    return p == 0 || (p < nax && ((cm >> ((p - 1) >> 2)) & 1u));
+}
+
 template <int KIND, int TERM>
 struct Model64 {
     static constexpr int DIM = TERM + 4;
@@ -601,10 +621,13 @@ __global__ void __launch_bounds__(128) k_re_fill(DevTables T, const IntDesc *__r
             const int md = 3 + r / MZ_PAIRS, j = r - (md - 3) * MZ_PAIRS;
             const int vm = mz_vm_of(j), vz = mz_vz_of(j);
             const int2 ent = Q[k];
-            if (!(ent.y >> 30) && (vm >= 5 || vz >= 5)) continue;  // split only: no corners
             const IntDesc &d = D[ent.x];
-            const long long slot = d.base + (ent.y & 0x3FFFFFFF);
             constexpr int zd = R::DIM - 1;
+            if (!(ent.y >> 30)) {  // split only: the centre and the contenders' axis variants
+                const unsigned cm = split_cmask(P, d, ent);
+                if ((vm && vz) || !split_variant(cm, md, vm) || !split_variant(cm, zd, vz)) continue;
+            }
+            const long long slot = d.base + (ent.y & 0x3FFFFFFF);
             Slot64 M;
             const double xm = variant_x(P.center[md * stride + slot],
                                         ldexp(d.hw0[md], -(int)P.level[md * stride + slot]), vm);
@@ -619,8 +642,9 @@ __global__ void __launch_bounds__(128) k_re_fill(DevTables T, const IntDesc *__r
         const int k = (int)(t / R::NS), r = (int)(t - (long long)k * R::NS);
         const int dim = r / NVAR, v = r - dim * NVAR;
         const int2 ent = Q[k];
-        if (!(ent.y >> 30) && v >= 5) continue;  // split only: variants c, -+r2, -+r4
         const IntDesc &d = D[ent.x];
+        // split only: the centre of every dimension, the contenders' axis variants
+        if (!(ent.y >> 30) && !split_variant(split_cmask(P, d, ent), dim, v)) continue;
         const long long slot = d.base + (ent.y & 0x3FFFFFFF);
         const double c = P.center[dim * stride + slot];
         const double hw = ldexp(d.hw0[dim], -(int)P.level[dim * stride + slot]);
@@ -665,7 +689,8 @@ __global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *_
             while (a + 1 < aux_nfun(TERM) && r >= aux_off(TERM, a + 1)) ++a;
             const int pr = auxlist[r];
             const int2 ent = Q[k];
-            if (!(ent.y >> 30) && pr >= R::NAX) continue;  // split only: axis points
+            // split only: the projections of the centre and the contenders' axis points
+            if (!(ent.y >> 30) && !split_point(split_cmask(P, D[ent.x], ent), pr, R::NAX)) continue;
             const uint32_t vv = sdesc[pr];
             const Slot64 *base = SL + (long long)k * R::NS;
             const Slot64 *sp[R::DIM];
@@ -681,7 +706,7 @@ __global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *_
             const int f = r / U3_MAX, j = r - f * U3_MAX;
             const int pr = u3list[f * U3_MAX + j];  // every projection index is used (93)
             const int2 ent = Q[k];
-            if (!(ent.y >> 30) && pr >= R::NAX) continue;  // split only: axis points
+            if (!(ent.y >> 30) && !split_point(split_cmask(P, D[ent.x], ent), pr, R::NAX)) continue;
             const uint32_t vv = sdesc[pr];
             const Slot64 *base = SL + (long long)k * R::NS;
             const Slot64 *sp[R::DIM];
@@ -697,9 +722,14 @@ __global__ void __launch_bounds__(128) k_re_ucache(DevTables T, const IntDesc *_
         const int2 ent = Q[k];
         const uint32_t key = ucl[f * UC_MAX + j];
         const int vl = key & 7, vm = (key >> 3) & 7, vz = (key >> 6) & 7;
-        if (!(ent.y >> 30) && (vl >= 5 || vm >= 5 || vz >= 5)) continue;
-        const Slot64 *base = SL + (long long)k * R::NS;
         const int dl = ucache_fun(KIND, TERM, f, 0), dm = ucache_fun(KIND, TERM, f, 1);
+        if (!(ent.y >> 30)) {  // split only: combinations of the centre and one contender axis
+            const unsigned cm = split_cmask(P, D[ent.x], ent);
+            if ((vl != 0) + (vm != 0) + (vz != 0) > 1 || !split_variant(cm, dl, vl) ||
+                !split_variant(cm, dm, vm) || !split_variant(cm, R::DIM - 1, vz))
+                continue;
+        }
+        const Slot64 *base = SL + (long long)k * R::NS;
         UC[((long long)k * UC_NF_MAX + f) * UC_MAX + j] = Model64<KIND, TERM>::ucached(
             T, D[ent.x], f, base[dl * NVAR + vl], base[dm * NVAR + vm], base[(R::DIM - 1) * NVAR + vz],
             R::MZ ? R::mz(P, k, dm, ((uint32_t)vm << (3 * dm)) | ((uint32_t)vz << (3 * (R::DIM - 1))))
@@ -735,8 +765,9 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
          t += (long long)gridDim.x * blockDim.x) {
         const int k = (int)(t / R::NPAD), p = (int)(t - (long long)k * R::NPAD);
         const int2 ent = Q[k];
-        if (p >= ((ent.y >> 30) ? R::NP : R::NAX)) continue;
+        if (p >= R::NP) continue;
         const IntDesc &d = D[ent.x];
+        if (!(ent.y >> 30) && !split_point(split_cmask(P, d, ent), p, R::NAX)) continue;
         const uint32_t vv = sdesc[p];
         const Slot64 *base = SL + (long long)k * R::NS;
         const Slot64 *sp[DIM];
@@ -769,7 +800,7 @@ __global__ void __launch_bounds__(128) k_re_points(DevTables T, const IntDesc *_
 // the sums of one re-evaluated region (vl: its rule-point values)
 template <int DIM>
 __device__ void reeval_finish(const IntDesc &d, const Pool &P, long long slot, bool full,
-                              const double *vl)
+                              const double *vl, unsigned cm)
 {
     const long long stride = P.stride;
     if (full) {
@@ -789,6 +820,7 @@ __device__ void reeval_finish(const IntDesc &d, const Pool &P, long long slot, b
         double maxdiff = 0;
         int dimDiffMax = 0;
         for (int q = 0; q < DIM; ++q) {
+            if (!((cm >> q) & 1u)) continue;  // not a contender (its points were not taken)
             double v0 = vl[1 + 4 * q], v1 = vl[2 + 4 * q];
             double v2 = vl[3 + 4 * q], v3 = vl[4 + 4 * q];
             double diff = 0;
@@ -815,7 +847,7 @@ __global__ void __launch_bounds__(128) k_re_combine(DevTables T, const IntDesc *
         const int2 ent = Q[k];
         const IntDesc &d = D[ent.x];
         reeval_finish<R::DIM>(d, P, d.base + (ent.y & 0x3FFFFFFF), (ent.y >> 30) != 0,
-                              VL + (long long)k * R::NPAD);
+                              VL + (long long)k * R::NPAD, (ent.y >> 30) ? 0u : split_cmask(P, d, ent));
     }
 }
 
@@ -854,8 +886,8 @@ __global__ void __launch_bounds__(128) k_reeval64(DevTables T, const IntDesc *__
             const int k = t / NS, r = t - k * NS;
             const int dim = r / NVAR, v = r - dim * NVAR;
             const int2 ent = sent[k];
-            if (!(ent.y >> 30) && v >= 5) continue;
             const IntDesc &d = D[ent.x];
+            if (!(ent.y >> 30) && !split_variant(split_cmask(P, d, ent), dim, v)) continue;
             const long long slot = d.base + (ent.y & 0x3FFFFFFF);
             const double c = P.center[dim * stride + slot];
             const double hw = ldexp(d.hw0[dim], -(int)P.level[dim * stride + slot]);
@@ -879,6 +911,7 @@ __global__ void __launch_bounds__(128) k_reeval64(DevTables T, const IntDesc *__
             for (int q = 1; q < RB; ++q) k += t >= pb[q] ? 1 : 0;
             const int p = t - pb[k];
             const IntDesc &d = D[sent[k].x];
+            if (!(sent[k].y >> 30) && !split_point(split_cmask(P, d, sent[k]), p, NAX)) continue;
             const uint32_t vv = sdesc[p];
             const Slot64 *sp[DIM];
 #pragma unroll
@@ -890,7 +923,7 @@ __global__ void __launch_bounds__(128) k_reeval64(DevTables T, const IntDesc *__
             const int2 ent = sent[threadIdx.x];
             const IntDesc &d = D[ent.x];
             reeval_finish<DIM>(d, P, d.base + (ent.y & 0x3FFFFFFF), (ent.y >> 30) != 0,
-                               vals[threadIdx.x]);
+                               vals[threadIdx.x], (ent.y >> 30) ? 0u : split_cmask(P, d, ent));
         }
     }
 }

@@ -917,6 +917,12 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
     // decisive when the gap between the two largest differences exceeds both bounds
     const bool split_sure = (best.hi - fmaxf(second.hi, 0.f)) > (ubest + usecond) &&
                             best.hi > ubest;
+    // the contenders: dimensions whose difference may reach the leader's under the bounds
+    // (an FP64 re-take of an unsettled split evaluates only their axis points)
+    const unsigned cbits = __ballot_sync(
+        0xffffffffu, active && hl < DIM &&
+                         diff.hi + udiff >= (best.hi - ubest) - 1e-6f * fabsf(best.hi));
+    const unsigned cmask = (cbits >> (16 * hh)) & ((1u << DIM) - 1u);
     // 7th- and 5th-degree brackets (double-float), then FP64 on four lanes
     df b7 = df_mul_f({df_hi_of(W::w1), df_lo_of(W::w1)}, val0);
     b7 = df_add(b7, df_mul(s2, {df_hi_of(W::w2), df_lo_of(W::w2)}));
@@ -958,6 +964,7 @@ __device__ void warp_itemF(const DevTables &T, const IntDesc &d, int iint, doubl
             // in FP64 only if the region is selected for cutting, so leaves never pay.
             const bool flag = !split_sure && out > T.tau_impact * fabs(Vcur);
             P.split[slot] = (unsigned char)(sidx | (flag ? 0x80 : 0));
+            P.cmask[slot] = (unsigned char)cmask;
         }
     }
     // child geometry

@@ -107,6 +107,10 @@ struct Pool {
     unsigned char *level;
     double *val, *err;
     unsigned char *split;
+    // mixed path: the dimensions whose fourth-difference bounds reach the leader's (bit
+    // per dimension), written with an unsettled split; its FP64 re-take evaluates only
+    // their axis points
+    unsigned char *cmask;
     unsigned long long *q;  // fixed-point errors (selection scratch)
     int *cand;              // selected parents, per-integral segment at base
     float *unc;             // mixed path: bound on the FP32 error of err, relative (0 = FP64)

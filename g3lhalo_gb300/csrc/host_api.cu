@@ -333,7 +333,7 @@ bool finite_all(const double *a, size_t n)
 
 void free_workspace(Workspace &W)
 {
-    void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.q, W.P.cand,
+    void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.cmask, W.P.q, W.P.cand,
                     W.P.unc,    W.P.esc,   W.P.uval, W.P.key, W.P.rscr, W.D, W.S, W.woff, W.H};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -353,6 +353,7 @@ int alloc_workspace(Workspace &W, int ncap, size_t pcap, const unsigned char *re
     st |= dalloc(&W.P.val, pcap);
     st |= dalloc(&W.P.err, pcap);
     st |= dalloc(&W.P.split, pcap);
+    st |= dalloc(&W.P.cmask, pcap);
     st |= dalloc(&W.P.q, pcap);
     st |= dalloc(&W.P.cand, pcap);
     st |= dalloc(&W.P.unc, pcap);
@@ -1393,7 +1394,7 @@ void g3l_ctx_destroy(g3l_ctx *c)
         cudaGraphDestroy(g.graph);
     }
     Workspace &W = c->W;
-    void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.q, W.P.cand,
+    void *ptrs[] = {W.P.center, W.P.level, W.P.val, W.P.err, W.P.split, W.P.cmask, W.P.q, W.P.cand,
                     W.P.unc,    W.P.esc,   W.P.uval, W.P.key, W.P.rscr, W.D, W.S, W.woff, W.H};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -2193,7 +2194,7 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // Bytes of scratch a call with n integrals and `pool` region slots needs, and the
 // offsets of its arrays (same arrays as the context workspace).
 struct StaticLayout {
-    size_t H, D, S, woff, center, level, val, err, split, q, cand, unc, uval, key, esc, rscr, end;
+    size_t H, D, S, woff, center, level, val, err, split, cmask, q, cand, unc, uval, key, esc, rscr, end;
 };
 
 StaticLayout static_layout(int n, size_t pool)
@@ -2209,6 +2210,7 @@ StaticLayout static_layout(int n, size_t pool)
     L.val = o;    o = align256(o + sizeof(double) * pool);
     L.err = o;    o = align256(o + sizeof(double) * pool);
     L.split = o;  o = align256(o + pool);
+    L.cmask = o;  o = align256(o + pool);
     L.q = o;      o = align256(o + sizeof(unsigned long long) * pool);
     L.cand = o;   o = align256(o + sizeof(int) * pool);
     L.unc = o;    o = align256(o + sizeof(float) * pool);
@@ -2310,6 +2312,7 @@ int eval_static_locked(g3l_ctx *c, const g3l_integral *items, int n, int precisi
     a.P.val = (double *)(base + L.val);
     a.P.err = (double *)(base + L.err);
     a.P.split = base + L.split;
+    a.P.cmask = base + L.cmask;
     a.P.q = (unsigned long long *)(base + L.q);
     a.P.cand = (int *)(base + L.cand);
     a.P.unc = (float *)(base + L.unc);
