@@ -304,8 +304,8 @@ int g3l_debug_region(g3l_ctx *ctx, const g3l_integral *item, const double *cente
  * allocator, or a loop that cannot take an allocation's implicit synchronisation.
  *  - Scratch: one fixed 64 MiB device array per device, built into the library.  A
  *    call may hold at most 1024 integrals and as many region slots as fit beside them
- *    and the ~31 MB of re-evaluation scratch (about 116 bytes per slot; each integral
- *    takes 3 + (max_eval + P) / (2 P) slots for its P-point rule, so ~310k slots, e.g.
+ *    and the ~31 MB of re-evaluation scratch (about 117 bytes per slot; each integral
+ *    takes 3 + (max_eval + P) / (2 P) slots for its P-point rule, so ~305k slots, e.g.
  *    145 seven-dimensional integrals at max_eval = 1e6).  An item with max_eval = 0
  *    takes the context's unlimited_pool slots (g3l_options; 1 << 20 by default, more
  *    than the scratch holds), so such items need unlimited_pool lowered to ~300k or
