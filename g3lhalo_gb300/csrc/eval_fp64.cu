@@ -47,16 +47,6 @@ __device__ __forceinline__ unsigned split_cmask(const Pool &P, const IntDesc &d,
 {
     return (unsigned)P.cmask[d.base + (ent.y & 0x3FFFFFFF)];
 }
-// coordinate variant v of dimension dim (centre, or an axis variant of a contender)
-__device__ __forceinline__ bool split_variant(unsigned cm, int dim, int v)
-{
-    return v == 0 || (v < 5 && ((cm >> dim) & 1u));
-}
-// rule point p (the centre, or an axis point of a contender; nax = 1 + 4 dim)
-__device__ __forceinline__ bool split_point(unsigned cm, int p, int nax)
-{
-    return p == 0 || (p < nax && ((cm >> ((p - 1) >> 2)) & 1u));
-}
 
 template <int KIND, int TERM>
 struct Model64 {

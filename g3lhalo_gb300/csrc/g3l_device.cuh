@@ -212,6 +212,19 @@ __host__ __device__ constexpr int mz_index(int vm, int vz)
                                          : 13 + 2 * (vm - 5) + (vz - 5)));
 }
 
+// An FP64 re-take of an unsettled split reads the centre and the axis points of the
+// contending dimensions cm (bit per dimension) only.  Whether it needs coordinate
+// variant v of dimension dim (the centre, or an axis variant of a contender):
+__host__ __device__ inline bool split_variant(unsigned cm, int dim, int v)
+{
+    return v == 0 || (v < 5 && ((cm >> dim) & 1u));
+}
+// and rule point p (the centre, or an axis point of a contender; nax = 1 + 4 dim)
+__host__ __device__ inline bool split_point(unsigned cm, int p, int nax)
+{
+    return p == 0 || (p < nax && ((cm >> ((p - 1) >> 2)) & 1u));
+}
+
 // Bytes of re-evaluation scratch per group for rcap entries (any term).
 constexpr long long reeval_slot_bytes = 56;  // sizeof(Slot64)
 __host__ __device__ constexpr long long reeval_scratch_group_bytes(int rcap)
